@@ -1,0 +1,282 @@
+#!/usr/bin/env python
+"""H.psi throughput of the Smolyak SG4 D=6 L=8 workload on one GB300.
+
+One step = one H.psi block: H applied to 64 FP64 vectors of the D=6, L=8 Smolyak basis
+(nb(l)=2l+1, nq(l)=2l+3, 2975 terms, 40,081 packed functions, 37.8 M grid points),
+type-10 KEO with G(Q) = 1 + g.q and a cubic+quartic potential, all drawn from a fixed
+seed (synthetic inputs with the benchmark's shapes and distributions).
+
+  value  : FP64 H.psi/s with the vectors resident in HBM (device entry point)
+  e2e    : FP64 H.psi/s through the host entry point evr_hpsi_host with pinned host
+           buffers (copies in and out inside the timed region)
+  mixed  : the FP32-contraction path on the same block, with its error against FP64
+  roofline: the term-pipeline kernel (hpsi_items_kernel) against the measured FP64 GEMM
+           rate of this GPU (cuBLAS DGEMM, measured in this run)
+  cpu_baseline / --impl reference: the CPU oracle (C++/OpenMP restatement of the
+           reference's OpPsi) on the host cores, bounded to a sample of the block.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, os.path.join(ROOT, "elvibrot-tnumtana_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "H.psi/s (OpPsi on SG4 D=6 L=8, 64-vector block)"
+UNIT = "Hpsi/s"
+NVEC = 64
+
+
+def workload_config(p=None):
+    cfg = {"workload": "OpPsi block: SG4 D=6 L=8, nb(l)=2l+1, nq(l)=2l+3, type-10 KEO, 64 vectors",
+           "nvec": NVEC, "seed": 1, "l2": "flushed between timed steps (512 MB write)"}
+    if p is not None:
+        cfg.update({"N": int(p.N), "terms": int(p.nterm), "grid_points": int(p.sum_nq),
+                    "gflop_per_hpsi": round(p.flop_per_hpsi / 1e9, 4)})
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.out = ""
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = [r.split(",") for r in self.out.strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if "Active" in v and "Not" not in v})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_oracle_rate(spec, nvec_sample, threads):
+    """Oracle H.psi/s on the host cores for a bounded sample of the block."""
+    from oracle import oracle as O
+
+    op = O.OracleProblem(spec)
+    rng = np.random.default_rng(0)
+    psi = rng.standard_normal((op.N, nvec_sample))
+    op.hpsi(psi[:, :1], nthreads=threads)  # grid set-up outside the timing
+    t0 = time.perf_counter()
+    op.hpsi(psi, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return nvec_sample / dt, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    from evrgpu import spec as S
+
+    spec = S.config_sg4_6d_l8()
+    threads = os.cpu_count() or 1
+    rates = []
+    for i in range(args.warmup + args.steps):
+        r, _ = cpu_oracle_rate(spec, 1, threads)
+        if i >= args.warmup:
+            rates.append(r)
+    v = statistics.median(rates)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": workload_config(),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "1 vector of the 64-vector block per step (the reference's Fortran "
+                                       "cannot be built here: no Fortran compiler)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def measure_dgemm_tflops(torch, dtype, n=4096, reps=5):
+    a = torch.randn(n, n, dtype=dtype, device="cuda")
+    b = torch.randn(n, n, dtype=dtype, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from evrgpu import Problem, spec as S
+    import evrgpu.lib as E
+
+    spec = S.config_sg4_6d_l8()
+    p = Problem(spec, device=local)
+    N = p.N
+    g = torch.Generator(device="cuda").manual_seed(1234 + rank)
+    x = torch.randn((N, NVEC), dtype=torch.float64, device="cuda", generator=g)
+    y = torch.empty_like(x)
+    y32 = torch.empty_like(x)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def step(prec, out):
+        p.hpsi_device(x.data_ptr(), NVEC, out.data_ptr(), NVEC, NVEC, layout=E.LAYOUT_INTERLEAVED, prec=prec,
+                      stream=stream)
+
+    for _ in range(args.warmup):
+        step("fp64", y)
+        step("fp32", y32)
+    torch.cuda.synchronize()
+
+    def timed(prec, out):
+        times, kms = [], []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            if world > 1:
+                torch.distributed.barrier()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            step(prec, out)
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            kms.append(p.last_kernel_ms())
+        return times, kms
+
+    with ClockSampler(local) as clk:
+        t64, k64 = timed("fp64", y)
+        t32, k32 = timed("fp32", y32)
+    total64 = sum(t64)
+    if world > 1:
+        tt = torch.tensor([total64], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total64 = float(tt.item())
+    value = world * NVEC * args.steps / total64
+    mixed = NVEC * args.steps / sum(t32)
+    err32 = float((y32 - y).abs().max() / y.abs().max())
+
+    # end to end through the host entry point with pinned buffers (column-major, as the
+    # Fortran host passes TabPsi(:)%RvecB)
+    hx = torch.empty((NVEC, N), dtype=torch.float64).pin_memory()
+    hx.copy_(x.t().cpu())
+    hy = torch.empty((NVEC, N), dtype=torch.float64).pin_memory()
+    p.hpsi_host_ptr(hx.data_ptr(), N, hy.data_ptr(), N, NVEC, E.LAYOUT_COLMAJOR)
+    te = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p.hpsi_host_ptr(hx.data_ptr(), N, hy.data_ptr(), N, NVEC, E.LAYOUT_COLMAJOR)
+        te.append(time.perf_counter() - t0)
+    e2e = NVEC * args.steps / sum(te)
+    e2e_err = float((hy.t().cuda() - y).abs().max() / y.abs().max())
+
+    # roofline of the dominant kernel
+    items_ms = statistics.mean(k[0] for k in k64)
+    flop_launch = p.flop_per_hpsi * NVEC
+    achieved = flop_launch / (items_ms / 1e3) / 1e12
+    peak64 = measure_dgemm_tflops(torch, torch.float64)
+    items32 = statistics.mean(k[0] for k in k32)
+    torch.backends.cuda.matmul.allow_tf32 = False
+    peak32 = measure_dgemm_tflops(torch, torch.float32)
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total64 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": workload_config(p),
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(N * NVEC * 8),
+                    "d2h_bytes_per_step": int(N * NVEC * 8), "rel_err_vs_device": e2e_err},
+            "mixed": {"value": mixed, "unit": UNIT, "dtype": "f32 contractions, f64 reduction",
+                      "rel_err_vs_fp64": err32, "items_kernel_ms": items32,
+                      "achieved_tflops": flop_launch / (items32 / 1e3) / 1e12, "fp32_sgemm_tflops": peak32},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+                         "frac": achieved / peak64, "traffic": None,
+                         "kernel": "hpsi_items_kernel<double>", "items_kernel_ms": items_ms,
+                         "algorithmic_flop_per_launch": flop_launch,
+                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in the "
+                                        "driver's peak file)"},
+            "gpu_launches": 2 * args.steps,
+            "clocks": clk.summary()}
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        r, dt = cpu_oracle_rate(spec, 1, threads)
+        line["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"1 vector of the block ({dt:.1f} s), CPU oracle with OpenMP over terms"}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

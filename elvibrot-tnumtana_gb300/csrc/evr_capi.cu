@@ -1,0 +1,196 @@
+// evr_capi.cu -- the C ABI of include/evr_gpu.h: context life cycle, table read-back,
+// H.psi entry points.  Davidson and Chebyshev drivers live in evr_davidson.cu and
+// evr_propagate.cu.
+#include <algorithm>
+#include <cstring>
+#include <new>
+
+#include "evr_internal.h"
+
+using namespace evr;
+
+#define EVR_CU(call, what)                              \
+  do {                                                  \
+    int _rc = cuda_check(c, (call), what);              \
+    if (_rc != EVR_OK) return _rc;                      \
+  } while (0)
+
+extern "C" {
+
+int evr_create(evr_ctx** out, const evr_problem_desc* desc, int device) {
+  if (!out) return EVR_EINVAL;
+  *out = nullptr;
+  evr_ctx* c = new (std::nothrow) evr_ctx();
+  if (!c) return EVR_ENOMEM;
+  c->device = device;
+  if (device < 0) {  // host-only context: tables are built and can be read back, no device work
+    *out = c;
+    c->host_only = true;
+    return build_host_problem(desc, c->hp, c->err);
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    (void)cudaGetLastError();
+    c->err = "no CUDA device " + std::to_string(device);
+    *out = c;
+    return EVR_EDEVICE;
+  }
+  *out = c;
+  EVR_CU(cudaSetDevice(device), "cudaSetDevice");
+  EVR_CU(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device), "attr");
+  EVR_CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  for (auto& e : c->ev) EVR_CU(cudaEventCreate(&e), "cudaEventCreate");
+  int rc = build_host_problem(desc, c->hp, c->err);
+  if (rc) return rc;
+  rc = upload_problem(c);
+  return rc;
+}
+
+int evr_destroy(evr_ctx* c) {
+  if (!c) return EVR_OK;
+  if (c->host_only) { delete c; return EVR_OK; }
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_workspace(c);
+  free_problem(c);
+  if (c->pinned) cudaFreeHost(c->pinned);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  delete c;
+  return EVR_OK;
+}
+
+const char* evr_last_error(const evr_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int evr_sizes(const evr_ctx* c, evr_sizes_t* o) {
+  if (!c || !o) return EVR_EINVAL;
+  const HostProblem& P = c->hp;
+  o->Np = P.Np;
+  o->N = P.Np * P.nb0;
+  o->n_terms = (int64_t)P.terms.size();
+  o->sum_nb = P.sum_nb;
+  o->sum_nq = P.sum_nq;
+  o->max_nq_term = P.max_nq;
+  o->flop_per_hpsi = P.flop_per_hpsi;
+  return EVR_OK;
+}
+
+int evr_get_tables(const evr_ctx* c, int* term_l, double* weight, int* map, int* packed) {
+  if (!c) return EVR_EINVAL;
+  const HostProblem& P = c->hp;
+  if (term_l) std::copy(P.term_l.begin(), P.term_l.end(), term_l);
+  if (weight) std::copy(P.weight.begin(), P.weight.end(), weight);
+  if (map) std::copy(P.map.begin(), P.map.end(), map);
+  if (packed) std::copy(P.packed.begin(), P.packed.end(), packed);
+  return EVR_OK;
+}
+
+int evr_get_basis(const evr_ctx* c, int mode, int level, int* nb_nq, double* x, double* w, double* d0b, double* d1b,
+                  double* d2b, double* bgw, double* d1gg, double* d2gg) {
+  if (!c || mode < 0 || mode >= c->hp.D || level < 0 || level >= (int)c->hp.bas[mode].size() || !nb_nq)
+    return EVR_EINVAL;
+  const Basis1D& b = c->hp.bas[mode][level];
+  nb_nq[0] = b.nb;
+  nb_nq[1] = b.nq;
+  auto cp = [](const std::vector<double>& v, double* d) {
+    if (d) std::copy(v.begin(), v.end(), d);
+  };
+  cp(b.x, x); cp(b.w, w); cp(b.d0b, d0b); cp(b.d1b, d1b); cp(b.d2b, d2b); cp(b.bgw, bgw); cp(b.d1gg, d1gg);
+  cp(b.d2gg, d2gg);
+  return EVR_OK;
+}
+
+int evr_get_vgrid(const evr_ctx* c0, double* v) {
+  evr_ctx* c = const_cast<evr_ctx*>(c0);
+  if (!c || !v) return EVR_EINVAL;
+  if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
+  EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
+  const size_t n = (size_t)c->hp.sum_nq * c->hp.nb0 * c->hp.nb0;
+  EVR_CU(cudaMemcpyAsync(v, c->dp.vgrid, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "copy vgrid");
+  EVR_CU(cudaStreamSynchronize(c->stream), "sync");
+  return EVR_OK;
+}
+
+int evr_hpsi_device(evr_ctx* c, const double* psi, int64_t ld_psi, double* hpsi, int64_t ld_hpsi, int nvec, int layout,
+                    int prec, void* stream) {
+  if (!c) return EVR_EINVAL;
+  if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
+  if (!psi || !hpsi || nvec < 1) return set_error(c, EVR_EINVAL, "evr_hpsi_device: null pointer or nvec < 1");
+  if (prec != EVR_PREC_FP64 && prec != EVR_PREC_FP32) return set_error(c, EVR_EINVAL, "unknown precision");
+  const int64_t N = c->hp.Np * c->hp.nb0;
+  cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+  EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
+  if (layout == EVR_LAYOUT_INTERLEAVED) {
+    if (ld_psi < nvec || ld_hpsi < nvec) return set_error(c, EVR_EINVAL, "interleaved ld < nvec");
+    return hpsi_interleaved(c, psi, ld_psi, hpsi, ld_hpsi, nvec, prec, s);
+  }
+  if (layout != EVR_LAYOUT_COLMAJOR) return set_error(c, EVR_EINVAL, "unknown layout");
+  if (ld_psi < N || ld_hpsi < N) return set_error(c, EVR_EINVAL, "column-major ld < N");
+  int rc = ensure_workspace(c, nvec, prec);
+  if (rc) return rc;
+  double* xin = (double*)c->ws.xin;
+  double* xout = (double*)c->ws.xout;
+  if ((rc = transpose_to_interleaved(psi, ld_psi, xin, nvec, N, nvec, s))) return set_error(c, rc, "transpose");
+  if ((rc = hpsi_interleaved(c, xin, nvec, xout, nvec, nvec, prec, s))) return rc;
+  if ((rc = transpose_from_interleaved(xout, nvec, hpsi, ld_hpsi, N, nvec, s))) return set_error(c, rc, "transpose");
+  c->last_kernels += 2;
+  return EVR_OK;
+}
+
+int evr_hpsi_host(evr_ctx* c, const double* psi, int64_t ld_psi, double* hpsi, int64_t ld_hpsi, int nvec, int layout,
+                  int prec) {
+  if (!c) return EVR_EINVAL;
+  if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
+  if (!psi || !hpsi || nvec < 1) return set_error(c, EVR_EINVAL, "evr_hpsi_host: null pointer or nvec < 1");
+  const int64_t N = c->hp.Np * c->hp.nb0;
+  EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
+  int rc = ensure_workspace(c, nvec, prec);
+  if (rc) return rc;
+  double* xin = (double*)c->ws.xin;
+  double* xout = (double*)c->ws.xout;
+  cudaStream_t s = c->stream;
+  if (layout == EVR_LAYOUT_INTERLEAVED) {
+    if (ld_psi < nvec || ld_hpsi < nvec) return set_error(c, EVR_EINVAL, "interleaved ld < nvec");
+    EVR_CU(cudaMemcpy2DAsync(xin, nvec * sizeof(double), psi, ld_psi * sizeof(double), nvec * sizeof(double), N,
+                             cudaMemcpyHostToDevice, s), "H2D");
+    if ((rc = hpsi_interleaved(c, xin, nvec, xout, nvec, nvec, prec, s))) return rc;
+    EVR_CU(cudaMemcpy2DAsync(hpsi, ld_hpsi * sizeof(double), xout, nvec * sizeof(double), nvec * sizeof(double), N,
+                             cudaMemcpyDeviceToHost, s), "D2H");
+  } else if (layout == EVR_LAYOUT_COLMAJOR) {
+    if (ld_psi < N || ld_hpsi < N) return set_error(c, EVR_EINVAL, "column-major ld < N");
+    // column-major staging in xout, transposed on the device into xin
+    EVR_CU(cudaMemcpy2DAsync(xout, N * sizeof(double), psi, ld_psi * sizeof(double), N * sizeof(double), nvec,
+                             cudaMemcpyHostToDevice, s), "H2D");
+    if ((rc = transpose_to_interleaved(xout, N, xin, nvec, N, nvec, s))) return set_error(c, rc, "transpose");
+    if ((rc = hpsi_interleaved(c, xin, nvec, xout, nvec, nvec, prec, s))) return rc;
+    if ((rc = transpose_from_interleaved(xout, nvec, xin, N, N, nvec, s))) return set_error(c, rc, "transpose");
+    EVR_CU(cudaMemcpy2DAsync(hpsi, ld_hpsi * sizeof(double), xin, N * sizeof(double), N * sizeof(double), nvec,
+                             cudaMemcpyDeviceToHost, s), "D2H");
+    c->last_kernels += 2;
+  } else {
+    return set_error(c, EVR_EINVAL, "unknown layout");
+  }
+  EVR_CU(cudaStreamSynchronize(s), "evr_hpsi_host");
+  return EVR_OK;
+}
+
+int evr_last_kernel_ms(evr_ctx* c, float* items_ms, float* reduce_ms) {
+  if (!c || c->host_only) return EVR_EINVAL;
+  EVR_CU(cudaEventSynchronize(c->ev[2]), "event sync");
+  float a = 0.f, b = 0.f;
+  EVR_CU(cudaEventElapsedTime(&a, c->ev[0], c->ev[1]), "event time");
+  EVR_CU(cudaEventElapsedTime(&b, c->ev[1], c->ev[2]), "event time");
+  if (items_ms) *items_ms = a;
+  if (reduce_ms) *reduce_ms = b;
+  return EVR_OK;
+}
+
+int evr_last_launch_count(const evr_ctx* c, int64_t* kernels, int64_t* items) {
+  if (!c) return EVR_EINVAL;
+  if (kernels) *kernels = c->last_kernels;
+  if (items) *items = c->last_items;
+  return EVR_OK;
+}
+
+}  // extern "C"

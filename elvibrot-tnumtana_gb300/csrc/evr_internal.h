@@ -1,0 +1,149 @@
+// evr_internal.h -- shared declarations of the GB300 H.psi library (host tables,
+// device context, kernel launchers).  Not part of the public ABI (include/evr_gpu.h).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/evr_gpu.h"
+
+namespace evr {
+
+constexpr int kMaxD = 16;      // modes
+constexpr int kMaxN1 = 32;     // largest 1-D nq (and nb)
+constexpr int kMaxNb0 = 4;     // electronic states
+
+// ---------------------------------------------------------------------------
+// Host-side tables (built once by evr_setup.cpp)
+// ---------------------------------------------------------------------------
+struct Basis1D {
+  int nb = 0, nq = 0;
+  std::vector<double> x, w;           // scaled grid, weights (wrho)
+  std::vector<double> d0b, d1b, d2b;  // nq x nb column-major
+  std::vector<double> bgw;            // nb x nq = d0b^T diag(w)
+  std::vector<double> d1gg, d2gg;     // nq x nq
+};
+
+// Per-term description used by the device kernels.  Offsets are in elements.
+struct TermDesc {
+  int64_t off_nb;        // offset of the term in the term-basis space (sum_nb order)
+  int64_t off_nq;        // offset of the term grid
+  int32_t NB, NQ;        // prod nb_i, prod nq_i
+  int32_t nb[kMaxD];
+  int32_t nq[kMaxD];
+  int32_t m_d0b[kMaxD];  // offsets of the 1-D matrices in the flat matrix pool
+  int32_t m_bgw[kMaxD];
+  int32_t m_d1[kMaxD];
+  int32_t m_d2[kMaxD];
+  int32_t m_x[kMaxD];
+  double weight;
+};
+
+// One unit of work of the H.psi kernel: one term, a tile of vectors.
+struct WorkItem {
+  int32_t term;
+  int32_t v0;
+  int32_t vt;            // vectors in the tile
+  int32_t smem;          // 1: buffers in shared memory, 0: in the CTA's global slab
+};
+
+struct HostProblem {
+  int kind = 0, D = 0, nb0 = 1, LG = 0, LB = 0, keo_type = 10;
+  std::vector<std::vector<Basis1D>> bas;  // [mode][level]
+  std::vector<std::vector<int>> ltab;     // l(n), 1-based n
+  std::vector<int> term_l;                // n_terms x D
+  std::vector<double> weight;
+  std::vector<TermDesc> terms;
+  int64_t Np = 0, sum_nb = 0, sum_nq = 0, max_nq = 0, max_nb = 0;
+  std::vector<int> packed;                // Np x D
+  std::vector<int> map;                   // sum_nb (packed index or -1)
+  std::vector<double> mat_pool;           // all 1-D matrices
+  // CSR of the transposed map over N = Np*nb0 rows: sources in the term-basis
+  // output buffer (off_nb*nb0 + a*NB + iB) and their Smolyak weight
+  std::vector<int64_t> csr_ptr;
+  std::vector<int64_t> csr_src;
+  std::vector<double> csr_w;
+  // operator
+  std::vector<double> mono_coef;
+  std::vector<int> mono_idx, mono_elec;
+  std::vector<double> G0, g;              // D*D, D*D*D
+  std::vector<double> e0diag;             // zero-order diagonal (preconditioner), N
+  double flop_per_hpsi = 0.0;
+};
+
+// Builds every host table from the public description; returns EVR_OK or an error
+// with a message in `err`.
+int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& err);
+
+// Device copy of the problem and the buffers of the H.psi pipeline.
+struct DeviceProblem {
+  TermDesc* terms = nullptr;
+  double* mats = nullptr;
+  float* mats32 = nullptr;
+  double* vgrid = nullptr;          // sum_nq * nb0^2
+  float* vgrid32 = nullptr;
+  int* map = nullptr;               // sum_nb
+  int64_t* csr_ptr = nullptr;
+  int64_t* csr_src = nullptr;
+  double* csr_w = nullptr;
+  double* G0 = nullptr;
+  double* g = nullptr;
+  double* mono_coef = nullptr;
+  int* mono_idx = nullptr;
+  int* mono_elec = nullptr;
+  double* e0diag = nullptr;
+};
+
+struct Workspace {
+  // keyed by (nvec, prec)
+  int nvec = -1, prec = -1;
+  WorkItem* items = nullptr;
+  int n_items = 0;
+  int* counter = nullptr;
+  void* slab = nullptr;             // per-CTA global scratch
+  size_t slab_per_cta = 0;          // elements
+  void* ht = nullptr;               // term-basis output (sum_nb*nb0 x nvec)
+  void* xin = nullptr;              // interleaved input copy (when converting layouts)
+  void* xout = nullptr;
+  int grid = 0, smem_bytes = 0;
+};
+
+}  // namespace evr
+
+struct evr_ctx {
+  int device = 0;
+  bool host_only = false;           // created with device < 0: tables only
+  cudaStream_t stream = nullptr;
+  evr::HostProblem hp;
+  evr::DeviceProblem dp;
+  evr::Workspace ws;
+  int num_sms = 0;
+  std::string err;
+  int64_t last_kernels = 0, last_items = 0;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // around the items kernel and the reduction
+  double* dp_ggrid = nullptr;      // symmetric G(Q) on the grid (type 10 with g != 0)
+  float* dp_ggrid32 = nullptr;
+  // host staging for the host-pointer entry points
+  double* pinned = nullptr;
+  size_t pinned_bytes = 0;
+};
+
+namespace evr {
+// kernels (evr_kernels.cu)
+int upload_problem(evr_ctx* c);
+void free_problem(evr_ctx* c);
+int ensure_workspace(evr_ctx* c, int nvec, int prec);
+void free_workspace(evr_ctx* c);
+// H.psi on interleaved device blocks (ld >= nvec); returns a status.
+int hpsi_interleaved(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, int prec,
+                     cudaStream_t s);
+int transpose_to_interleaved(const double* in, int64_t ld_in, double* out, int64_t ld_out, int64_t N, int nvec,
+                             cudaStream_t s);
+int transpose_from_interleaved(const double* in, int64_t ld_in, double* out, int64_t ld_out, int64_t N, int nvec,
+                               cudaStream_t s);
+int set_error(evr_ctx* c, int code, const std::string& msg);
+int cuda_check(evr_ctx* c, cudaError_t e, const char* what);
+}  // namespace evr

@@ -1,0 +1,639 @@
+// evr_kernels.cu -- sm_103a kernels of the SG4 / direct-product H.psi path.
+//
+// One persistent kernel runs the whole per-term pipeline of the reference's
+// sub_TabOpPsi_OF_ONEDP_FOR_SGtype4 (Source_ElVibRot/sub_Operator/sub_OpPsi_SG4.f90:1354-1668)
+// for a (term, vector tile) work item per CTA:
+//   gather psi_packed -> term basis   (tabPackedBasis_TO_tabR_AT_iG, BtoG_GtoB_SG4.f90:1176-1246)
+//   B->G, modes 1..D with d0b         (BDP_TO_GDP_OF_SmolyakRep, :2385-2496)      [fused with the gather]
+//   V.psi on the grid                 (:1566-1576)
+//   KEO type 10: D first derivatives, G(Q) combination, D derivatives accumulated
+//                                     (:1578-1628, DerivOp_TO_RDP_OF_SmolaykRep :2690-2795)
+//   KEO type 1: F2 d2 / d1 d1 terms   (:1490-1546)
+//   G->B, modes 1..D with d0b^T w     (GDP_TO_BDP_OF_SmolyakRep, :2497-2581)
+// The weighted scatter-add of the reference (tabR_AT_iG_TO_tabPackedBasis, :1250-1289,
+// OMP ATOMIC) becomes a deterministic CSR gather-reduce over the transposed map.
+//
+// Work buffers of an item live in shared memory when they fit, otherwise in a per-CTA
+// slab of global memory (L2-resident for the CTAs in flight).  Every stage is a small
+// dense contraction along one mode, executed by the whole CTA with one output fibre
+// (M values) per thread and the 1-D matrix read through the read-only cache.
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "evr_internal.h"
+
+namespace evr {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+template <typename T>
+struct ItemParams {
+  const TermDesc* terms;
+  const T* mats;
+  const T* vgrid;
+  const T* ggrid;          // SoA symmetric G per term grid point, or nullptr (G constant)
+  const double* G0;        // D*D (used when ggrid == nullptr)
+  const int* map;
+  const WorkItem* items;
+  int n_items;
+  int* counter;
+  T* slab;
+  int64_t slab_per_cta;
+  const double* x;         // interleaved input (FP64)
+  int64_t ldx;
+  T* ht;                   // term-basis output
+  int64_t ldh;
+  int64_t Np;
+  int D, nb0, keo_type;
+  int has_offdiag;         // type 1 with off-diagonal F2 terms
+};
+
+// out(a, m, b, v) = alpha * sum_k mat[m + M*k] * in(a, k, b, v)  (+ out if acc)
+// element (a, k, b, v) of a tensor with vector stride ld lives at ((a + A*(k + K*b))*ld + v).
+template <typename T, int MAXM>
+__device__ __forceinline__ void contract_m(const T* __restrict__ in, int64_t ldi, T* __restrict__ out, int64_t ldo,
+                                           int A, int K, int M, int B, int Vt, const T* __restrict__ mat, T alpha,
+                                           bool acc) {
+  const int ncol = A * B * Vt;
+  for (int col = threadIdx.x; col < ncol; col += blockDim.x) {
+    const int v = col % Vt;
+    const int r = col / Vt;
+    const int a = r % A, b = r / A;
+    const T* ip = in + (int64_t)(a + (int64_t)A * K * b) * ldi + v;
+    const int64_t istr = (int64_t)A * ldi;
+    T accv[MAXM];
+#pragma unroll
+    for (int m = 0; m < MAXM; ++m) accv[m] = T(0);
+    for (int k = 0; k < K; ++k) {
+      const T xk = ip[k * istr];
+      const T* mk = mat + M * k;
+#pragma unroll
+      for (int m = 0; m < MAXM; ++m)
+        if (m < M) accv[m] = fma(__ldg(mk + m), xk, accv[m]);
+    }
+    T* op = out + (int64_t)(a + (int64_t)A * M * b) * ldo + v;
+    const int64_t ostr = (int64_t)A * ldo;
+#pragma unroll
+    for (int m = 0; m < MAXM; ++m)
+      if (m < M) {
+        T val = alpha * accv[m];
+        if (acc) val += op[m * ostr];
+        op[m * ostr] = val;
+      }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64_t ldo, int A, int K, int M, int B,
+                                         int Vt, const T* mat, T alpha, bool acc) {
+  if (M <= 8) contract_m<T, 8>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  else if (M <= 16) contract_m<T, 16>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  else if (M <= 24) contract_m<T, 24>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  else contract_m<T, 32>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+}
+
+// First B->G mode fused with the gather from the packed vector block:
+// in(k, b, v) = x[(map[off_nb + k + K*b] + Np*e) * ldx + v0 + v]  (0 when excluded)
+template <typename T, int MAXM>
+__device__ __forceinline__ void gather_contract_m(const double* __restrict__ x, int64_t ldx, const int* __restrict__ mp,
+                                                  int64_t eoff, T* __restrict__ out, int K, int M, int B, int Vt,
+                                                  const T* __restrict__ mat) {
+  const int ncol = B * Vt;
+  for (int col = threadIdx.x; col < ncol; col += blockDim.x) {
+    const int v = col % Vt;
+    const int b = col / Vt;
+    T accv[MAXM];
+#pragma unroll
+    for (int m = 0; m < MAXM; ++m) accv[m] = T(0);
+    for (int k = 0; k < K; ++k) {
+      const int p = __ldg(mp + k + K * b);
+      const T xk = (p >= 0) ? (T)__ldg(x + (p + eoff) * ldx + v) : T(0);
+      const T* mk = mat + M * k;
+#pragma unroll
+      for (int m = 0; m < MAXM; ++m)
+        if (m < M) accv[m] = fma(__ldg(mk + m), xk, accv[m]);
+    }
+    T* op = out + (int64_t)M * b * Vt + v;
+#pragma unroll
+    for (int m = 0; m < MAXM; ++m)
+      if (m < M) op[(int64_t)m * Vt] = accv[m];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void gather_contract(const double* x, int64_t ldx, const int* mp, int64_t eoff, T* out,
+                                                int K, int M, int B, int Vt, const T* mat) {
+  if (M <= 8) gather_contract_m<T, 8>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+  else if (M <= 16) gather_contract_m<T, 16>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+  else if (M <= 24) gather_contract_m<T, 24>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+  else gather_contract_m<T, 32>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) hpsi_items_kernel(ItemParams<T> p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  __shared__ TermDesc s_term;
+  const int D = p.D, nb0 = p.nb0;
+  while (true) {
+    if (threadIdx.x == 0) s_item = atomicAdd(p.counter, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= p.n_items) break;
+    const WorkItem w = p.items[it];
+    {
+      const int* src = reinterpret_cast<const int*>(p.terms + w.term);
+      int* dst = reinterpret_cast<int*>(&s_term);
+      for (int i = threadIdx.x; i < (int)(sizeof(TermDesc) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const TermDesc& Tm = s_term;
+    const int NQ = Tm.NQ, NB = Tm.NB, Vt = w.vt;
+    T* buf = w.smem ? reinterpret_cast<T*>(smem_raw) : p.slab + (int64_t)blockIdx.x * p.slab_per_cta;
+    const int64_t stride = (int64_t)NQ * Vt;
+    T* X0 = buf;                     // psi on the grid, nb0 components
+    T* X1 = buf + nb0 * stride;      // H.psi accumulator, nb0 components
+    T* Y = buf + 2 * nb0 * stride;   // derivative arrays
+
+    // ---- gather + B->G (modes 0..D-1), ping-pong between X0[e] and X1[e]
+    for (int e = 0; e < nb0; ++e) {
+      T* A0 = X0 + e * stride;
+      T* A1 = X1 + e * stride;
+      T* cur = (D % 2) ? A0 : A1;   // so that the chain ends in A0
+      int nb_rest = NB / Tm.nb[0];
+      gather_contract<T>(p.x + w.v0, p.ldx, p.map + Tm.off_nb, p.Np * e, cur, Tm.nb[0], Tm.nq[0], nb_rest, Vt,
+                         p.mats + Tm.m_d0b[0]);
+      __syncthreads();
+      int A = Tm.nq[0];
+      for (int i = 1; i < D; ++i) {
+        nb_rest /= Tm.nb[i];
+        T* nxt = (cur == A0) ? A1 : A0;
+        contract<T>(cur, Vt, nxt, Vt, A, Tm.nb[i], Tm.nq[i], nb_rest, Vt, p.mats + Tm.m_d0b[i], T(1), false);
+        __syncthreads();
+        cur = nxt;
+        A *= Tm.nq[i];
+      }
+    }
+
+    // ---- V.psi: X1[a] = sum_b V_ab X0[b]
+    {
+      const T* Vt_ = p.vgrid + Tm.off_nq * nb0 * nb0;
+      const int64_t n = stride;
+      for (int64_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
+        const int q = (int)(idx / Vt);
+        for (int a = 0; a < nb0; ++a) {
+          T s = T(0);
+          for (int b = 0; b < nb0; ++b) s = fma(__ldg(Vt_ + (int64_t)(a + nb0 * b) * NQ + q), X0[b * stride + idx], s);
+          X1[a * stride + idx] = s;
+        }
+      }
+      __syncthreads();
+    }
+
+    // ---- KEO
+    if (p.keo_type == 10) {
+      for (int e = 0; e < nb0; ++e) {
+        const T* P0 = X0 + e * stride;
+        T* Acc = X1 + e * stride;
+        int A = 1, Bq = NQ;
+        for (int j = 0; j < D; ++j) {  // Y[j] = d1_j . psi_G
+          Bq /= Tm.nq[j];
+          contract<T>(P0, Vt, Y + j * stride, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, p.mats + Tm.m_d1[j], T(1), false);
+          A *= Tm.nq[j];
+        }
+        __syncthreads();
+        // Y[i] <- sum_j G_ij(q) Y[j]
+        const int nG = D * (D + 1) / 2;
+        for (int64_t idx = threadIdx.x; idx < stride; idx += blockDim.x) {
+          const int q = (int)(idx / Vt);
+          T y[kMaxD], z[kMaxD];
+#pragma unroll
+          for (int j = 0; j < kMaxD; ++j) { y[j] = (j < D) ? Y[j * stride + idx] : T(0); z[j] = T(0); }
+          if (p.ggrid) {
+            const T* Gp = p.ggrid + Tm.off_nq * nG + q;
+            int c = 0;
+#pragma unroll
+            for (int i = 0; i < kMaxD; ++i) {
+              if (i >= D) break;
+#pragma unroll
+              for (int j = i; j < kMaxD; ++j) {
+                if (j >= D) break;
+                const T gij = __ldg(Gp + (int64_t)c * NQ);
+                ++c;
+                z[i] = fma(gij, y[j], z[i]);
+                if (j != i) z[j] = fma(gij, y[i], z[j]);
+              }
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < kMaxD; ++i) {
+              if (i >= D) break;
+#pragma unroll
+              for (int j = 0; j < kMaxD; ++j) {
+                if (j >= D) break;
+                z[i] = fma((T)__ldg(p.G0 + i + D * j), y[j], z[i]);
+              }
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < kMaxD; ++i)
+            if (i < D) Y[i * stride + idx] = z[i];
+        }
+        __syncthreads();
+        A = 1; Bq = NQ;
+        for (int i = 0; i < D; ++i) {  // Acc += -1/2 d1_i . Y[i]; same-fibre updates per mode
+          Bq /= Tm.nq[i];
+          contract<T>(Y + i * stride, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, p.mats + Tm.m_d1[i], T(-0.5), true);
+          __syncthreads();
+          A *= Tm.nq[i];
+        }
+      }
+    } else {
+      // type 1: Acc += F2_ii d2_i psi + sum_{i<j} F2_ij d1_i d1_j psi, F2 = -G0/2 (diag), -G0 (off)
+      for (int e = 0; e < nb0; ++e) {
+        const T* P0 = X0 + e * stride;
+        T* Acc = X1 + e * stride;
+        int A = 1, Bq = NQ;
+        for (int i = 0; i < D; ++i) {
+          Bq /= Tm.nq[i];
+          const T f = (T)(-0.5 * __ldg(p.G0 + i + D * i));
+          if (f != T(0))
+            contract<T>(P0, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, p.mats + Tm.m_d2[i], f, true);
+          __syncthreads();
+          A *= Tm.nq[i];
+        }
+        if (p.has_offdiag) {
+          int Ai = 1;
+          for (int i = 0; i < D; ++i) {
+            const int Bi = NQ / (Ai * Tm.nq[i]);
+            int Aj = Ai * Tm.nq[i];
+            for (int j = i + 1; j < D; ++j) {
+              const int Bj = NQ / (Aj * Tm.nq[j]);
+              const T f = (T)(-__ldg(p.G0 + i + D * j));
+              if (f != T(0)) {
+                contract<T>(P0, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, p.mats + Tm.m_d1[i], T(1), false);
+                __syncthreads();
+                contract<T>(Y, Vt, Acc, Vt, Aj, Tm.nq[j], Tm.nq[j], Bj, Vt, p.mats + Tm.m_d1[j], f, true);
+                __syncthreads();
+              }
+              Aj *= Tm.nq[j];
+            }
+            Ai *= Tm.nq[i];
+          }
+        }
+      }
+    }
+
+    // ---- G->B (modes 0..D-1) with d0b^T w; the last mode writes the term-basis output
+    for (int e = 0; e < nb0; ++e) {
+      T* A0 = X1 + e * stride;
+      T* A1 = X0 + e * stride;
+      T* cur = A0;
+      int A = 1, Bq = NQ;
+      for (int i = 0; i < D; ++i) {
+        Bq /= Tm.nq[i];
+        if (i == D - 1) {
+          T* dst = p.ht + (Tm.off_nb * nb0 + (int64_t)e * NB) * p.ldh + w.v0;
+          contract<T>(cur, Vt, dst, p.ldh, A, Tm.nq[i], Tm.nb[i], Bq, Vt, p.mats + Tm.m_bgw[i], T(1), false);
+        } else {
+          T* nxt = (cur == A0) ? A1 : A0;
+          contract<T>(cur, Vt, nxt, Vt, A, Tm.nq[i], Tm.nb[i], Bq, Vt, p.mats + Tm.m_bgw[i], T(1), false);
+          cur = nxt;
+        }
+        __syncthreads();
+        A *= Tm.nb[i];
+      }
+    }
+  }
+}
+
+// y[k*ldy + v] = sum_{e in row k} w_e * ht[src_e*ldh + v]   (FP64 accumulation)
+template <typename T>
+__global__ void csr_reduce_kernel(const int64_t* __restrict__ ptr, const int64_t* __restrict__ src,
+                                  const double* __restrict__ wt, const T* __restrict__ ht, int64_t ldh,
+                                  double* __restrict__ y, int64_t ldy, int64_t N, int nvec) {
+  const int64_t total = N * nvec;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = idx / nvec;
+    const int v = (int)(idx - k * nvec);
+    double s = 0.0;
+    const int64_t e1 = __ldg(ptr + k + 1);
+    for (int64_t e = __ldg(ptr + k); e < e1; ++e) s = fma(__ldg(wt + e), (double)ht[__ldg(src + e) * ldh + v], s);
+    y[k * ldy + v] = s;
+  }
+}
+
+// grid tables: V_ab(Q) from monomials and the symmetric G(Q) = G0 + sum_k g_ijk Q_k
+__global__ void grid_eval_kernel(const TermDesc* __restrict__ terms, int n_terms, const double* __restrict__ mats,
+                                 int64_t sum_nq, int D, int nb0, int n_mono, const double* __restrict__ coef,
+                                 const int* __restrict__ midx, const int* __restrict__ melec, const double* __restrict__ G0,
+                                 const double* __restrict__ g, double* __restrict__ vgrid, double* __restrict__ ggrid) {
+  for (int64_t gq = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; gq < sum_nq;
+       gq += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = n_terms - 1;  // last term with off_nq <= gq
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (terms[mid].off_nq <= gq) lo = mid; else hi = mid - 1;
+    }
+    const TermDesc& T = terms[lo];
+    int64_t q = gq - T.off_nq;
+    const int NQ = T.NQ;
+    double Q[kMaxD];
+    int64_t r = q;
+    for (int d = 0; d < D; ++d) {
+      Q[d] = mats[T.m_x[d] + (int)(r % T.nq[d])];
+      r /= T.nq[d];
+    }
+    double* V = vgrid + T.off_nq * nb0 * nb0;
+    for (int ab = 0; ab < nb0 * nb0; ++ab) V[(int64_t)ab * NQ + q] = 0.0;
+    for (int m = 0; m < n_mono; ++m) {
+      double v = coef[m];
+      for (int k = 0; k < 4; ++k) {
+        int i = midx[4 * m + k];
+        if (i >= 0) v *= Q[i];
+      }
+      V[(int64_t)(melec[2 * m] + nb0 * melec[2 * m + 1]) * NQ + q] += v;
+    }
+    if (ggrid) {
+      const int nG = D * (D + 1) / 2;
+      double* Gp = ggrid + T.off_nq * nG + q;
+      int c = 0;
+      for (int i = 0; i < D; ++i)
+        for (int j = i; j < D; ++j) {
+          double s = G0[i + D * j];
+          for (int k = 0; k < D; ++k) s += g[i + D * (j + D * k)] * Q[k];
+          Gp[(int64_t)c * NQ] = s;
+          ++c;
+        }
+    }
+  }
+}
+
+__global__ void to_float_kernel(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+// out[v*ld_out + k] <-> in[k*ld_in + v] tiled transposes
+__global__ void transpose_kernel(const double* __restrict__ in, int64_t ld_in, double* __restrict__ out,
+                                 int64_t ld_out, int64_t rows, int64_t cols) {
+  // in: rows x cols with row stride ld_in (in[r*ld_in + c]); out[c*ld_out + r]
+  __shared__ double tile[32][33];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    int64_t r = r0 + i, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) tile[i][threadIdx.x] = in[r * ld_in + c];
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    int64_t c = c0 + i, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) out[c * ld_out + r] = tile[threadIdx.x][i];
+  }
+}
+
+template <typename T>
+size_t footprint_elems(const HostProblem& P, const TermDesc& Tm, int vt) {
+  int ny = (P.keo_type == 10) ? P.D : 1;
+  return (size_t)(2 * P.nb0 + ny) * (size_t)Tm.NQ * (size_t)vt;
+}
+
+template <typename T>
+void* dev_alloc(size_t n, int& rc) {
+  void* p = nullptr;
+  if (n == 0) n = 1;
+  if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) { rc = EVR_ENOMEM; return nullptr; }
+  return p;
+}
+
+}  // namespace
+
+int set_error(evr_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_check(evr_ctx* c, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return EVR_OK;
+  (void)cudaGetLastError();
+  return set_error(c, e == cudaErrorMemoryAllocation ? EVR_ENOMEM : EVR_EDEVICE,
+                   std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define EVR_CU(call, what)                              \
+  do {                                                  \
+    int _rc = cuda_check(c, (call), what);              \
+    if (_rc != EVR_OK) return _rc;                      \
+  } while (0)
+
+template <typename V>
+static int upload(evr_ctx* c, V** dst, const std::vector<V>& src) {
+  size_t n = std::max<size_t>(src.size(), 1);
+  EVR_CU(cudaMalloc((void**)dst, n * sizeof(V)), "cudaMalloc");
+  if (!src.empty()) EVR_CU(cudaMemcpy(*dst, src.data(), src.size() * sizeof(V), cudaMemcpyHostToDevice), "cudaMemcpy");
+  return EVR_OK;
+}
+
+int upload_problem(evr_ctx* c) {
+  HostProblem& P = c->hp;
+  DeviceProblem& d = c->dp;
+  int rc;
+  if ((rc = upload(c, &d.terms, P.terms))) return rc;
+  if ((rc = upload(c, &d.mats, P.mat_pool))) return rc;
+  if ((rc = upload(c, &d.map, P.map))) return rc;
+  if ((rc = upload(c, &d.csr_ptr, P.csr_ptr))) return rc;
+  if ((rc = upload(c, &d.csr_src, P.csr_src))) return rc;
+  if ((rc = upload(c, &d.csr_w, P.csr_w))) return rc;
+  if ((rc = upload(c, &d.G0, P.G0))) return rc;
+  if ((rc = upload(c, &d.g, P.g))) return rc;
+  if ((rc = upload(c, &d.mono_coef, P.mono_coef))) return rc;
+  if ((rc = upload(c, &d.mono_idx, P.mono_idx))) return rc;
+  if ((rc = upload(c, &d.mono_elec, P.mono_elec))) return rc;
+  if ((rc = upload(c, &d.e0diag, P.e0diag))) return rc;
+  const int nb0 = P.nb0, D = P.D;
+  bool g_nonzero = false;
+  for (double v : P.g) g_nonzero |= (v != 0.0);
+  const int64_t nv = P.sum_nq * nb0 * nb0;
+  EVR_CU(cudaMalloc((void**)&d.vgrid, nv * sizeof(double)), "cudaMalloc vgrid");
+  double* gg = nullptr;
+  if (P.keo_type == 10 && g_nonzero) {
+    EVR_CU(cudaMalloc((void**)&gg, P.sum_nq * (D * (D + 1) / 2) * sizeof(double)), "cudaMalloc ggrid");
+  }
+  c->dp_ggrid = gg;
+  grid_eval_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(d.terms, (int)P.terms.size(), d.mats, P.sum_nq, D, nb0,
+                                                          (int)P.mono_coef.size(), d.mono_coef, d.mono_idx,
+                                                          d.mono_elec, d.G0, d.g, d.vgrid, gg);
+  EVR_CU(cudaGetLastError(), "grid_eval_kernel");
+  // FP32 copies for the mixed-precision contractions
+  EVR_CU(cudaMalloc((void**)&d.mats32, P.mat_pool.size() * sizeof(float) + 16), "cudaMalloc mats32");
+  EVR_CU(cudaMalloc((void**)&d.vgrid32, nv * sizeof(float)), "cudaMalloc vgrid32");
+  to_float_kernel<<<c->num_sms * 4, 256, 0, c->stream>>>(d.mats, d.mats32, (int64_t)P.mat_pool.size());
+  to_float_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(d.vgrid, d.vgrid32, nv);
+  if (gg) {
+    const int64_t ng = P.sum_nq * (D * (D + 1) / 2);
+    EVR_CU(cudaMalloc((void**)&c->dp_ggrid32, ng * sizeof(float)), "cudaMalloc ggrid32");
+    to_float_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(gg, c->dp_ggrid32, ng);
+  }
+  EVR_CU(cudaGetLastError(), "to_float_kernel");
+  EVR_CU(cudaStreamSynchronize(c->stream), "grid set-up");
+  return EVR_OK;
+}
+
+void free_problem(evr_ctx* c) {
+  DeviceProblem& d = c->dp;
+  void* ptrs[] = {d.terms, d.mats, d.mats32, d.vgrid, d.vgrid32, d.map, d.csr_ptr, d.csr_src, d.csr_w, d.G0, d.g,
+                  d.mono_coef, d.mono_idx, d.mono_elec, d.e0diag, c->dp_ggrid, c->dp_ggrid32};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  d = DeviceProblem();
+  c->dp_ggrid = nullptr;
+  c->dp_ggrid32 = nullptr;
+}
+
+void free_workspace(evr_ctx* c) {
+  Workspace& w = c->ws;
+  void* ptrs[] = {w.items, w.counter, w.slab, w.ht, w.xin, w.xout};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  w = Workspace();
+}
+
+// Work decomposition for a block of nvec vectors: per term the widest vector tile whose
+// buffers fit the shared-memory budget; terms that do not fit even with one vector run
+// from the CTA's global slab.  Items are ordered by decreasing cost.
+int ensure_workspace(evr_ctx* c, int nvec, int prec) {
+  Workspace& w = c->ws;
+  if (w.nvec == nvec && w.prec == prec && w.items) return EVR_OK;
+  free_workspace(c);
+  const HostProblem& P = c->hp;
+  const size_t esz = prec == EVR_PREC_FP32 ? sizeof(float) : sizeof(double);
+  int smem_budget = 0;
+  EVR_CU(cudaDeviceGetAttribute(&smem_budget, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attr");
+  const int ctas_per_sm = 2;
+  smem_budget = std::min(smem_budget, (int)(228 * 1024 / ctas_per_sm) - 2048);
+  std::vector<WorkItem> items;
+  size_t slab_elems = 0;
+  int max_vt_smem = 1;
+  for (int t = 0; t < (int)P.terms.size(); ++t) {
+    const TermDesc& Tm = P.terms[t];
+    if (Tm.weight == 0.0) continue;
+    int vt = 1;
+    size_t fp1 = (prec == EVR_PREC_FP32) ? footprint_elems<float>(P, Tm, 1) : footprint_elems<double>(P, Tm, 1);
+    bool in_smem = fp1 * esz <= (size_t)smem_budget;
+    if (in_smem) {
+      while (vt * 2 <= nvec && vt * 2 <= 32 && fp1 * (size_t)(vt * 2) * esz <= (size_t)smem_budget) vt *= 2;
+      max_vt_smem = std::max(max_vt_smem, vt);
+    } else {
+      slab_elems = std::max(slab_elems, fp1);
+    }
+    for (int v0 = 0; v0 < nvec; v0 += vt) items.push_back(WorkItem{t, v0, std::min(vt, nvec - v0), in_smem ? 1 : 0});
+  }
+  std::stable_sort(items.begin(), items.end(), [&](const WorkItem& a, const WorkItem& b) {
+    return (int64_t)P.terms[a.term].NQ * a.vt > (int64_t)P.terms[b.term].NQ * b.vt;
+  });
+  int rc = EVR_OK;
+  w.n_items = (int)items.size();
+  w.items = (WorkItem*)dev_alloc<WorkItem>(items.size(), rc);
+  if (rc) return set_error(c, rc, "workspace allocation (items)");
+  EVR_CU(cudaMemcpy(w.items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice), "items");
+  w.counter = (int*)dev_alloc<int>(1, rc);
+  if (rc) return set_error(c, rc, "workspace allocation (counter)");
+  w.grid = c->num_sms * ctas_per_sm;
+  w.smem_bytes = smem_budget;
+  w.slab_per_cta = slab_elems;
+  if (slab_elems) {
+    w.slab = esz == 4 ? dev_alloc<float>(slab_elems * w.grid, rc) : dev_alloc<double>(slab_elems * w.grid, rc);
+    if (rc) return set_error(c, rc, "workspace allocation (slab)");
+  }
+  const size_t ht_elems = (size_t)P.sum_nb * P.nb0 * nvec;
+  w.ht = esz == 4 ? dev_alloc<float>(ht_elems, rc) : dev_alloc<double>(ht_elems, rc);
+  if (rc) return set_error(c, rc, "workspace allocation (term-basis output)");
+  const size_t xe = (size_t)P.Np * P.nb0 * nvec;
+  w.xin = dev_alloc<double>(xe, rc);
+  if (rc) return set_error(c, rc, "workspace allocation (xin)");
+  w.xout = dev_alloc<double>(xe, rc);
+  if (rc) return set_error(c, rc, "workspace allocation (xout)");
+  if (esz == 4) {
+    EVR_CU(cudaFuncSetAttribute(hpsi_items_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_budget),
+           "smem attr");
+  } else {
+    EVR_CU(cudaFuncSetAttribute(hpsi_items_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_budget),
+           "smem attr");
+  }
+  w.nvec = nvec;
+  w.prec = prec;
+  return EVR_OK;
+}
+
+template <typename T>
+static int run_items(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, cudaStream_t s) {
+  const HostProblem& P = c->hp;
+  Workspace& w = c->ws;
+  ItemParams<T> p;
+  const bool f32 = sizeof(T) == 4;
+  p.terms = c->dp.terms;
+  p.mats = f32 ? (const T*)c->dp.mats32 : (const T*)c->dp.mats;
+  p.vgrid = f32 ? (const T*)c->dp.vgrid32 : (const T*)c->dp.vgrid;
+  p.ggrid = f32 ? (const T*)c->dp_ggrid32 : (const T*)c->dp_ggrid;
+  p.G0 = c->dp.G0;
+  p.map = c->dp.map;
+  p.items = w.items;
+  p.n_items = w.n_items;
+  p.counter = w.counter;
+  p.slab = (T*)w.slab;
+  p.slab_per_cta = (int64_t)w.slab_per_cta;
+  p.x = x;
+  p.ldx = ldx;
+  p.ht = (T*)w.ht;
+  p.ldh = nvec;
+  p.Np = P.Np;
+  p.D = P.D;
+  p.nb0 = P.nb0;
+  p.keo_type = P.keo_type;
+  p.has_offdiag = 0;
+  if (P.keo_type == 1)
+    for (int i = 0; i < P.D; ++i)
+      for (int j = i + 1; j < P.D; ++j) p.has_offdiag |= (P.G0[i + (size_t)P.D * j] != 0.0);
+  EVR_CU(cudaMemsetAsync(w.counter, 0, sizeof(int), s), "memset counter");
+  EVR_CU(cudaEventRecord(c->ev[0], s), "event");
+  hpsi_items_kernel<T><<<w.grid, kThreads, w.smem_bytes, s>>>(p);
+  EVR_CU(cudaGetLastError(), "hpsi_items_kernel launch");
+  EVR_CU(cudaEventRecord(c->ev[1], s), "event");
+  const int64_t N = P.Np * P.nb0;
+  int rblocks = (int)std::min<int64_t>((N * nvec + 255) / 256, (int64_t)c->num_sms * 16);
+  csr_reduce_kernel<T><<<rblocks, 256, 0, s>>>(c->dp.csr_ptr, c->dp.csr_src, c->dp.csr_w, (const T*)w.ht, nvec, y, ldy,
+                                                N, nvec);
+  EVR_CU(cudaGetLastError(), "csr_reduce_kernel launch");
+  EVR_CU(cudaEventRecord(c->ev[2], s), "event");
+  c->last_kernels = 2;
+  c->last_items = w.n_items;
+  return EVR_OK;
+}
+
+int hpsi_interleaved(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, int prec,
+                     cudaStream_t s) {
+  int rc = ensure_workspace(c, nvec, prec);
+  if (rc) return rc;
+  if (prec == EVR_PREC_FP32) return run_items<float>(c, x, ldx, y, ldy, nvec, s);
+  return run_items<double>(c, x, ldx, y, ldy, nvec, s);
+}
+
+int transpose_to_interleaved(const double* in, int64_t ld_in, double* out, int64_t ld_out, int64_t N, int nvec,
+                             cudaStream_t s) {
+  // in: column-major N x nvec (in[v*ld_in + k]) == row-major nvec x N
+  dim3 blk(32, 8), grd((unsigned)((N + 31) / 32), (unsigned)((nvec + 31) / 32));
+  transpose_kernel<<<grd, blk, 0, s>>>(in, ld_in, out, ld_out, nvec, N);
+  return cudaGetLastError() == cudaSuccess ? EVR_OK : EVR_EDEVICE;
+}
+
+int transpose_from_interleaved(const double* in, int64_t ld_in, double* out, int64_t ld_out, int64_t N, int nvec,
+                               cudaStream_t s) {
+  dim3 blk(32, 8), grd((unsigned)((nvec + 31) / 32), (unsigned)((N + 31) / 32));
+  transpose_kernel<<<grd, blk, 0, s>>>(in, ld_in, out, ld_out, N, nvec);
+  return cudaGetLastError() == cudaSuccess ? EVR_OK : EVR_EDEVICE;
+}
+
+}  // namespace evr

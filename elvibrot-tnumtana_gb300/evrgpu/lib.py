@@ -1,0 +1,272 @@
+"""ctypes binding of libevrgpu.so (include/evr_gpu.h) and the host-side mirror of the
+reference's OpPsi / Davidson / propagation call surface.
+
+``Problem`` plays the role of the reference's ``para_Op`` for the H.psi path: it is
+created once from a ``ProblemSpec`` and then applies H to blocks of vectors
+(``hpsi`` ~ ``sub_TabOpPsi``, Source_ElVibRot/sub_Operator/sub_OpPsi.f90:701),
+computes levels (``davidson`` ~ ``sub_propagation_Davidson``,
+sub_propagation/sub_module_Davidson.f90:54) and propagates packets
+(``chebyshev`` ~ ``march_cheby``, sub_propagation/sub_module_propa_march.f90:4142).
+Errors come back as ``EvrError`` carrying the library's status and message; there is
+no CPU fallback: without the compiled library or a GPU the calls fail.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+EVR_OK, EVR_EINVAL, EVR_ENOMEM, EVR_ETIMEDOUT, EVR_EDEVICE, EVR_ENOCONV = 0, 22, 12, 110, 1001, 1002
+PREC = {"fp64": 0, "fp32": 1}
+LAYOUT_COLMAJOR, LAYOUT_INTERLEAVED = 0, 1
+
+_ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+_lp = C.POINTER(C.c_int64)
+
+
+class EvrError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"evr error {code}: {msg}")
+        self.code = code
+
+
+class ProblemDesc(C.Structure):
+    _fields_ = [("kind", C.c_int), ("D", C.c_int), ("nb0", C.c_int), ("LG", C.c_int), ("LB", C.c_int),
+                ("Aq", _ip), ("Bq", _ip), ("Ab", _ip), ("Bb", _ip), ("nq_dp", _ip), ("nb_dp", _ip),
+                ("scaleQ", _dp), ("Q0", _dp), ("n_mono", C.c_int), ("mono_coef", _dp), ("mono_idx", _ip),
+                ("mono_elec", _ip), ("keo_type", C.c_int), ("G0", _dp), ("g", _dp)]
+
+
+class Sizes(C.Structure):
+    _fields_ = [("Np", C.c_int64), ("N", C.c_int64), ("n_terms", C.c_int64), ("sum_nb", C.c_int64),
+                ("sum_nq", C.c_int64), ("max_nq_term", C.c_int64), ("flop_per_hpsi", C.c_double)]
+
+
+class DavidsonOpts(C.Structure):
+    _fields_ = [("n_levels", C.c_int), ("block", C.c_int), ("max_dim", C.c_int), ("max_it", C.c_int),
+                ("conv_resi", C.c_double), ("conv_ene", C.c_double), ("prec", C.c_int), ("n_guess", C.c_int)]
+
+
+EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_tables", "evr_get_basis",
+           "evr_get_vgrid", "evr_hpsi_host", "evr_hpsi_device", "evr_last_launch_count", "evr_last_kernel_ms",
+           "evr_davidson",
+           "evr_cheby_propagate"]
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build: bool = True):
+    """Load (building first if needed) libevrgpu.so and declare its signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build:
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise EvrError(EVR_EDEVICE, f"{_build.LIB} is missing: build the CUDA library first")
+    L = C.CDLL(_build.LIB)
+    vp = C.c_void_p
+    L.evr_create.argtypes = [C.POINTER(vp), C.POINTER(ProblemDesc), C.c_int]
+    L.evr_destroy.argtypes = [vp]
+    L.evr_last_error.argtypes = [vp]
+    L.evr_last_error.restype = C.c_char_p
+    L.evr_sizes.argtypes = [vp, C.POINTER(Sizes)]
+    L.evr_get_tables.argtypes = [vp, _ip, _dp, _ip, _ip]
+    L.evr_get_basis.argtypes = [vp, C.c_int, C.c_int, _ip] + [_dp] * 8
+    L.evr_get_vgrid.argtypes = [vp, _dp]
+    L.evr_hpsi_host.argtypes = [vp, _dp, C.c_int64, _dp, C.c_int64, C.c_int, C.c_int, C.c_int]
+    L.evr_hpsi_device.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.c_int, C.c_int, C.c_int, vp]
+    L.evr_last_launch_count.argtypes = [vp, _lp, _lp]
+    L.evr_last_kernel_ms.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    if hasattr(L, "evr_davidson"):
+        L.evr_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _dp, _dp, _dp, _lp]
+    if hasattr(L, "evr_cheby_propagate"):
+        L.evr_cheby_propagate.argtypes = [vp, _dp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double,
+                                          C.c_double, C.c_int, _dp, _dp, _lp]
+    _lib = L
+    return L
+
+
+def _iarr(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _darr(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+class Problem:
+    """One H.psi problem on one GPU (device=-1: host tables only)."""
+
+    def __init__(self, spec, device: int = 0):
+        L = load()
+        self.spec = spec
+        D = spec.D
+        keep = []
+
+        def I(a):
+            if a is None:
+                return None
+            a = _iarr(a)
+            keep.append(a)
+            return _p(a, _ip)
+
+        def F(a):
+            if a is None:
+                return None
+            a = _darr(a)
+            keep.append(a)
+            return _p(a, _dp)
+
+        d = ProblemDesc()
+        d.kind = 0 if spec.kind == "sg4" else 1
+        d.D, d.nb0, d.LG, d.LB = D, spec.nb0, spec.LG, spec.LB
+        d.Aq, d.Bq, d.Ab, d.Bb = I(spec.Aq), I(spec.Bq), I(spec.Ab), I(spec.Bb)
+        d.nq_dp, d.nb_dp = I(spec.nq_dp), I(spec.nb_dp)
+        d.scaleQ, d.Q0 = F(spec.scaleQ), F(spec.Q0)
+        d.n_mono = len(spec.mono_coef)
+        d.mono_coef, d.mono_idx, d.mono_elec = F(spec.mono_coef), I(spec.mono_idx), I(spec.mono_elec)
+        d.keo_type = spec.keo_type
+        d.G0 = F(np.asarray(spec.G0).ravel(order="F"))
+        d.g = F(np.asarray(spec.g).ravel(order="F"))
+        h = C.c_void_p()
+        rc = L.evr_create(C.byref(h), C.byref(d), device)
+        self.h = h
+        if rc != 0:
+            msg = L.evr_last_error(h).decode() if h else ""
+            self.close()
+            raise EvrError(rc, msg)
+        s = Sizes()
+        L.evr_sizes(self.h, C.byref(s))
+        self.Np, self.N, self.nterm = s.Np, s.N, s.n_terms
+        self.sum_nb, self.sum_nq, self.max_nq = s.sum_nb, s.sum_nq, s.max_nq_term
+        self.flop_per_hpsi = s.flop_per_hpsi
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().evr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise EvrError(rc, load().evr_last_error(self.h).decode())
+
+    # ---- tables -------------------------------------------------------------------
+    def tables(self):
+        D = self.spec.D
+        term_l = np.zeros((self.nterm, D), dtype=np.int32)
+        weight = np.zeros(self.nterm)
+        mp = np.zeros(self.sum_nb, dtype=np.int32)
+        packed = np.zeros((self.Np, D), dtype=np.int32)
+        self._check(load().evr_get_tables(self.h, _p(term_l, _ip), _p(weight, _dp), _p(mp, _ip), _p(packed, _ip)))
+        return dict(term_l=term_l, weight=weight, map=mp, packed=packed)
+
+    def basis(self, mode, level):
+        bufs = [np.zeros(64 * 64) for _ in range(8)]
+        nbq = np.zeros(2, dtype=np.int32)
+        self._check(load().evr_get_basis(self.h, mode, level, _p(nbq, _ip), *[_p(b, _dp) for b in bufs]))
+        nb, nq = int(nbq[0]), int(nbq[1])
+        x, w, d0, d1, d2, bgw, g1, g2 = bufs
+        f = lambda a, r, c: a[: r * c].reshape((r, c), order="F").copy()
+        return dict(nb=nb, nq=nq, x=x[:nq].copy(), w=w[:nq].copy(), d0b=f(d0, nq, nb), d1b=f(d1, nq, nb),
+                    d2b=f(d2, nq, nb), bgw=f(bgw, nb, nq), d1gg=f(g1, nq, nq), d2gg=f(g2, nq, nq))
+
+    def vgrid(self):
+        v = np.zeros(self.sum_nq * self.spec.nb0 ** 2)
+        self._check(load().evr_get_vgrid(self.h, _p(v, _dp)))
+        return v
+
+    # ---- H.psi ----------------------------------------------------------------------
+    def hpsi(self, psi, prec: str = "fp64"):
+        """H applied to the columns of a HOST array psi (N x nvec); copies in and out."""
+        psi = np.asfortranarray(psi, dtype=np.float64)
+        if psi.ndim == 1:
+            psi = psi[:, None]
+        N, nvec = psi.shape
+        if N != self.N:
+            raise EvrError(EVR_EINVAL, f"psi has {N} rows, expected {self.N}")
+        out = np.zeros((N, nvec), order="F")
+        self._check(load().evr_hpsi_host(self.h, _p(psi, _dp), N, _p(out, _dp), N, nvec, LAYOUT_COLMAJOR,
+                                         PREC[prec]))
+        return out
+
+    def hpsi_host_ptr(self, psi_ptr, ld_psi, hpsi_ptr, ld_hpsi, nvec, layout, prec="fp64"):
+        """Raw host-pointer entry point (pinned buffers for the end-to-end timing)."""
+        self._check(load().evr_hpsi_host(self.h, C.cast(psi_ptr, _dp), ld_psi, C.cast(hpsi_ptr, _dp), ld_hpsi, nvec,
+                                         layout, PREC[prec]))
+
+    def hpsi_device(self, psi_ptr, ld_psi, hpsi_ptr, ld_hpsi, nvec, layout=LAYOUT_INTERLEAVED, prec="fp64",
+                    stream=None):
+        """H.psi on DEVICE pointers (e.g. torch tensor data_ptr()), stream-ordered."""
+        self._check(load().evr_hpsi_device(self.h, C.c_void_p(psi_ptr), ld_psi, C.c_void_p(hpsi_ptr), ld_hpsi, nvec,
+                                           layout, PREC[prec], C.c_void_p(stream) if stream else None))
+
+    def last_launch_count(self):
+        k = C.c_int64()
+        it = C.c_int64()
+        self._check(load().evr_last_launch_count(self.h, C.byref(k), C.byref(it)))
+        return k.value, it.value
+
+    def last_kernel_ms(self):
+        a, b = C.c_float(), C.c_float()
+        self._check(load().evr_last_kernel_ms(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    # ---- drivers ------------------------------------------------------------------
+    def davidson(self, n_levels, block=None, max_dim=None, max_it=200, conv_resi=1e-7, conv_ene=1e-10,
+                 prec="fp64", guess=None, want_vectors=False):
+        L = load()
+        o = DavidsonOpts()
+        o.n_levels = n_levels
+        o.block = block or n_levels
+        o.max_dim = max_dim or max(4 * n_levels, n_levels + 3 * o.block)
+        o.max_it = max_it
+        o.conv_resi, o.conv_ene = conv_resi, conv_ene
+        o.prec = PREC[prec]
+        g = None
+        if guess is not None:
+            g = np.asfortranarray(guess, dtype=np.float64)
+            o.n_guess = g.shape[1]
+        eig = np.zeros(n_levels)
+        vec = np.zeros((self.N, n_levels), order="F") if want_vectors else None
+        info = np.zeros(4, dtype=np.int64)
+        self._check(L.evr_davidson(self.h, C.byref(o), _p(g, _dp), _p(eig, _dp), _p(vec, _dp), _p(info, _lp)))
+        return eig, vec, dict(iterations=int(info[0]), hpsi_fp64=int(info[1]), hpsi_fp32=int(info[2]),
+                              converged=bool(info[3]))
+
+    def chebyshev(self, psi0, dt, nsteps, emin, emax, poly_tol=1e-10, prec="fp64", want_psi=False):
+        """Chebyshev propagation of complex packets psi0 (N x npsi, complex128)."""
+        L = load()
+        psi0 = np.asarray(psi0, dtype=np.complex128)
+        if psi0.ndim == 1:
+            psi0 = psi0[:, None]
+        N, npsi = psi0.shape
+        buf = np.asfortranarray(psi0).view(np.float64)  # (2N x npsi): re/im interleaved per element
+        buf = np.ascontiguousarray(np.asfortranarray(psi0).T).view(np.float64)  # npsi rows of 2N
+        ac = np.zeros((nsteps + 1) * npsi * 2)
+        out = np.zeros(npsi * 2 * N) if want_psi else None
+        info = np.zeros(3, dtype=np.int64)
+        self._check(L.evr_cheby_propagate(self.h, _p(buf, _dp), npsi, dt, nsteps, emin, emax, poly_tol, PREC[prec],
+                                          _p(ac, _dp), _p(out, _dp), _p(info, _lp)))
+        autocorr = ac.view(np.complex128).reshape(nsteps + 1, npsi)
+        psi = out.view(np.complex128).reshape(npsi, N).T.copy() if want_psi else None
+        return autocorr, psi, dict(max_order=int(info[0]), hpsi=int(info[1]), status=int(info[2]))

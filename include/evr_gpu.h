@@ -1,0 +1,177 @@
+/*
+ * evr_gpu.h -- C ABI of the GB300 (sm_103a) H.psi library for ElVibRot-TnumTana.
+ *
+ * The library replaces the reference's OpPsi hot path and the loops that drive it.
+ * Every entry point returns an int status (EVR_OK = 0) and never stops the process;
+ * the message of the last failure is available from evr_last_error().
+ * No entry point takes C++ or torch types: plain pointers, sizes and flags only, so
+ * a Fortran ISO_C_BINDING interface, ctypes or cgo can bind it directly.
+ *
+ * Vector layouts
+ *   "basis column-major" (EVR_LAYOUT_COLMAJOR): nvec columns, each a packed basis
+ *       vector of length N = Np*nb0 (the reference's RvecB, electronic index slowest:
+ *       element (ib0, iB) at ib0*Np + iB), column stride ld >= N.  This is what the
+ *       Fortran host passes (TabPsi(i)%RvecB).
+ *   "interleaved" (EVR_LAYOUT_INTERLEAVED): element (k, v) at k*ld + v with ld >= nvec;
+ *       the library's native device layout (vectors fastest).
+ */
+#ifndef EVR_GPU_H
+#define EVR_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define EVR_OK          0
+#define EVR_EINVAL      22   /* bad argument, shape or table entry            */
+#define EVR_ENOMEM      12   /* device or host allocation failed              */
+#define EVR_ETIMEDOUT  110   /* a bounded device wait expired                  */
+#define EVR_EDEVICE    1001  /* CUDA runtime / library error                   */
+#define EVR_ENOCONV    1002  /* iterative solver did not converge              */
+
+/* basis kinds */
+#define EVR_BASIS_SG4  0     /* Smolyak SparseGrid_type=4                       */
+#define EVR_BASIS_DP   1     /* direct product                                  */
+
+/* precisions of the basis<->grid contractions */
+#define EVR_PREC_FP64  0     /* plain form: everything in FP64                  */
+#define EVR_PREC_FP32  1     /* contractions and grid terms in FP32             */
+
+/* vector layouts */
+#define EVR_LAYOUT_COLMAJOR    0
+#define EVR_LAYOUT_INTERLEAVED 1
+
+typedef struct evr_ctx evr_ctx;
+
+/*
+ * Problem description: the basis tables the reference builds in
+ *   construct_primitive_basis (Source_ElVibRot/sub_Basis/sub_module_basis.f90:391-782),
+ *   RecSparseGrid_ForDP_type4 (sub_Basis/sub_quadra_SparseBasis.f90:924-1435) and
+ *   Set_tables_FOR_SmolyakRepBasis_TO_tabPackedBasis
+ *   (sub_Basis/sub_Basis_SG4/sub_module_basis_BtoG_GtoB_SG4.f90:625-949),
+ * and the operator of sub_TabOpPsi_OF_ONEDP_FOR_SGtype4
+ *   (Source_ElVibRot/sub_Operator/sub_OpPsi_SG4.f90:1354-1668).
+ * The library builds all tables itself from these few numbers.
+ */
+typedef struct evr_problem_desc {
+  int kind;              /* EVR_BASIS_SG4 or EVR_BASIS_DP                          */
+  int D;                 /* number of modes, 1..16                                  */
+  int nb0;               /* electronic states (nb_elec), >= 1                       */
+  int LG, LB;            /* SG4: L_SparseGrid, L_SparseBasis (LB <= LG)             */
+  const int *Aq, *Bq;    /* SG4: nq(l) = Aq[i] + Bq[i]*l   (L_TO_nq_A/B)            */
+  const int *Ab, *Bb;    /* SG4: nb(l) = Ab[i] + Bb[i]*l   (L_TO_nb_A/B)            */
+  const int *nq_dp;      /* DP: grid points per mode                                */
+  const int *nb_dp;      /* DP: basis functions per mode                            */
+  const double *scaleQ;  /* per mode (sub_scale_basis), NULL = 1                    */
+  const double *Q0;      /* per mode, NULL = 0                                      */
+  /* potential: V_{ab}(Q) += coef[m] * prod_{k<4, idx>=0} Q[idx[4m+k]] for (a,b) = elec[2m..] */
+  int n_mono;
+  const double *mono_coef;
+  const int *mono_idx;   /* n_mono*4, -1 = unused                                   */
+  const int *mono_elec;  /* n_mono*2 or NULL (all on (0,0))                          */
+  /* KEO: keo_type 10: -1/2 sum_ij d_i G_ij(Q) d_j, G = G0 + sum_k g[i+D*(j+D*k)] Q_k;
+   *      keo_type 1 : sum_ij F2_ij d_i d_j with F2 = -G0/2 constant (second derivative
+   *                   matrices on the diagonal), diagonal in the electronic index. */
+  int keo_type;
+  const double *G0;      /* D*D column-major, NULL = identity                       */
+  const double *g;       /* D*D*D, NULL = 0                                          */
+} evr_problem_desc;
+
+/* sizes reported by evr_sizes(): */
+typedef struct evr_sizes_t {
+  int64_t Np;            /* packed basis size per electronic state                  */
+  int64_t N;             /* Np*nb0, length of one vector                             */
+  int64_t n_terms;       /* Smolyak terms (1 for DP)                                 */
+  int64_t sum_nb;        /* sum over terms of prod nb_i                              */
+  int64_t sum_nq;        /* sum over terms of prod nq_i (grid points)                */
+  int64_t max_nq_term;   /* largest term grid                                        */
+  double  flop_per_hpsi; /* algorithmic FLOP of one H.psi on one real vector         */
+} evr_sizes_t;
+
+/* Replaces the reference's set-up of para_Op/BasisnD for the OpPsi path
+ * (sub_module_basis.f90:391, sub_quadra_SparseBasis.f90:924, BtoG_GtoB_SG4.f90:625,
+ * grid fill sub_OpPsi_SG4.f90:2642-2767).  Builds every table on the host and
+ * uploads them; the potential is evaluated on the device grid. */
+/* device < 0 creates a host-only context: tables are built and can be read back
+ * (evr_get_tables, evr_get_basis, evr_sizes); the device entry points return EVR_EDEVICE. */
+int evr_create(evr_ctx **ctx, const evr_problem_desc *desc, int device);
+int evr_destroy(evr_ctx *ctx);
+const char *evr_last_error(const evr_ctx *ctx);
+int evr_sizes(const evr_ctx *ctx, evr_sizes_t *out);
+
+/* Read back the tables (host arrays sized from evr_sizes; any pointer may be NULL):
+ * term_l[n_terms*D] Smolyak levels (first index fastest order of the reference),
+ * weight[n_terms], map[sum_nb] 0-based packed index or -1, packed[Np*D] 1-based n. */
+int evr_get_tables(const evr_ctx *ctx, int *term_l, double *weight, int *map, int *packed);
+/* 1-D tables of (mode, level): nb, nq, x, w, d0b (nq x nb), d1b, d2b, bgw (nb x nq),
+ * d1gg, d2gg (nq x nq), column-major.  Buffers of at least nq*nq doubles. */
+int evr_get_basis(const evr_ctx *ctx, int mode, int level, int *nb_nq, double *x, double *w, double *d0b,
+                  double *d1b, double *d2b, double *bgw, double *d1gg, double *d2gg);
+/* Potential on the grid, sum_nq*nb0*nb0 values (term-major, point fastest, then (a,b)). */
+int evr_get_vgrid(const evr_ctx *ctx, double *v);
+
+/* H.psi on a block of vectors.
+ * Replaces sub_TabOpPsi (Source_ElVibRot/sub_Operator/sub_OpPsi.f90:701-795) on SG4,
+ * i.e. sub_TabOpPsi_FOR_SGtype4 (sub_OpPsi_SG4.f90:678-979), and on direct-product
+ * bases sub_OpPsi_WITH_MemGrid_BGG_Hamil10 (sub_OpPsi.f90:1528-1794).
+ * evr_hpsi_host: psi/hpsi are HOST arrays; copies in and out are inside the call.
+ * evr_hpsi_device: psi/hpsi are DEVICE pointers; stream-ordered on `stream`
+ *   (a cudaStream_t, NULL = the context's stream); no host synchronisation. */
+int evr_hpsi_host(evr_ctx *ctx, const double *psi, int64_t ld_psi, double *hpsi, int64_t ld_hpsi, int nvec,
+                  int layout, int prec);
+int evr_hpsi_device(evr_ctx *ctx, const double *psi, int64_t ld_psi, double *hpsi, int64_t ld_hpsi, int nvec,
+                    int layout, int prec, void *stream);
+
+/* Launch statistics of the last evr_hpsi_* call (kernels launched, work items). */
+int evr_last_launch_count(const evr_ctx *ctx, int64_t *kernels, int64_t *items);
+/* Device time (ms) of the term-pipeline kernel and of the weighted reduction of the last
+ * H.psi call, from CUDA events recorded on the launching stream (waits for them). */
+int evr_last_kernel_ms(evr_ctx *ctx, float *items_ms, float *reduce_ms);
+
+/*
+ * Block Davidson for the lowest levels.
+ * Replaces sub_propagation_Davidson (Source_ElVibRot/sub_propagation/sub_module_Davidson.f90:54-748):
+ * H.psi of the new vectors, Rayleigh-Ritz on the subspace (FP64 on the GPU), residuals
+ * g_j = sum_i (H psi_i - E_j psi_i) V_ij (MakeResidual_Davidson :1214-1288), new vectors
+ * from the residuals, two classical Gram-Schmidt passes (:1513-1529), restarts.
+ * prec selects the H.psi precision; with EVR_PREC_FP32 the iteration runs on FP32
+ * contractions and finishes with FP64 H.psi refinement so the returned levels are
+ * converged with the FP64 operator.
+ * guess: optional HOST array (N x n_guess column-major); NULL = unit vectors on the
+ *   lowest diagonal elements of H.
+ * eig: out, n_levels eigenvalues (au).  vec: optional HOST out (N x n_levels col-major).
+ * info: optional out [iterations, H.psi count (FP64), H.psi count (FP32), converged]. */
+typedef struct evr_davidson_opts {
+  int n_levels;          /* levels wanted (nb_WP)                                   */
+  int block;             /* start / block size                                      */
+  int max_dim;           /* subspace size that triggers a restart (max_WP)          */
+  int max_it;            /* max_it                                                  */
+  double conv_resi;      /* residual norm tolerance (au)                            */
+  double conv_ene;       /* eigenvalue change tolerance (au)                         */
+  int prec;              /* EVR_PREC_FP64 or EVR_PREC_FP32                           */
+  int n_guess;
+} evr_davidson_opts;
+int evr_davidson(evr_ctx *ctx, const evr_davidson_opts *opts, const double *guess, double *eig, double *vec,
+                 int64_t *info);
+
+/*
+ * Chebyshev propagation of complex wave packets.
+ * Replaces march_cheby (Source_ElVibRot/sub_propagation/sub_module_propa_march.f90:4142-4434):
+ * psi(t+dt) = exp(-i E0 dt) sum_k c_k T_k(Hs) psi(t), c_0 = J_0(r), c_k = 2 J_k(r)
+ * (cof :5734-5757), r = dE*dt/2, Hs = (H - E0)/(dE/2), E0 = (Emin+Emax)/2; the series
+ * stops when |c_k|*||w_k|| < poly_tol.  psi0: HOST complex array (N x npsi interleaved
+ * re/im pairs per element, column-major per packet).  autocorr (HOST, optional):
+ * (nsteps+1) x npsi complex <psi0|psi(t_n)>.  psi_out (HOST, optional): final packets.
+ * info: [max order used, total H.psi count, status]. */
+int evr_cheby_propagate(evr_ctx *ctx, const double *psi0, int npsi, double dt, int nsteps, double emin,
+                        double emax, double poly_tol, int prec, double *autocorr, double *psi_out,
+                        int64_t *info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EVR_GPU_H */

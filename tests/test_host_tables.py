@@ -1,0 +1,71 @@
+"""Host-side tables of the product library against the oracle (no GPU needed)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from evrgpu import spec as S
+from evrgpu import lib as E
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = E.load()
+    with open(os.path.join(ROOT, "include", "evr_gpu.h")) as f:
+        hdr = f.read()
+    declared = set(re.findall(r"^\s*(?:int|const char \*)\s*(evr_\w+)\s*\(", hdr, flags=re.M))
+    assert declared, "no declarations parsed"
+    for name in sorted(declared):
+        assert hasattr(L, name), name
+    assert set(E.EXPORTS) <= declared
+
+
+@pytest.mark.parametrize("mk", [lambda: S.henon_heiles(6, 3), lambda: S.pyrazine_12d(1),
+                                lambda: S.config_dp3(), lambda: S.config_sg4(4, 5, seed=5),
+                                lambda: S.config_sg4(3, 4, seed=7, nq_A=1)])
+def test_tables_match_oracle(mk):
+    spec = mk()
+    pg = E.Problem(spec, device=-1)
+    po = O.OracleProblem(spec)
+    assert (pg.Np, pg.nterm, pg.sum_nb, pg.sum_nq) == (po.Np, po.nterm, po.sum_nb, po.sum_nq)
+    tg, to = pg.tables(), po.tables()
+    for k in ("term_l", "weight", "map", "packed"):
+        assert np.array_equal(tg[k], to[k]), k
+    levels = range(spec.LG + 1) if spec.kind == "sg4" else [0]
+    for d in range(spec.D):
+        for l in levels:
+            bg, bo = pg.basis(d, l), po.basis(d, l)
+            assert (bg["nb"], bg["nq"]) == (bo["nb"], bo["nq"])
+            for k in ("x", "w", "d0b", "d1b", "d2b", "bgw", "d1gg", "d2gg"):
+                scale = max(1.0, np.abs(bo[k]).max())
+                assert np.abs(bg[k] - bo[k]).max() <= 1e-11 * scale, (d, l, k)
+
+
+def test_sg4_6d_l8_sizes_and_flops():
+    pg = E.Problem(S.config_sg4_6d_l8(), device=-1)
+    assert (pg.nterm, pg.Np, pg.sum_nb, pg.sum_nq) == (2975, 40081, 860455, 37769167)
+    assert 5e9 < pg.flop_per_hpsi < 2e10
+
+
+def test_bad_descriptions_are_rejected():
+    spec = S.henon_heiles(3, 2)
+    spec.LB = 5  # LB > LG
+    with pytest.raises(E.EvrError) as ei:
+        E.Problem(spec, device=-1)
+    assert ei.value.code == E.EVR_EINVAL
+    spec = S.henon_heiles(3, 2)
+    spec.mono_idx = spec.mono_idx.copy()
+    spec.mono_idx[0, 0] = 7  # mode out of range
+    with pytest.raises(E.EvrError):
+        E.Problem(spec, device=-1)
+
+
+def test_device_calls_fail_loudly_on_host_only_context():
+    pg = E.Problem(S.henon_heiles(3, 2), device=-1)
+    with pytest.raises(E.EvrError) as ei:
+        pg.hpsi(np.ones(pg.N))
+    assert ei.value.code == E.EVR_EDEVICE
