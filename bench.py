@@ -185,7 +185,10 @@ def main():
     y = torch.empty_like(x)
     y32 = torch.empty_like(x)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    stream = torch.cuda.current_stream().cuda_stream
+    # a dedicated stream: the library launches on it and the CUDA events are recorded on it
+    torch_stream = torch.cuda.Stream()
+    torch.cuda.set_stream(torch_stream)
+    stream = torch_stream.cuda_stream
 
     def step(prec, out):
         p.hpsi_device(x.data_ptr(), NVEC, out.data_ptr(), NVEC, NVEC, layout=E.LAYOUT_INTERLEAVED, prec=prec,

@@ -112,6 +112,13 @@ int evr_get_vgrid(const evr_ctx* c0, double* v) {
   return EVR_OK;
 }
 
+int evr_set_operator(evr_ctx* c, int form) {
+  if (!c) return EVR_EINVAL;
+  if (form != EVR_OP_H && form != EVR_OP_HT && form != EVR_OP_HSYM) return set_error(c, EVR_EINVAL, "operator form");
+  c->op_form = form;
+  return EVR_OK;
+}
+
 int evr_hpsi_device(evr_ctx* c, const double* psi, int64_t ld_psi, double* hpsi, int64_t ld_hpsi, int nvec, int layout,
                     int prec, void* stream) {
   if (!c) return EVR_EINVAL;
@@ -123,18 +130,25 @@ int evr_hpsi_device(evr_ctx* c, const double* psi, int64_t ld_psi, double* hpsi,
   EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
   if (layout == EVR_LAYOUT_INTERLEAVED) {
     if (ld_psi < nvec || ld_hpsi < nvec) return set_error(c, EVR_EINVAL, "interleaved ld < nvec");
-    return hpsi_interleaved(c, psi, ld_psi, hpsi, ld_hpsi, nvec, prec, s);
+    return hpsi_blocks(c, psi, ld_psi, hpsi, ld_hpsi, nvec, prec, s, c->op_form);
   }
   if (layout != EVR_LAYOUT_COLMAJOR) return set_error(c, EVR_EINVAL, "unknown layout");
   if (ld_psi < N || ld_hpsi < N) return set_error(c, EVR_EINVAL, "column-major ld < N");
-  int rc = ensure_workspace(c, nvec, prec);
-  if (rc) return rc;
-  double* xin = (double*)c->ws.xin;
-  double* xout = (double*)c->ws.xout;
-  if ((rc = transpose_to_interleaved(psi, ld_psi, xin, nvec, N, nvec, s))) return set_error(c, rc, "transpose");
-  if ((rc = hpsi_interleaved(c, xin, nvec, xout, nvec, nvec, prec, s))) return rc;
-  if ((rc = transpose_from_interleaved(xout, nvec, hpsi, ld_hpsi, N, nvec, s))) return set_error(c, rc, "transpose");
-  c->last_kernels += 2;
+  int64_t kernels = 0;
+  for (int v0 = 0; v0 < nvec; v0 += kMaxBlock) {
+    const int nb = std::min(kMaxBlock, nvec - v0);
+    int rc = ensure_workspace(c, nb, prec);
+    if (rc) return rc;
+    double* xin = c->ws.xin;
+    double* xout = c->ws.xout;
+    if ((rc = transpose_to_interleaved(psi + v0 * ld_psi, ld_psi, xin, nb, N, nb, s)))
+      return set_error(c, rc, "transpose");
+    if ((rc = hpsi_interleaved(c, xin, nb, xout, nb, nb, prec, s, c->op_form))) return rc;
+    if ((rc = transpose_from_interleaved(xout, nb, hpsi + v0 * ld_hpsi, ld_hpsi, N, nb, s)))
+      return set_error(c, rc, "transpose");
+    kernels += c->last_kernels + 2;
+  }
+  c->last_kernels = kernels;
   return EVR_OK;
 }
 
@@ -143,37 +157,45 @@ int evr_hpsi_host(evr_ctx* c, const double* psi, int64_t ld_psi, double* hpsi, i
   if (!c) return EVR_EINVAL;
   if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
   if (!psi || !hpsi || nvec < 1) return set_error(c, EVR_EINVAL, "evr_hpsi_host: null pointer or nvec < 1");
+  if (prec != EVR_PREC_FP64 && prec != EVR_PREC_FP32) return set_error(c, EVR_EINVAL, "unknown precision");
+  if (layout != EVR_LAYOUT_INTERLEAVED && layout != EVR_LAYOUT_COLMAJOR) return set_error(c, EVR_EINVAL, "layout");
   const int64_t N = c->hp.Np * c->hp.nb0;
+  if (layout == EVR_LAYOUT_INTERLEAVED && (ld_psi < nvec || ld_hpsi < nvec))
+    return set_error(c, EVR_EINVAL, "interleaved ld < nvec");
+  if (layout == EVR_LAYOUT_COLMAJOR && (ld_psi < N || ld_hpsi < N)) return set_error(c, EVR_EINVAL, "column-major ld < N");
   EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
-  int rc = ensure_workspace(c, nvec, prec);
-  if (rc) return rc;
-  double* xin = (double*)c->ws.xin;
-  double* xout = (double*)c->ws.xout;
   cudaStream_t s = c->stream;
-  if (layout == EVR_LAYOUT_INTERLEAVED) {
-    if (ld_psi < nvec || ld_hpsi < nvec) return set_error(c, EVR_EINVAL, "interleaved ld < nvec");
-    EVR_CU(cudaMemcpy2DAsync(xin, nvec * sizeof(double), psi, ld_psi * sizeof(double), nvec * sizeof(double), N,
-                             cudaMemcpyHostToDevice, s), "H2D");
-    if ((rc = hpsi_interleaved(c, xin, nvec, xout, nvec, nvec, prec, s))) return rc;
-    EVR_CU(cudaMemcpy2DAsync(hpsi, ld_hpsi * sizeof(double), xout, nvec * sizeof(double), nvec * sizeof(double), N,
-                             cudaMemcpyDeviceToHost, s), "D2H");
-  } else if (layout == EVR_LAYOUT_COLMAJOR) {
-    if (ld_psi < N || ld_hpsi < N) return set_error(c, EVR_EINVAL, "column-major ld < N");
-    // column-major staging in xout, transposed on the device into xin
-    EVR_CU(cudaMemcpy2DAsync(xout, N * sizeof(double), psi, ld_psi * sizeof(double), N * sizeof(double), nvec,
-                             cudaMemcpyHostToDevice, s), "H2D");
-    if ((rc = transpose_to_interleaved(xout, N, xin, nvec, N, nvec, s))) return set_error(c, rc, "transpose");
-    if ((rc = hpsi_interleaved(c, xin, nvec, xout, nvec, nvec, prec, s))) return rc;
-    if ((rc = transpose_from_interleaved(xout, nvec, xin, N, N, nvec, s))) return set_error(c, rc, "transpose");
-    EVR_CU(cudaMemcpy2DAsync(hpsi, ld_hpsi * sizeof(double), xin, N * sizeof(double), N * sizeof(double), nvec,
-                             cudaMemcpyDeviceToHost, s), "D2H");
-    c->last_kernels += 2;
-  } else {
-    return set_error(c, EVR_EINVAL, "unknown layout");
+  int64_t kernels = 0;
+  for (int v0 = 0; v0 < nvec; v0 += kMaxBlock) {
+    const int nb = std::min(kMaxBlock, nvec - v0);
+    int rc = ensure_workspace(c, nb, prec);
+    if (rc) return rc;
+    double* xin = c->ws.xin;
+    double* xout = c->ws.xout;
+    if (layout == EVR_LAYOUT_INTERLEAVED) {
+      EVR_CU(cudaMemcpy2DAsync(xin, nb * sizeof(double), psi + v0, ld_psi * sizeof(double), nb * sizeof(double), N,
+                               cudaMemcpyHostToDevice, s), "H2D");
+      if ((rc = hpsi_interleaved(c, xin, nb, xout, nb, nb, prec, s, c->op_form))) return rc;
+      EVR_CU(cudaMemcpy2DAsync(hpsi + v0, ld_hpsi * sizeof(double), xout, nb * sizeof(double), nb * sizeof(double), N,
+                               cudaMemcpyDeviceToHost, s), "D2H");
+      kernels += c->last_kernels;
+    } else {
+      // column-major staging in xout, transposed on the device into xin
+      EVR_CU(cudaMemcpy2DAsync(xout, N * sizeof(double), psi + v0 * ld_psi, ld_psi * sizeof(double),
+                               N * sizeof(double), nb, cudaMemcpyHostToDevice, s), "H2D");
+      if ((rc = transpose_to_interleaved(xout, N, xin, nb, N, nb, s))) return set_error(c, rc, "transpose");
+      if ((rc = hpsi_interleaved(c, xin, nb, xout, nb, nb, prec, s, c->op_form))) return rc;
+      kernels += c->last_kernels + 2;
+      if ((rc = transpose_from_interleaved(xout, nb, xin, N, N, nb, s))) return set_error(c, rc, "transpose");
+      EVR_CU(cudaMemcpy2DAsync(hpsi + v0 * ld_hpsi, ld_hpsi * sizeof(double), xin, N * sizeof(double),
+                               N * sizeof(double), nb, cudaMemcpyDeviceToHost, s), "D2H");
+    }
   }
+  c->last_kernels = kernels;
   EVR_CU(cudaStreamSynchronize(s), "evr_hpsi_host");
   return EVR_OK;
 }
+
 
 int evr_last_kernel_ms(evr_ctx* c, float* items_ms, float* reduce_ms) {
   if (!c || c->host_only) return EVR_EINVAL;

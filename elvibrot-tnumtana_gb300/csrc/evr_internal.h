@@ -52,11 +52,13 @@ struct WorkItem {
 
 struct HostProblem {
   int kind = 0, D = 0, nb0 = 1, LG = 0, LB = 0, keo_type = 10;
+  bool symmetric = true;                  // every 1-D basis has nq == nb (operator symmetric)
   std::vector<std::vector<Basis1D>> bas;  // [mode][level]
   std::vector<std::vector<int>> ltab;     // l(n), 1-based n
   std::vector<int> term_l;                // n_terms x D
   std::vector<double> weight;
   std::vector<TermDesc> terms;
+  std::vector<TermDesc> termsT;           // same terms, matrix offsets of the transposed operator
   int64_t Np = 0, sum_nb = 0, sum_nq = 0, max_nq = 0, max_nb = 0;
   std::vector<int> packed;                // Np x D
   std::vector<int> map;                   // sum_nb (packed index or -1)
@@ -81,6 +83,7 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
 // Device copy of the problem and the buffers of the H.psi pipeline.
 struct DeviceProblem {
   TermDesc* terms = nullptr;
+  TermDesc* termsT = nullptr;
   double* mats = nullptr;
   float* mats32 = nullptr;
   double* vgrid = nullptr;          // sum_nq * nb0^2
@@ -97,25 +100,36 @@ struct DeviceProblem {
   double* e0diag = nullptr;
 };
 
-struct Workspace {
-  // keyed by (nvec, prec)
-  int nvec = -1, prec = -1;
+// Work decomposition of one (nvec, precision) pair.
+struct ItemSet {
+  int nvec = 0, prec = 0;
   WorkItem* items = nullptr;
   int n_items = 0;
+};
+
+struct Workspace {
+  std::vector<ItemSet> sets;        // cached decompositions
   int* counter = nullptr;
   void* slab = nullptr;             // per-CTA global scratch
-  size_t slab_per_cta = 0;          // elements
-  void* ht = nullptr;               // term-basis output (sum_nb*nb0 x nvec)
-  void* xin = nullptr;              // interleaved input copy (when converting layouts)
-  void* xout = nullptr;
+  size_t slab_per_cta_bytes = 0;
+  int cap = 0;                      // vector capacity of ht/ht2/xin/xout
+  void* ht = nullptr;               // term-basis output (sum_nb*nb0 x cap)
+  void* ht2 = nullptr;              // second output for the symmetrised operator
+  double* xin = nullptr;            // interleaved copies (layout conversions)
+  double* xout = nullptr;
   int grid = 0, smem_bytes = 0;
 };
+
+// operator forms
+enum OpForm { OP_H = 0, OP_HT = 1, OP_HSYM = 2 };
 
 }  // namespace evr
 
 struct evr_ctx {
   int device = 0;
   bool host_only = false;           // created with device < 0: tables only
+  int op_form = 0;                  // EVR_OP_H, EVR_OP_HT or EVR_OP_HSYM
+  bool capturing = false;           // inside a stream capture: no event records
   cudaStream_t stream = nullptr;
   evr::HostProblem hp;
   evr::DeviceProblem dp;
@@ -137,9 +151,14 @@ int upload_problem(evr_ctx* c);
 void free_problem(evr_ctx* c);
 int ensure_workspace(evr_ctx* c, int nvec, int prec);
 void free_workspace(evr_ctx* c);
-// H.psi on interleaved device blocks (ld >= nvec); returns a status.
+// H.psi (op = OP_H), H^T.psi or (H+H^T)/2.psi on interleaved device blocks (ld >= nvec),
+// nvec <= kMaxBlock per call; returns a status.
+constexpr int kMaxBlock = 64;
 int hpsi_interleaved(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, int prec,
-                     cudaStream_t s);
+                     cudaStream_t s, int op = OP_H);
+// any nvec: splits into blocks of kMaxBlock vectors
+int hpsi_blocks(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, int prec,
+                cudaStream_t s, int op = OP_H);
 int transpose_to_interleaved(const double* in, int64_t ld_in, double* out, int64_t ld_out, int64_t N, int nvec,
                              cudaStream_t s);
 int transpose_from_interleaved(const double* in, int64_t ld_in, double* out, int64_t ld_out, int64_t N, int nvec,

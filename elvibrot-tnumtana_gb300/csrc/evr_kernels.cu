@@ -49,15 +49,45 @@ struct ItemParams {
   int64_t Np;
   int D, nb0, keo_type;
   int has_offdiag;         // type 1 with off-diagonal F2 terms
+  int vtrans;              // 1: V_ab read as V_ba (transposed operator)
 };
 
 // out(a, m, b, v) = alpha * sum_k mat[m + M*k] * in(a, k, b, v)  (+ out if acc)
 // element (a, k, b, v) of a tensor with vector stride ld lives at ((a + A*(k + K*b))*ld + v).
+// four consecutive matrix coefficients in one 16-byte read-only load
+__device__ __forceinline__ void load4(const float* p, float& a, float& b, float& c, float& d) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+  a = v.x; b = v.y; c = v.z; d = v.w;
+}
+__device__ __forceinline__ void load4(const double* p, double& a, double& b, double& c, double& d) {
+  const double2 u = __ldg(reinterpret_cast<const double2*>(p));
+  const double2 w = __ldg(reinterpret_cast<const double2*>(p) + 1);
+  a = u.x; b = u.y; c = w.x; d = w.y;
+}
+
+// acc[m] += mat[m + ldm*k] * xk for m < M; the matrix columns are padded to ldm = 4*ceil(M/4)
+template <typename T, int MAXM>
+__device__ __forceinline__ void fma_column(T (&accv)[MAXM], const T* __restrict__ mk, T xk, int M) {
+#pragma unroll
+  for (int m4 = 0; m4 < MAXM; m4 += 4)
+    if (m4 < M) {
+      T c0, c1, c2, c3;
+      load4(mk + m4, c0, c1, c2, c3);
+      accv[m4] = fma(c0, xk, accv[m4]);
+      accv[m4 + 1] = fma(c1, xk, accv[m4 + 1]);
+      accv[m4 + 2] = fma(c2, xk, accv[m4 + 2]);
+      accv[m4 + 3] = fma(c3, xk, accv[m4 + 3]);
+    }
+}
+
+// Loads of a fibre are issued eight at a time so that each thread keeps eight memory
+// requests in flight before the FMAs that consume them.
 template <typename T, int MAXM>
 __device__ __forceinline__ void contract_m(const T* __restrict__ in, int64_t ldi, T* __restrict__ out, int64_t ldo,
                                            int A, int K, int M, int B, int Vt, const T* __restrict__ mat, T alpha,
                                            bool acc) {
   const int ncol = A * B * Vt;
+  const int ldm = (M + 3) & ~3;
   for (int col = threadIdx.x; col < ncol; col += blockDim.x) {
     const int v = col % Vt;
     const int r = col / Vt;
@@ -67,12 +97,13 @@ __device__ __forceinline__ void contract_m(const T* __restrict__ in, int64_t ldi
     T accv[MAXM];
 #pragma unroll
     for (int m = 0; m < MAXM; ++m) accv[m] = T(0);
-    for (int k = 0; k < K; ++k) {
-      const T xk = ip[k * istr];
-      const T* mk = mat + M * k;
+    for (int k0 = 0; k0 < K; k0 += 8) {
+      T x[8];
 #pragma unroll
-      for (int m = 0; m < MAXM; ++m)
-        if (m < M) accv[m] = fma(__ldg(mk + m), xk, accv[m]);
+      for (int j = 0; j < 8; ++j) x[j] = (k0 + j < K) ? ip[(k0 + j) * istr] : T(0);
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (k0 + j < K) fma_column<T, MAXM>(accv, mat + ldm * (k0 + j), x[j], M);
     }
     T* op = out + (int64_t)(a + (int64_t)A * M * b) * ldo + v;
     const int64_t ostr = (int64_t)A * ldo;
@@ -102,19 +133,23 @@ __device__ __forceinline__ void gather_contract_m(const double* __restrict__ x, 
                                                   int64_t eoff, T* __restrict__ out, int K, int M, int B, int Vt,
                                                   const T* __restrict__ mat) {
   const int ncol = B * Vt;
+  const int ldm = (M + 3) & ~3;
   for (int col = threadIdx.x; col < ncol; col += blockDim.x) {
     const int v = col % Vt;
     const int b = col / Vt;
     T accv[MAXM];
 #pragma unroll
     for (int m = 0; m < MAXM; ++m) accv[m] = T(0);
-    for (int k = 0; k < K; ++k) {
-      const int p = __ldg(mp + k + K * b);
-      const T xk = (p >= 0) ? (T)__ldg(x + (p + eoff) * ldx + v) : T(0);
-      const T* mk = mat + M * k;
+    for (int k0 = 0; k0 < K; k0 += 8) {
+      int pk[8];
 #pragma unroll
-      for (int m = 0; m < MAXM; ++m)
-        if (m < M) accv[m] = fma(__ldg(mk + m), xk, accv[m]);
+      for (int j = 0; j < 8; ++j) pk[j] = (k0 + j < K) ? __ldg(mp + k0 + j + K * b) : -1;
+      T xv[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) xv[j] = (pk[j] >= 0) ? (T)__ldg(x + (pk[j] + eoff) * ldx + v) : T(0);
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (k0 + j < K) fma_column<T, MAXM>(accv, mat + ldm * (k0 + j), xv[j], M);
     }
     T* op = out + (int64_t)M * b * Vt + v;
 #pragma unroll
@@ -186,7 +221,10 @@ __global__ void __launch_bounds__(kThreads) hpsi_items_kernel(ItemParams<T> p) {
         const int q = (int)(idx / Vt);
         for (int a = 0; a < nb0; ++a) {
           T s = T(0);
-          for (int b = 0; b < nb0; ++b) s = fma(__ldg(Vt_ + (int64_t)(a + nb0 * b) * NQ + q), X0[b * stride + idx], s);
+          for (int b = 0; b < nb0; ++b) {
+            const int ab = p.vtrans ? (b + nb0 * a) : (a + nb0 * b);
+            s = fma(__ldg(Vt_ + (int64_t)ab * NQ + q), X0[b * stride + idx], s);
+          }
           X1[a * stride + idx] = s;
         }
       }
@@ -310,11 +348,12 @@ __global__ void __launch_bounds__(kThreads) hpsi_items_kernel(ItemParams<T> p) {
   }
 }
 
-// y[k*ldy + v] = sum_{e in row k} w_e * ht[src_e*ldh + v]   (FP64 accumulation)
+// y[k*ldy + v] = scale * sum_{e in row k} w_e * (ht[src_e*ldh + v] (+ ht2[...]))   (FP64 accumulation)
 template <typename T>
 __global__ void csr_reduce_kernel(const int64_t* __restrict__ ptr, const int64_t* __restrict__ src,
-                                  const double* __restrict__ wt, const T* __restrict__ ht, int64_t ldh,
-                                  double* __restrict__ y, int64_t ldy, int64_t N, int nvec) {
+                                  const double* __restrict__ wt, const T* __restrict__ ht, const T* __restrict__ ht2,
+                                  int64_t ldh, double scale, double* __restrict__ y, int64_t ldy, int64_t N,
+                                  int nvec) {
   const int64_t total = N * nvec;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
@@ -322,8 +361,15 @@ __global__ void csr_reduce_kernel(const int64_t* __restrict__ ptr, const int64_t
     const int v = (int)(idx - k * nvec);
     double s = 0.0;
     const int64_t e1 = __ldg(ptr + k + 1);
-    for (int64_t e = __ldg(ptr + k); e < e1; ++e) s = fma(__ldg(wt + e), (double)ht[__ldg(src + e) * ldh + v], s);
-    y[k * ldy + v] = s;
+    if (ht2) {
+      for (int64_t e = __ldg(ptr + k); e < e1; ++e) {
+        const int64_t o = __ldg(src + e) * ldh + v;
+        s = fma(__ldg(wt + e), (double)ht[o] + (double)ht2[o], s);
+      }
+    } else {
+      for (int64_t e = __ldg(ptr + k); e < e1; ++e) s = fma(__ldg(wt + e), (double)ht[__ldg(src + e) * ldh + v], s);
+    }
+    y[k * ldy + v] = scale * s;
   }
 }
 
@@ -442,6 +488,7 @@ int upload_problem(evr_ctx* c) {
   DeviceProblem& d = c->dp;
   int rc;
   if ((rc = upload(c, &d.terms, P.terms))) return rc;
+  if ((rc = upload(c, &d.termsT, P.termsT))) return rc;
   if ((rc = upload(c, &d.mats, P.mat_pool))) return rc;
   if ((rc = upload(c, &d.map, P.map))) return rc;
   if ((rc = upload(c, &d.csr_ptr, P.csr_ptr))) return rc;
@@ -484,8 +531,8 @@ int upload_problem(evr_ctx* c) {
 
 void free_problem(evr_ctx* c) {
   DeviceProblem& d = c->dp;
-  void* ptrs[] = {d.terms, d.mats, d.mats32, d.vgrid, d.vgrid32, d.map, d.csr_ptr, d.csr_src, d.csr_w, d.G0, d.g,
-                  d.mono_coef, d.mono_idx, d.mono_elec, d.e0diag, c->dp_ggrid, c->dp_ggrid32};
+  void* ptrs[] = {d.terms, d.termsT, d.mats, d.mats32, d.vgrid, d.vgrid32, d.map, d.csr_ptr, d.csr_src, d.csr_w,
+                  d.G0, d.g, d.mono_coef, d.mono_idx, d.mono_elec, d.e0diag, c->dp_ggrid, c->dp_ggrid32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   d = DeviceProblem();
@@ -495,130 +542,179 @@ void free_problem(evr_ctx* c) {
 
 void free_workspace(evr_ctx* c) {
   Workspace& w = c->ws;
-  void* ptrs[] = {w.items, w.counter, w.slab, w.ht, w.xin, w.xout};
+  for (ItemSet& s : w.sets)
+    if (s.items) cudaFree(s.items);
+  void* ptrs[] = {w.counter, w.slab, w.ht, w.ht2, w.xin, w.xout};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   w = Workspace();
 }
 
+static int smem_budget_bytes(evr_ctx* c) {
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device) != cudaSuccess) return 0;
+  const int ctas_per_sm = 2;
+  return std::min(optin, (int)(228 * 1024 / ctas_per_sm) - 2048);
+}
+
 // Work decomposition for a block of nvec vectors: per term the widest vector tile whose
 // buffers fit the shared-memory budget; terms that do not fit even with one vector run
-// from the CTA's global slab.  Items are ordered by decreasing cost.
+// from the CTA's global slab.  Items are ordered by decreasing cost.  Buffers are sized
+// once for kMaxBlock vectors in FP64 and shared by every decomposition.
 int ensure_workspace(evr_ctx* c, int nvec, int prec) {
   Workspace& w = c->ws;
-  if (w.nvec == nvec && w.prec == prec && w.items) return EVR_OK;
-  free_workspace(c);
+  if (nvec < 1 || nvec > kMaxBlock) return set_error(c, EVR_EINVAL, "block of more than 64 vectors");
   const HostProblem& P = c->hp;
+  int rc = EVR_OK;
+  if (!w.counter) {
+    const int smem = smem_budget_bytes(c);
+    if (smem <= 0) return set_error(c, EVR_EDEVICE, "shared-memory attribute");
+    w.smem_bytes = smem;
+    w.grid = c->num_sms * 2;
+    size_t slab = 0;
+    for (const TermDesc& Tm : P.terms) {
+      size_t fp1 = footprint_elems<double>(P, Tm, 1) * sizeof(double);
+      if (fp1 > (size_t)smem) slab = std::max(slab, fp1);
+    }
+    // FP32 items use the same slab (half the bytes per element)
+    w.slab_per_cta_bytes = slab;
+    w.counter = (int*)dev_alloc<int>(1, rc);
+    if (rc) return set_error(c, rc, "workspace allocation (counter)");
+    if (slab) {
+      w.slab = dev_alloc<unsigned char>(slab * w.grid, rc);
+      if (rc) return set_error(c, rc, "workspace allocation (slab)");
+    }
+    w.cap = kMaxBlock;
+    w.ht = dev_alloc<double>((size_t)P.sum_nb * P.nb0 * w.cap, rc);
+    if (rc) return set_error(c, rc, "workspace allocation (term-basis output)");
+    const size_t xe = (size_t)P.Np * P.nb0 * w.cap;
+    w.xin = (double*)dev_alloc<double>(xe, rc);
+    if (rc) return set_error(c, rc, "workspace allocation (xin)");
+    w.xout = (double*)dev_alloc<double>(xe, rc);
+    if (rc) return set_error(c, rc, "workspace allocation (xout)");
+    EVR_CU(cudaFuncSetAttribute(hpsi_items_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "attr");
+    EVR_CU(cudaFuncSetAttribute(hpsi_items_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "attr");
+  }
+  for (const ItemSet& s : w.sets)
+    if (s.nvec == nvec && s.prec == prec) return EVR_OK;
   const size_t esz = prec == EVR_PREC_FP32 ? sizeof(float) : sizeof(double);
-  int smem_budget = 0;
-  EVR_CU(cudaDeviceGetAttribute(&smem_budget, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attr");
-  const int ctas_per_sm = 2;
-  smem_budget = std::min(smem_budget, (int)(228 * 1024 / ctas_per_sm) - 2048);
   std::vector<WorkItem> items;
-  size_t slab_elems = 0;
-  int max_vt_smem = 1;
   for (int t = 0; t < (int)P.terms.size(); ++t) {
     const TermDesc& Tm = P.terms[t];
     if (Tm.weight == 0.0) continue;
     int vt = 1;
-    size_t fp1 = (prec == EVR_PREC_FP32) ? footprint_elems<float>(P, Tm, 1) : footprint_elems<double>(P, Tm, 1);
-    bool in_smem = fp1 * esz <= (size_t)smem_budget;
-    if (in_smem) {
-      while (vt * 2 <= nvec && vt * 2 <= 32 && fp1 * (size_t)(vt * 2) * esz <= (size_t)smem_budget) vt *= 2;
-      max_vt_smem = std::max(max_vt_smem, vt);
-    } else {
-      slab_elems = std::max(slab_elems, fp1);
-    }
+    const size_t fp1 = footprint_elems<double>(P, Tm, 1) * esz;
+    const bool in_smem = fp1 <= (size_t)w.smem_bytes;
+    if (in_smem)
+      while (vt * 2 <= nvec && vt * 2 <= 32 && fp1 * (size_t)(vt * 2) <= (size_t)w.smem_bytes) vt *= 2;
     for (int v0 = 0; v0 < nvec; v0 += vt) items.push_back(WorkItem{t, v0, std::min(vt, nvec - v0), in_smem ? 1 : 0});
   }
   std::stable_sort(items.begin(), items.end(), [&](const WorkItem& a, const WorkItem& b) {
     return (int64_t)P.terms[a.term].NQ * a.vt > (int64_t)P.terms[b.term].NQ * b.vt;
   });
-  int rc = EVR_OK;
-  w.n_items = (int)items.size();
-  w.items = (WorkItem*)dev_alloc<WorkItem>(items.size(), rc);
+  ItemSet s;
+  s.nvec = nvec;
+  s.prec = prec;
+  s.n_items = (int)items.size();
+  s.items = (WorkItem*)dev_alloc<WorkItem>(items.size(), rc);
   if (rc) return set_error(c, rc, "workspace allocation (items)");
-  EVR_CU(cudaMemcpy(w.items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice), "items");
-  w.counter = (int*)dev_alloc<int>(1, rc);
-  if (rc) return set_error(c, rc, "workspace allocation (counter)");
-  w.grid = c->num_sms * ctas_per_sm;
-  w.smem_bytes = smem_budget;
-  w.slab_per_cta = slab_elems;
-  if (slab_elems) {
-    w.slab = esz == 4 ? dev_alloc<float>(slab_elems * w.grid, rc) : dev_alloc<double>(slab_elems * w.grid, rc);
-    if (rc) return set_error(c, rc, "workspace allocation (slab)");
-  }
-  const size_t ht_elems = (size_t)P.sum_nb * P.nb0 * nvec;
-  w.ht = esz == 4 ? dev_alloc<float>(ht_elems, rc) : dev_alloc<double>(ht_elems, rc);
-  if (rc) return set_error(c, rc, "workspace allocation (term-basis output)");
-  const size_t xe = (size_t)P.Np * P.nb0 * nvec;
-  w.xin = dev_alloc<double>(xe, rc);
-  if (rc) return set_error(c, rc, "workspace allocation (xin)");
-  w.xout = dev_alloc<double>(xe, rc);
-  if (rc) return set_error(c, rc, "workspace allocation (xout)");
-  if (esz == 4) {
-    EVR_CU(cudaFuncSetAttribute(hpsi_items_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_budget),
-           "smem attr");
-  } else {
-    EVR_CU(cudaFuncSetAttribute(hpsi_items_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_budget),
-           "smem attr");
-  }
-  w.nvec = nvec;
-  w.prec = prec;
+  EVR_CU(cudaMemcpy(s.items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice), "items");
+  w.sets.push_back(s);
   return EVR_OK;
 }
 
 template <typename T>
-static int run_items(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, cudaStream_t s) {
+static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, int vtrans, T* ht, const double* x,
+                        int64_t ldx, int nvec, cudaStream_t s) {
   const HostProblem& P = c->hp;
   Workspace& w = c->ws;
   ItemParams<T> p;
   const bool f32 = sizeof(T) == 4;
-  p.terms = c->dp.terms;
+  p.terms = terms;
   p.mats = f32 ? (const T*)c->dp.mats32 : (const T*)c->dp.mats;
   p.vgrid = f32 ? (const T*)c->dp.vgrid32 : (const T*)c->dp.vgrid;
   p.ggrid = f32 ? (const T*)c->dp_ggrid32 : (const T*)c->dp_ggrid;
   p.G0 = c->dp.G0;
   p.map = c->dp.map;
-  p.items = w.items;
-  p.n_items = w.n_items;
+  p.items = set.items;
+  p.n_items = set.n_items;
   p.counter = w.counter;
   p.slab = (T*)w.slab;
-  p.slab_per_cta = (int64_t)w.slab_per_cta;
+  p.slab_per_cta = (int64_t)(w.slab_per_cta_bytes / sizeof(T));
   p.x = x;
   p.ldx = ldx;
-  p.ht = (T*)w.ht;
+  p.ht = ht;
   p.ldh = nvec;
   p.Np = P.Np;
   p.D = P.D;
   p.nb0 = P.nb0;
   p.keo_type = P.keo_type;
+  p.vtrans = vtrans;
   p.has_offdiag = 0;
   if (P.keo_type == 1)
     for (int i = 0; i < P.D; ++i)
       for (int j = i + 1; j < P.D; ++j) p.has_offdiag |= (P.G0[i + (size_t)P.D * j] != 0.0);
   EVR_CU(cudaMemsetAsync(w.counter, 0, sizeof(int), s), "memset counter");
-  EVR_CU(cudaEventRecord(c->ev[0], s), "event");
   hpsi_items_kernel<T><<<w.grid, kThreads, w.smem_bytes, s>>>(p);
   EVR_CU(cudaGetLastError(), "hpsi_items_kernel launch");
-  EVR_CU(cudaEventRecord(c->ev[1], s), "event");
+  return EVR_OK;
+}
+
+template <typename T>
+static int run_items(evr_ctx* c, const ItemSet& set, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec,
+                     cudaStream_t s, int op) {
+  const HostProblem& P = c->hp;
+  Workspace& w = c->ws;
+  if (op == OP_HSYM && !w.ht2) {
+    int rc = EVR_OK;
+    w.ht2 = dev_alloc<double>((size_t)P.sum_nb * P.nb0 * w.cap, rc);
+    if (rc) return set_error(c, rc, "workspace allocation (second term-basis output)");
+  }
+  int rc;
+  if (!c->capturing) EVR_CU(cudaEventRecord(c->ev[0], s), "event");
+  if (op == OP_H || op == OP_HSYM)
+    if ((rc = launch_items<T>(c, set, c->dp.terms, 0, (T*)w.ht, x, ldx, nvec, s))) return rc;
+  if (op == OP_HT || op == OP_HSYM)
+    if ((rc = launch_items<T>(c, set, c->dp.termsT, 1, (T*)(op == OP_HT ? w.ht : w.ht2), x, ldx, nvec, s))) return rc;
+  if (!c->capturing) EVR_CU(cudaEventRecord(c->ev[1], s), "event");
   const int64_t N = P.Np * P.nb0;
   int rblocks = (int)std::min<int64_t>((N * nvec + 255) / 256, (int64_t)c->num_sms * 16);
-  csr_reduce_kernel<T><<<rblocks, 256, 0, s>>>(c->dp.csr_ptr, c->dp.csr_src, c->dp.csr_w, (const T*)w.ht, nvec, y, ldy,
-                                                N, nvec);
+  csr_reduce_kernel<T><<<rblocks, 256, 0, s>>>(c->dp.csr_ptr, c->dp.csr_src, c->dp.csr_w, (const T*)w.ht,
+                                                op == OP_HSYM ? (const T*)w.ht2 : nullptr, nvec,
+                                                op == OP_HSYM ? 0.5 : 1.0, y, ldy, N, nvec);
   EVR_CU(cudaGetLastError(), "csr_reduce_kernel launch");
-  EVR_CU(cudaEventRecord(c->ev[2], s), "event");
-  c->last_kernels = 2;
-  c->last_items = w.n_items;
+  if (!c->capturing) EVR_CU(cudaEventRecord(c->ev[2], s), "event");
+  c->last_kernels = op == OP_HSYM ? 3 : 2;
+  c->last_items = (int64_t)set.n_items * (op == OP_HSYM ? 2 : 1);
   return EVR_OK;
 }
 
 int hpsi_interleaved(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, int prec,
-                     cudaStream_t s) {
+                     cudaStream_t s, int op) {
   int rc = ensure_workspace(c, nvec, prec);
   if (rc) return rc;
-  if (prec == EVR_PREC_FP32) return run_items<float>(c, x, ldx, y, ldy, nvec, s);
-  return run_items<double>(c, x, ldx, y, ldy, nvec, s);
+  const ItemSet* set = nullptr;
+  for (const ItemSet& it : c->ws.sets)
+    if (it.nvec == nvec && it.prec == prec) set = &it;
+  if (!set) return set_error(c, EVR_EINVAL, "no work decomposition");
+  const ItemSet cp = *set;
+  if (prec == EVR_PREC_FP32) return run_items<float>(c, cp, x, ldx, y, ldy, nvec, s, op);
+  return run_items<double>(c, cp, x, ldx, y, ldy, nvec, s, op);
+}
+
+int hpsi_blocks(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, int prec, cudaStream_t s,
+                int op) {
+  int64_t k = 0, items = 0;
+  for (int v0 = 0; v0 < nvec; v0 += kMaxBlock) {
+    const int nb = std::min(kMaxBlock, nvec - v0);
+    int rc = hpsi_interleaved(c, x + v0, ldx, y + v0, ldy, nb, prec, s, op);
+    if (rc) return rc;
+    k += c->last_kernels;
+    items += c->last_items;
+  }
+  c->last_kernels = k;
+  c->last_items = items;
+  return EVR_OK;
 }
 
 int transpose_to_interleaved(const double* in, int64_t ld_in, double* out, int64_t ld_out, int64_t N, int nvec,

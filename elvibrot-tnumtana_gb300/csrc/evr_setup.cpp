@@ -263,20 +263,42 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
   }
 
   // matrix pool
+  // matrices of H and of its transpose: H^T applies (d0b^T w)^T = w d0b on the way to the
+  // grid, d1gg^T / d2gg^T on the grid and d0b^T on the way back
   std::vector<std::vector<int>> off_d0(D), off_bgw(D), off_d1(D), off_d2(D), off_x(D);
+  std::vector<std::vector<int>> offT_in(D), offT_out(D), offT_d1(D), offT_d2(D);
+  auto transpose = [](const std::vector<double>& a, int r, int cc) {
+    std::vector<double> t((size_t)r * cc);
+    for (int i = 0; i < r; ++i) for (int j = 0; j < cc; ++j) t[j + (size_t)cc * i] = a[i + (size_t)r * j];
+    return t;
+  };
+  P.symmetric = true;
   for (int i = 0; i < D; ++i) {
     int nl = (int)P.bas[i].size();
     off_d0[i].resize(nl); off_bgw[i].resize(nl); off_d1[i].resize(nl); off_d2[i].resize(nl); off_x[i].resize(nl);
+    offT_in[i].resize(nl); offT_out[i].resize(nl); offT_d1[i].resize(nl); offT_d2[i].resize(nl);
     for (int L = 0; L < nl; ++L) {
       const Basis1D& b = P.bas[i][L];
-      auto put = [&](const std::vector<double>& v) {
+      if (b.nq != b.nb) P.symmetric = false;
+      // column-major rows x cols matrix stored with its columns padded to a multiple of 4
+      // rows, each block starting on a 32-byte boundary (16-byte vector loads in FP32/FP64)
+      auto put = [&](const std::vector<double>& v, int rows, int cols) {
+        const int ld = (rows + 3) & ~3;
         int o = (int)P.mat_pool.size();
-        P.mat_pool.insert(P.mat_pool.end(), v.begin(), v.end());
-        while (P.mat_pool.size() % 2) P.mat_pool.push_back(0.0);  // 16-byte aligned blocks
+        for (int cc = 0; cc < cols; ++cc) {
+          P.mat_pool.insert(P.mat_pool.end(), v.begin() + (size_t)rows * cc, v.begin() + (size_t)rows * (cc + 1));
+          for (int r = rows; r < ld; ++r) P.mat_pool.push_back(0.0);
+        }
+        while (P.mat_pool.size() % 4) P.mat_pool.push_back(0.0);
         return o;
       };
-      off_d0[i][L] = put(b.d0b); off_bgw[i][L] = put(b.bgw); off_d1[i][L] = put(b.d1gg);
-      off_d2[i][L] = put(b.d2gg); off_x[i][L] = put(b.x);
+      off_d0[i][L] = put(b.d0b, b.nq, b.nb); off_bgw[i][L] = put(b.bgw, b.nb, b.nq);
+      off_d1[i][L] = put(b.d1gg, b.nq, b.nq); off_d2[i][L] = put(b.d2gg, b.nq, b.nq);
+      off_x[i][L] = put(b.x, b.nq, 1);
+      offT_in[i][L] = put(transpose(b.bgw, b.nb, b.nq), b.nq, b.nb);   // nq x nb
+      offT_out[i][L] = put(transpose(b.d0b, b.nq, b.nb), b.nb, b.nq);  // nb x nq
+      offT_d1[i][L] = put(transpose(b.d1gg, b.nq, b.nq), b.nq, b.nq);
+      offT_d2[i][L] = put(transpose(b.d2gg, b.nq, b.nq), b.nq, b.nq);
     }
   }
 
@@ -309,6 +331,14 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
     P.max_nq = std::max<int64_t>(P.max_nq, NQ); P.max_nb = std::max<int64_t>(P.max_nb, NB);
   }
   P.sum_nb = onb; P.sum_nq = onq;
+  P.termsT = P.terms;
+  for (int t = 0; t < nterm; ++t) {
+    TermDesc& T = P.termsT[t];
+    for (int i = 0; i < D; ++i) {
+      int L = P.term_l[(size_t)t * D + i];
+      T.m_d0b[i] = offT_in[i][L]; T.m_bgw[i] = offT_out[i][L]; T.m_d1[i] = offT_d1[i][L]; T.m_d2[i] = offT_d2[i][L];
+    }
+  }
 
   // packed basis: SG4 -> all n with sum l(n_i) <= LB, last index fastest
   // (nDindB type 5, ADD_ONE_TO_nDindex_type5p, Source_Lib/sub_nDindex/sub_module_nDindex.f90:2396);

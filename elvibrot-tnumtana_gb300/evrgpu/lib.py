@@ -48,11 +48,13 @@ class Sizes(C.Structure):
 
 class DavidsonOpts(C.Structure):
     _fields_ = [("n_levels", C.c_int), ("block", C.c_int), ("max_dim", C.c_int), ("max_it", C.c_int),
-                ("conv_resi", C.c_double), ("conv_ene", C.c_double), ("prec", C.c_int), ("n_guess", C.c_int)]
+                ("conv_resi", C.c_double), ("conv_ene", C.c_double), ("prec", C.c_int), ("n_guess", C.c_int),
+                ("sym", C.c_int)]
 
 
 EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_tables", "evr_get_basis",
-           "evr_get_vgrid", "evr_hpsi_host", "evr_hpsi_device", "evr_last_launch_count", "evr_last_kernel_ms",
+           "evr_get_vgrid", "evr_hpsi_host", "evr_hpsi_device", "evr_set_operator", "evr_last_launch_count",
+           "evr_last_kernel_ms",
            "evr_davidson",
            "evr_cheby_propagate"]
 
@@ -86,6 +88,7 @@ def load(build: bool = True):
     L.evr_hpsi_device.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.c_int, C.c_int, C.c_int, vp]
     L.evr_last_launch_count.argtypes = [vp, _lp, _lp]
     L.evr_last_kernel_ms.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.evr_set_operator.argtypes = [vp, C.c_int]
     if hasattr(L, "evr_davidson"):
         L.evr_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _dp, _dp, _dp, _lp]
     if hasattr(L, "evr_cheby_propagate"):
@@ -233,7 +236,7 @@ class Problem:
 
     # ---- drivers ------------------------------------------------------------------
     def davidson(self, n_levels, block=None, max_dim=None, max_it=200, conv_resi=1e-7, conv_ene=1e-10,
-                 prec="fp64", guess=None, want_vectors=False):
+                 prec="fp64", guess=None, want_vectors=False, sym=-1):
         L = load()
         o = DavidsonOpts()
         o.n_levels = n_levels
@@ -242,6 +245,7 @@ class Problem:
         o.max_it = max_it
         o.conv_resi, o.conv_ene = conv_resi, conv_ene
         o.prec = PREC[prec]
+        o.sym = sym
         g = None
         if guess is not None:
             g = np.asfortranarray(guess, dtype=np.float64)
@@ -249,9 +253,16 @@ class Problem:
         eig = np.zeros(n_levels)
         vec = np.zeros((self.N, n_levels), order="F") if want_vectors else None
         info = np.zeros(4, dtype=np.int64)
-        self._check(L.evr_davidson(self.h, C.byref(o), _p(g, _dp), _p(eig, _dp), _p(vec, _dp), _p(info, _lp)))
-        return eig, vec, dict(iterations=int(info[0]), hpsi_fp64=int(info[1]), hpsi_fp32=int(info[2]),
-                              converged=bool(info[3]))
+        rc = L.evr_davidson(self.h, C.byref(o), _p(g, _dp), _p(eig, _dp), _p(vec, _dp), _p(info, _lp))
+        stats = dict(iterations=int(info[0]), hpsi_fp64=int(info[1]), hpsi_fp32=int(info[2]),
+                     converged=bool(info[3]))
+        if rc not in (0, EVR_ENOCONV):
+            self._check(rc)
+        return eig, vec, stats
+
+    def set_operator(self, form):
+        """'H' (the reference's OpPsi), 'HT' (its transpose) or 'HSYM' ((H+H^T)/2)."""
+        self._check(load().evr_set_operator(self.h, {"H": 0, "HT": 1, "HSYM": 2}[form]))
 
     def chebyshev(self, psi0, dt, nsteps, emin, emax, poly_tol=1e-10, prec="fp64", want_psi=False):
         """Chebyshev propagation of complex packets psi0 (N x npsi, complex128)."""

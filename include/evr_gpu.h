@@ -126,6 +126,14 @@ int evr_hpsi_host(evr_ctx *ctx, const double *psi, int64_t ld_psi, double *hpsi,
 int evr_hpsi_device(evr_ctx *ctx, const double *psi, int64_t ld_psi, double *hpsi, int64_t ld_hpsi, int nvec,
                     int layout, int prec, void *stream);
 
+/* Operator applied by evr_hpsi_*: EVR_OP_H (default) is the reference's OpPsi;
+ * EVR_OP_HT its transpose; EVR_OP_HSYM (H + H^T)/2.  The grid-derivative matrices
+ * d1b.pinv(d0b) of sub_dnGB_TO_dnGG make H non-symmetric whenever nq > nb. */
+#define EVR_OP_H    0
+#define EVR_OP_HT   1
+#define EVR_OP_HSYM 2
+int evr_set_operator(evr_ctx *ctx, int form);
+
 /* Launch statistics of the last evr_hpsi_* call (kernels launched, work items). */
 int evr_last_launch_count(const evr_ctx *ctx, int64_t *kernels, int64_t *items);
 /* Device time (ms) of the term-pipeline kernel and of the weighted reduction of the last
@@ -154,6 +162,8 @@ typedef struct evr_davidson_opts {
   double conv_ene;       /* eigenvalue change tolerance (au)                         */
   int prec;              /* EVR_PREC_FP64 or EVR_PREC_FP32                           */
   int n_guess;
+  int sym;               /* operator: 0 = H, 1 = (H + H^T)/2, -1 = (H + H^T)/2 when H is
+                            not symmetric by construction (some nq > nb)               */
 } evr_davidson_opts;
 int evr_davidson(evr_ctx *ctx, const evr_davidson_opts *opts, const double *guess, double *eig, double *vec,
                  int64_t *info);
