@@ -137,6 +137,31 @@ def run_reference(args):
     return 0
 
 
+def run_profile(args):
+    """A handful of H.psi launches (FP64 then FP32, 64 vectors) for ncu captures:
+    D=6 Smolyak level 6 (small case) or level 8 (the benchmark workload)."""
+    import torch
+    from evrgpu import Problem, spec as S
+    import evrgpu.lib as E
+
+    spec = S.config_sg4(6, 6, seed=1) if args.profile == "sg4_6d_l6" else S.config_sg4_6d_l8()
+    p = Problem(spec, device=0)
+    x = torch.randn((p.N, NVEC), dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    st = torch.cuda.Stream()
+    torch.cuda.set_stream(st)
+    out = {}
+    for prec in ("fp64", "fp32"):
+        for _ in range(args.steps):
+            p.hpsi_device(x.data_ptr(), NVEC, y.data_ptr(), NVEC, NVEC, layout=E.LAYOUT_INTERLEAVED, prec=prec,
+                          stream=st.cuda_stream)
+        torch.cuda.synchronize()
+        out[prec] = p.last_kernel_ms()[0]
+    print(json.dumps({"profile": args.profile, "N": p.N, "terms": p.nterm, "gflop_per_hpsi": p.flop_per_hpsi / 1e9,
+                      "items_ms": out}))
+    return 0
+
+
 def measure_dgemm_tflops(torch, dtype, n=4096, reps=5):
     a = torch.randn(n, n, dtype=dtype, device="cuda")
     b = torch.randn(n, n, dtype=dtype, device="cuda")
@@ -161,10 +186,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", default=None, choices=["sg4_6d_l6", "sg4_6d_l8"],
+                    help="profiling mode: a few H.psi launches of the named workload, nothing else")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile:
+        return run_profile(args)
 
     import torch
 

@@ -56,7 +56,7 @@ EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_
            "evr_get_vgrid", "evr_hpsi_host", "evr_hpsi_device", "evr_set_operator", "evr_last_launch_count",
            "evr_last_kernel_ms",
            "evr_davidson",
-           "evr_cheby_propagate"]
+           "evr_cheby_propagate", "evr_fma_peak"]
 
 _lib = None
 
@@ -89,6 +89,7 @@ def load(build: bool = True):
     L.evr_last_launch_count.argtypes = [vp, _lp, _lp]
     L.evr_last_kernel_ms.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.evr_set_operator.argtypes = [vp, C.c_int]
+    L.evr_fma_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     if hasattr(L, "evr_davidson"):
         L.evr_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _dp, _dp, _dp, _lp]
     if hasattr(L, "evr_cheby_propagate"):
@@ -96,6 +97,15 @@ def load(build: bool = True):
                                           C.c_double, C.c_int, _dp, _dp, _lp]
     _lib = L
     return L
+
+
+def fma_peak(device: int = 0, prec: str = "fp64") -> float:
+    """Measured FMA issue rate (TFLOP/s) of the CUDA-core pipe for prec."""
+    t = C.c_double()
+    rc = load().evr_fma_peak(device, PREC[prec], C.byref(t))
+    if rc != 0:
+        raise EvrError(rc, "evr_fma_peak failed")
+    return t.value
 
 
 def _iarr(a):
@@ -271,8 +281,7 @@ class Problem:
         if psi0.ndim == 1:
             psi0 = psi0[:, None]
         N, npsi = psi0.shape
-        buf = np.asfortranarray(psi0).view(np.float64)  # (2N x npsi): re/im interleaved per element
-        buf = np.ascontiguousarray(np.asfortranarray(psi0).T).view(np.float64)  # npsi rows of 2N
+        buf = np.ascontiguousarray(psi0.T).view(np.float64)  # packet p: 2N doubles (re, im per element)
         ac = np.zeros((nsteps + 1) * npsi * 2)
         out = np.zeros(npsi * 2 * N) if want_psi else None
         info = np.zeros(3, dtype=np.int64)

@@ -181,6 +181,11 @@ int evr_cheby_propagate(evr_ctx *ctx, const double *psi0, int npsi, double dt, i
                         double emax, double poly_tol, int prec, double *autocorr, double *psi_out,
                         int64_t *info);
 
+/* FMA issue-rate micro-benchmark of the device (independent FMA chains, no memory
+ * traffic): the peak of the CUDA-core pipe the contractions run on, in TFLOP/s.
+ * Utility for roofline reporting; no counterpart in the reference. */
+int evr_fma_peak(int device, int prec, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif
