@@ -106,9 +106,34 @@ int evr_get_vgrid(const evr_ctx* c0, double* v) {
   if (!c || !v) return EVR_EINVAL;
   if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
   EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
-  const size_t n = (size_t)c->hp.sum_nq * c->hp.nb0 * c->hp.nb0;
-  EVR_CU(cudaMemcpyAsync(v, c->dp.vgrid, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "copy vgrid");
+  const HostProblem& P = c->hp;
+  const int nb2 = P.nb0 * P.nb0;
+  const size_t n = (size_t)P.sum_nq * nb2;
+  std::vector<double> dev(n);
+  EVR_CU(cudaMemcpyAsync(dev.data(), c->dp.vgrid, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+         "copy vgrid");
   EVR_CU(cudaStreamSynchronize(c->stream), "sync");
+  // device grid points follow each term's permuted mode order: back to the reference order
+  for (const TermDesc& T : P.terms)
+    for (int ab = 0; ab < nb2; ++ab)
+      for (int64_t qp = 0; qp < T.NQ; ++qp) {
+        const int64_t q = P.grid_perm[(size_t)T.off_nq + qp] - T.off_nq;
+        v[(size_t)T.off_nq * nb2 + (size_t)ab * T.NQ + q] = dev[(size_t)T.off_nq * nb2 + (size_t)ab * T.NQ + qp];
+      }
+  return EVR_OK;
+}
+
+int evr_set_kernel_path(evr_ctx* c, int slab) {
+  if (!c) return EVR_EINVAL;
+  if (slab != 0 && slab != 1) return set_error(c, EVR_EINVAL, "evr_set_kernel_path: 0 or 1");
+  if (c->use_slab != (slab == 1)) {
+    c->use_slab = slab == 1;
+    if (!c->host_only) {
+      cudaSetDevice(c->device);
+      cudaStreamSynchronize(c->stream);
+      free_workspace(c);  // work decompositions depend on the path
+    }
+  }
   return EVR_OK;
 }
 

@@ -13,7 +13,7 @@
 namespace evr {
 
 constexpr int kMaxD = 16;      // modes
-constexpr int kMaxN1 = 32;     // largest 1-D nq (and nb)
+constexpr int kMaxN1 = 24;     // largest 1-D nq (and nb)
 constexpr int kMaxNb0 = 4;     // electronic states
 
 // ---------------------------------------------------------------------------
@@ -28,17 +28,26 @@ struct Basis1D {
 };
 
 // Per-term description used by the device kernels.  Offsets are in elements.
+// The modes of a term are stored in a permuted order (perm[p] = reference mode of
+// position p) that puts the mode with the most grid points last: the slab kernel walks
+// the term grid one slab (fixed last-mode point) at a time.  Term-local basis and grid
+// indices on the device (map, CSR, V and G grids) follow the permuted order, first
+// position fastest.
 struct TermDesc {
   int64_t off_nb;        // offset of the term in the term-basis space (sum_nb order)
   int64_t off_nq;        // offset of the term grid
   int32_t NB, NQ;        // prod nb_i, prod nq_i
   int32_t nb[kMaxD];
   int32_t nq[kMaxD];
+  int32_t perm[kMaxD];
   int32_t m_d0b[kMaxD];  // offsets of the 1-D matrices in the flat matrix pool
   int32_t m_bgw[kMaxD];
   int32_t m_d1[kMaxD];
   int32_t m_d2[kMaxD];
   int32_t m_x[kMaxD];
+  // last-position (slab) mode: d1.d0b, d2.d0b (grid <- basis) and bgw.d1, bgw.d2
+  // (basis <- grid), padded like the others
+  int32_t m_x1L, m_x2L, m_e1L, m_e2L;
   double weight;
 };
 
@@ -61,7 +70,9 @@ struct HostProblem {
   std::vector<TermDesc> termsT;           // same terms, matrix offsets of the transposed operator
   int64_t Np = 0, sum_nb = 0, sum_nq = 0, max_nq = 0, max_nb = 0;
   std::vector<int> packed;                // Np x D
-  std::vector<int> map;                   // sum_nb (packed index or -1)
+  std::vector<int> map;                   // sum_nb (packed index or -1), reference term-local order
+  std::vector<int> map_perm;              // same, term-local order of the permuted modes (device)
+  std::vector<int64_t> grid_perm;         // device grid point -> reference grid point (sum_nq)
   std::vector<double> mat_pool;           // all 1-D matrices
   // CSR of the transposed map over N = Np*nb0 rows: sources in the term-basis
   // output buffer (off_nb*nb0 + a*NB + iB) and their Smolyak weight
@@ -94,6 +105,8 @@ struct DeviceProblem {
   double* csr_w = nullptr;
   double* G0 = nullptr;
   double* g = nullptr;
+  float* G032 = nullptr;
+  float* g32 = nullptr;
   double* mono_coef = nullptr;
   int* mono_idx = nullptr;
   int* mono_elec = nullptr;
@@ -103,8 +116,10 @@ struct DeviceProblem {
 // Work decomposition of one (nvec, precision) pair.
 struct ItemSet {
   int nvec = 0, prec = 0;
-  WorkItem* items = nullptr;
+  WorkItem* items = nullptr;       // general kernel
   int n_items = 0;
+  WorkItem* items_slab = nullptr;  // slab kernel
+  int n_slab = 0;
 };
 
 struct Workspace {
@@ -117,7 +132,9 @@ struct Workspace {
   void* ht2 = nullptr;              // second output for the symmetrised operator
   double* xin = nullptr;            // interleaved copies (layout conversions)
   double* xout = nullptr;
-  int grid = 0, smem_bytes = 0;
+  int grid = 0, smem_bytes = 0;             // general kernel
+  int grid_slab = 0, smem_slab_bytes = 0;   // slab kernel
+  size_t slab_slab_bytes = 0;               // slab kernel's global tensor per CTA
 };
 
 // operator forms
@@ -130,6 +147,7 @@ struct evr_ctx {
   bool host_only = false;           // created with device < 0: tables only
   int op_form = 0;                  // EVR_OP_H, EVR_OP_HT or EVR_OP_HSYM
   bool capturing = false;           // inside a stream capture: no event records
+  bool use_slab = true;             // slab kernel for the terms that fit (EVR_NO_SLAB=1 disables)
   cudaStream_t stream = nullptr;
   evr::HostProblem hp;
   evr::DeviceProblem dp;

@@ -50,7 +50,11 @@ struct ItemParams {
   int D, nb0, keo_type;
   int has_offdiag;         // type 1 with off-diagonal F2 terms
   int vtrans;              // 1: V_ab read as V_ba (transposed operator)
+  const T* gT;             // g in T precision (on-the-fly G(Q) in the slab kernel), or nullptr
+  const T* G0T;            // G0 in T precision
 };
+
+constexpr int kSlabThreads = 512;
 
 // out(a, m, b, v) = alpha * sum_k mat[m + M*k] * in(a, k, b, v)  (+ out if acc)
 // element (a, k, b, v) of a tensor with vector stride ld lives at ((a + A*(k + K*b))*ld + v).
@@ -122,8 +126,7 @@ __device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64
                                          int Vt, const T* mat, T alpha, bool acc) {
   if (M <= 8) contract_m<T, 8>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
   else if (M <= 16) contract_m<T, 16>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
-  else if (M <= 24) contract_m<T, 24>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
-  else contract_m<T, 32>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  else contract_m<T, 24>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
 }
 
 // First B->G mode fused with the gather from the packed vector block:
@@ -163,12 +166,11 @@ __device__ __forceinline__ void gather_contract(const double* x, int64_t ldx, co
                                                 int K, int M, int B, int Vt, const T* mat) {
   if (M <= 8) gather_contract_m<T, 8>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
   else if (M <= 16) gather_contract_m<T, 16>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
-  else if (M <= 24) gather_contract_m<T, 24>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
-  else gather_contract_m<T, 32>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+  else gather_contract_m<T, 24>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) hpsi_items_kernel(ItemParams<T> p) {
+__global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   __shared__ TermDesc s_term;
@@ -272,7 +274,7 @@ __global__ void __launch_bounds__(kThreads) hpsi_items_kernel(ItemParams<T> p) {
 #pragma unroll
               for (int j = 0; j < kMaxD; ++j) {
                 if (j >= D) break;
-                z[i] = fma((T)__ldg(p.G0 + i + D * j), y[j], z[i]);
+                z[i] = fma((T)__ldg(p.G0 + Tm.perm[i] + D * Tm.perm[j]), y[j], z[i]);
               }
             }
           }
@@ -297,7 +299,7 @@ __global__ void __launch_bounds__(kThreads) hpsi_items_kernel(ItemParams<T> p) {
         int A = 1, Bq = NQ;
         for (int i = 0; i < D; ++i) {
           Bq /= Tm.nq[i];
-          const T f = (T)(-0.5 * __ldg(p.G0 + i + D * i));
+          const T f = (T)(-0.5 * __ldg(p.G0 + Tm.perm[i] + D * Tm.perm[i]));
           if (f != T(0))
             contract<T>(P0, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, p.mats + Tm.m_d2[i], f, true);
           __syncthreads();
@@ -310,7 +312,7 @@ __global__ void __launch_bounds__(kThreads) hpsi_items_kernel(ItemParams<T> p) {
             int Aj = Ai * Tm.nq[i];
             for (int j = i + 1; j < D; ++j) {
               const int Bj = NQ / (Aj * Tm.nq[j]);
-              const T f = (T)(-__ldg(p.G0 + i + D * j));
+              const T f = (T)(-__ldg(p.G0 + Tm.perm[i] + D * Tm.perm[j]));
               if (f != T(0)) {
                 contract<T>(P0, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, p.mats + Tm.m_d1[i], T(1), false);
                 __syncthreads();
@@ -339,6 +341,301 @@ __global__ void __launch_bounds__(kThreads) hpsi_items_kernel(ItemParams<T> p) {
         } else {
           T* nxt = (cur == A0) ? A1 : A0;
           contract<T>(cur, Vt, nxt, Vt, A, Tm.nq[i], Tm.nb[i], Bq, Vt, p.mats + Tm.m_bgw[i], T(1), false);
+          cur = nxt;
+        }
+        __syncthreads();
+        A *= Tm.nb[i];
+      }
+    }
+  }
+}
+
+// P[a] = sum_{k < nL} X[ldx*k] * Tg[a + ss*k]  for a < ss  (one grid slab of the streamed
+// position: row q of its grid<-basis matrix applied to the partially transformed tensor)
+template <typename T>
+__device__ __forceinline__ void slab_extract(const T* __restrict__ Tg, int64_t ss, int nL, const T* __restrict__ X,
+                                             int ldx, T* __restrict__ P) {
+  for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) {
+    T s = T(0);
+    for (int k0 = 0; k0 < nL; k0 += 8) {
+      T t[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) t[j] = (k0 + j < nL) ? Tg[a + ss * (k0 + j)] : T(0);
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (k0 + j < nL) s = fma(__ldg(X + ldx * (k0 + j)), t[j], s);
+    }
+    P[a] = s;
+  }
+}
+
+// W[a + ss*k] += c1*O[k]*A1[a] + c2*E[k]*A2[a]  for k < nL (A2 may be null): the slab's
+// image under G->B of the streamed position
+template <typename T>
+__device__ __forceinline__ void slab_accumulate(T* __restrict__ W, int64_t ss, int nL, const T* __restrict__ O,
+                                                const T* __restrict__ A1, T c1, const T* __restrict__ E,
+                                                const T* __restrict__ A2, T c2) {
+  for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) {
+    const T u = c1 * A1[a];
+    const T z = A2 ? c2 * A2[a] : T(0);
+    for (int k = 0; k < nL; ++k) {
+      T wv = W[a + ss * k];
+      wv = fma(__ldg(O + k), u, wv);
+      if (A2) wv = fma(__ldg(E + k), z, wv);
+      W[a + ss * k] = wv;
+    }
+  }
+}
+
+// Phi_i = sum_j G_ij(Q) y_j on one slab, in place: y_j = Y[j] (j < L) and P (j = L).
+// G(Q) = G0 + sum_k g_ijk Q_k is formed on the fly (gT), read from the grid table
+// (ggrid) or constant (G0); symmetric pairs are visited once.
+template <typename T, int DM>
+__device__ __forceinline__ void slab_pointwise_G(const ItemParams<T>& p, const TermDesc& Tm, T* Y, T* P, int64_t ss,
+                                                 int Vt, int q, int NQs, int nG) {
+  const int D = p.D, L = D - 1;
+  for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) {
+    const int pt = (int)(a / Vt);
+    T y[DM], z[DM], Qp[DM];
+#pragma unroll
+    for (int j = 0; j < DM; ++j) {
+      y[j] = (j < L) ? Y[j * ss + a] : ((j == L) ? P[a] : T(0));
+      z[j] = T(0);
+    }
+    if (sizeof(T) == 4 && p.gT) {  // coordinates of the point, by position
+      int r = pt;
+#pragma unroll
+      for (int d = 0; d < DM; ++d) {
+        if (d < L) {
+          Qp[d] = __ldg(p.mats + Tm.m_x[d] + r % Tm.nq[d]);
+          r /= Tm.nq[d];
+        } else if (d == L) {
+          Qp[d] = __ldg(p.mats + Tm.m_x[d] + q);
+        } else {
+          Qp[d] = T(0);
+        }
+      }
+    }
+    const T* Gp = p.ggrid ? p.ggrid + Tm.off_nq * nG + (int64_t)q * NQs + pt : nullptr;
+    int c = 0;
+#pragma unroll
+    for (int i = 0; i < DM; ++i) {
+      if (i >= D) break;
+#pragma unroll
+      for (int j = i; j < DM; ++j) {
+        if (j >= D) break;
+        const int oi = Tm.perm[i], oj = Tm.perm[j];
+        T gij = T(0);
+        bool done = false;
+        if constexpr (sizeof(T) == 4) {  // FP32 forms G on the fly; FP64 reads the grid table
+          if (p.gT) {
+            gij = __ldg(p.G0T + oi + D * oj);
+            const T* gp = p.gT + oi + D * oj;
+#pragma unroll
+            for (int k = 0; k < DM; ++k)
+              if (k < D) gij = fma(__ldg(gp + D * D * Tm.perm[k]), Qp[k], gij);
+            done = true;
+          }
+        }
+        if (done) {
+        } else if (Gp) {
+          gij = __ldg(Gp + (int64_t)c * Tm.NQ);
+        } else {
+          gij = (T)__ldg(p.G0 + oi + D * oj);
+        }
+        ++c;
+        z[i] = fma(gij, y[j], z[i]);
+        if (j != i) z[j] = fma(gij, y[i], z[j]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < DM; ++i) {
+      if (i < L) Y[i * ss + a] = z[i];
+      else if (i == L) P[a] = z[i];
+    }
+  }
+}
+
+// Slab-streaming pipeline for one (term, vector tile) item, one electronic state.  Positions
+// 0..L-1 of the term's mode order are transformed whole, position L = D-1 is streamed:
+//   A: gather + B->G over positions 0..L-1 (shared-memory ping-pong) -> Tg (global, L2)
+//   B: for each grid point q of position L: extract the grid slab P = d0b_L[q,:].Tg, apply V,
+//      the derivatives along positions < L and the G(Q) combination on the slab in shared
+//      memory (d_L psi comes from (d1.d0b)_L[q,:].Tg), and accumulate the slab's image under
+//      G->B of position L into W (shared memory):
+//      W[:,k] += bgw_L[k,q] Acc - 1/2 (bgw.d1)_L[k,q] Phi_L        (type 10)
+//      W[:,k] += bgw_L[k,q] Acc + F2_LL (bgw.d2)_L[k,q] P           (type 1)
+//   C: G->B over positions 0..L-1 of W (shared-memory ping-pong), the last one into the
+//      term-basis output.
+// The algebra is that of sub_TabOpPsi_OF_ONEDP_FOR_SGtype4 (sub_OpPsi_SG4.f90:1490-1650)
+// with the last mode's B->G, derivative and G->B matrices multiplied together.
+template <typename T>
+__global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T> p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  __shared__ TermDesc s_term;
+  const int D = p.D, L = D - 1;
+  while (true) {
+    if (threadIdx.x == 0) s_item = atomicAdd(p.counter, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= p.n_items) break;
+    const WorkItem w = p.items[it];
+    {
+      const int* src = reinterpret_cast<const int*>(p.terms + w.term);
+      int* dst = reinterpret_cast<int*>(&s_term);
+      for (int i = threadIdx.x; i < (int)(sizeof(TermDesc) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const TermDesc& Tm = s_term;
+    const int Vt = w.vt;
+    const int gL = Tm.nq[L], nL = Tm.nb[L];
+    const int NQs = Tm.NQ / gL;
+    const int64_t ss = (int64_t)NQs * Vt;  // one slab array
+    const int64_t tsz = ss * nL;           // T and W
+    T* sm = reinterpret_cast<T*>(smem_raw);
+    T* Tg = p.slab + (int64_t)blockIdx.x * p.slab_per_cta;
+
+    // ---- A: gather + B->G over positions 0..L-1
+    if (L == 0) {
+      for (int64_t i = threadIdx.x; i < (int64_t)nL * Vt; i += blockDim.x) {
+        const int v = (int)(i % Vt), k = (int)(i / Vt);
+        const int pk = __ldg(p.map + Tm.off_nb + k);
+        Tg[i] = pk >= 0 ? (T)__ldg(p.x + (int64_t)pk * p.ldx + w.v0 + v) : T(0);
+      }
+    } else {
+      T* b0 = sm;
+      T* b1 = sm + tsz;
+      int nb_rest = Tm.NB / Tm.nb[0];
+      T* cur = (L == 1) ? Tg : b0;
+      gather_contract<T>(p.x + w.v0, p.ldx, p.map + Tm.off_nb, 0, cur, Tm.nb[0], Tm.nq[0], nb_rest, Vt,
+                         p.mats + Tm.m_d0b[0]);
+      __syncthreads();
+      int A = Tm.nq[0];
+      for (int i = 1; i < L; ++i) {
+        nb_rest /= Tm.nb[i];
+        T* nxt = (i == L - 1) ? Tg : (cur == b0 ? b1 : b0);
+        contract<T>(cur, Vt, nxt, Vt, A, Tm.nb[i], Tm.nq[i], nb_rest, Vt, p.mats + Tm.m_d0b[i], T(1), false);
+        __syncthreads();
+        cur = nxt;
+        A *= Tm.nq[i];
+      }
+    }
+    __syncthreads();
+
+    // ---- B: stream the grid slabs of position L
+    T* W = sm;
+    T* Acc = sm + tsz;
+    T* P = Acc + ss;
+    T* Y = P + ss;
+    for (int64_t i = threadIdx.x; i < tsz; i += blockDim.x) W[i] = T(0);
+    const int ldx0 = (gL + 3) & ~3, ldo = (nL + 3) & ~3;
+    const T* X0 = p.mats + Tm.m_d0b[L];
+    const T* OUT = p.mats + Tm.m_bgw[L];
+    const int nG = D * (D + 1) / 2;
+    for (int q = 0; q < gL; ++q) {
+      __syncthreads();
+      slab_extract<T>(Tg, ss, nL, X0 + q, ldx0, P);
+      __syncthreads();
+      const T* Vq = p.vgrid + Tm.off_nq + (int64_t)q * NQs;
+      for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) Acc[a] = __ldg(Vq + a / Vt) * P[a];
+      if (p.keo_type == 10) {
+        int A = 1, Bq = NQs;
+        for (int j = 0; j < L; ++j) {  // Y[j] = d1_j P
+          Bq /= Tm.nq[j];
+          contract<T>(P, Vt, Y + j * ss, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, p.mats + Tm.m_d1[j], T(1), false);
+          A *= Tm.nq[j];
+        }
+        __syncthreads();
+        slab_extract<T>(Tg, ss, nL, p.mats + Tm.m_x1L + q, ldx0, P);  // P <- d_L psi on the slab
+        __syncthreads();
+        // Phi_i = sum_j G_ij(Q) y_j, in place (Y[i] for i < L, P for i = L)
+        if (D <= 4) slab_pointwise_G<T, 4>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
+        else if (D <= 8) slab_pointwise_G<T, 8>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
+        else if (D <= 12) slab_pointwise_G<T, 12>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
+        else slab_pointwise_G<T, 16>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
+        __syncthreads();
+        A = 1;
+        Bq = NQs;
+        for (int i = 0; i < L; ++i) {  // Acc += -1/2 d1_i Phi_i
+          Bq /= Tm.nq[i];
+          contract<T>(Y + i * ss, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, p.mats + Tm.m_d1[i], T(-0.5), true);
+          __syncthreads();
+          A *= Tm.nq[i];
+        }
+        slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), p.mats + Tm.m_e1L + (int64_t)ldo * q, P,
+                           T(-0.5));
+      } else {
+        __syncthreads();
+        int A = 1, Bq = NQs;
+        for (int i = 0; i < L; ++i) {  // Acc += F2_ii d2_i P
+          Bq /= Tm.nq[i];
+          const T f = (T)(-0.5 * __ldg(p.G0 + Tm.perm[i] + D * Tm.perm[i]));
+          if (f != T(0))
+            contract<T>(P, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, p.mats + Tm.m_d2[i], f, true);
+          __syncthreads();
+          A *= Tm.nq[i];
+        }
+        if (p.has_offdiag) {
+          int Ai = 1;
+          for (int i = 0; i < L; ++i) {
+            const int Bi = NQs / (Ai * Tm.nq[i]);
+            int Aj = Ai * Tm.nq[i];
+            for (int j = i + 1; j < L; ++j) {
+              const int Bj = NQs / (Aj * Tm.nq[j]);
+              const T f = (T)(-__ldg(p.G0 + Tm.perm[i] + D * Tm.perm[j]));
+              if (f != T(0)) {
+                contract<T>(P, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, p.mats + Tm.m_d1[i], T(1), false);
+                __syncthreads();
+                contract<T>(Y, Vt, Acc, Vt, Aj, Tm.nq[j], Tm.nq[j], Bj, Vt, p.mats + Tm.m_d1[j], f, true);
+                __syncthreads();
+              }
+              Aj *= Tm.nq[j];
+            }
+            Ai *= Tm.nq[i];
+          }
+        }
+        const T fLL = (T)(-0.5 * __ldg(p.G0 + Tm.perm[L] + D * Tm.perm[L]));
+        slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), p.mats + Tm.m_e2L + (int64_t)ldo * q, P,
+                           fLL);
+        if (p.has_offdiag) {  // F2_iL d1_i d_L: d_L through (bgw.d1)_L on the way back
+          int Ai = 1;
+          for (int i = 0; i < L; ++i) {
+            const int Bi = NQs / (Ai * Tm.nq[i]);
+            const T f = (T)(-__ldg(p.G0 + Tm.perm[i] + D * Tm.perm[L]));
+            if (f != T(0)) {
+              __syncthreads();
+              contract<T>(P, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, p.mats + Tm.m_d1[i], T(1), false);
+              __syncthreads();
+              slab_accumulate<T>(W, ss, nL, p.mats + Tm.m_e1L + (int64_t)ldo * q, Y, f, nullptr, nullptr, T(0));
+            }
+            Ai *= Tm.nq[i];
+          }
+        }
+      }
+    }
+    __syncthreads();
+
+    // ---- C: G->B over positions 0..L-1 of W, the last one into the term-basis output
+    T* dst = p.ht + Tm.off_nb * p.ldh + w.v0;
+    if (L == 0) {
+      for (int64_t i = threadIdx.x; i < (int64_t)nL * Vt; i += blockDim.x) {
+        const int v = (int)(i % Vt), k = (int)(i / Vt);
+        dst[(int64_t)k * p.ldh + v] = W[i];
+      }
+    } else {
+      T* b0 = W;
+      T* b1 = sm + tsz;
+      T* cur = b0;
+      int A = 1, Bq = NQs;
+      for (int i = 0; i < L; ++i) {
+        Bq /= Tm.nq[i];
+        const int Bt = Bq * nL;
+        if (i == L - 1) {
+          contract<T>(cur, Vt, dst, p.ldh, A, Tm.nq[i], Tm.nb[i], Bt, Vt, p.mats + Tm.m_bgw[i], T(1), false);
+        } else {
+          T* nxt = (cur == b0) ? b1 : b0;
+          contract<T>(cur, Vt, nxt, Vt, A, Tm.nq[i], Tm.nb[i], Bt, Vt, p.mats + Tm.m_bgw[i], T(1), false);
           cur = nxt;
         }
         __syncthreads();
@@ -388,10 +685,10 @@ __global__ void grid_eval_kernel(const TermDesc* __restrict__ terms, int n_terms
     const TermDesc& T = terms[lo];
     int64_t q = gq - T.off_nq;
     const int NQ = T.NQ;
-    double Q[kMaxD];
+    double Q[kMaxD];  // coordinates in the reference's mode order
     int64_t r = q;
     for (int d = 0; d < D; ++d) {
-      Q[d] = mats[T.m_x[d] + (int)(r % T.nq[d])];
+      Q[T.perm[d]] = mats[T.m_x[d] + (int)(r % T.nq[d])];
       r /= T.nq[d];
     }
     double* V = vgrid + T.off_nq * nb0 * nb0;
@@ -408,10 +705,11 @@ __global__ void grid_eval_kernel(const TermDesc* __restrict__ terms, int n_terms
       const int nG = D * (D + 1) / 2;
       double* Gp = ggrid + T.off_nq * nG + q;
       int c = 0;
-      for (int i = 0; i < D; ++i)
+      for (int i = 0; i < D; ++i)  // (i, j) positions of the term's mode order
         for (int j = i; j < D; ++j) {
-          double s = G0[i + D * j];
-          for (int k = 0; k < D; ++k) s += g[i + D * (j + D * k)] * Q[k];
+          const int oi = T.perm[i], oj = T.perm[j];
+          double s = G0[oi + D * oj];
+          for (int k = 0; k < D; ++k) s += g[oi + D * (oj + D * k)] * Q[k];
           Gp[(int64_t)c * NQ] = s;
           ++c;
         }
@@ -490,7 +788,7 @@ int upload_problem(evr_ctx* c) {
   if ((rc = upload(c, &d.terms, P.terms))) return rc;
   if ((rc = upload(c, &d.termsT, P.termsT))) return rc;
   if ((rc = upload(c, &d.mats, P.mat_pool))) return rc;
-  if ((rc = upload(c, &d.map, P.map))) return rc;
+  if ((rc = upload(c, &d.map, P.map_perm))) return rc;
   if ((rc = upload(c, &d.csr_ptr, P.csr_ptr))) return rc;
   if ((rc = upload(c, &d.csr_src, P.csr_src))) return rc;
   if ((rc = upload(c, &d.csr_w, P.csr_w))) return rc;
@@ -524,6 +822,10 @@ int upload_problem(evr_ctx* c) {
     EVR_CU(cudaMalloc((void**)&c->dp_ggrid32, ng * sizeof(float)), "cudaMalloc ggrid32");
     to_float_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(gg, c->dp_ggrid32, ng);
   }
+  EVR_CU(cudaMalloc((void**)&d.G032, sizeof(float) * D * D), "cudaMalloc G032");
+  EVR_CU(cudaMalloc((void**)&d.g32, sizeof(float) * D * D * D), "cudaMalloc g32");
+  to_float_kernel<<<1, 256, 0, c->stream>>>(d.G0, d.G032, (int64_t)D * D);
+  to_float_kernel<<<4, 256, 0, c->stream>>>(d.g, d.g32, (int64_t)D * D * D);
   EVR_CU(cudaGetLastError(), "to_float_kernel");
   EVR_CU(cudaStreamSynchronize(c->stream), "grid set-up");
   return EVR_OK;
@@ -532,7 +834,8 @@ int upload_problem(evr_ctx* c) {
 void free_problem(evr_ctx* c) {
   DeviceProblem& d = c->dp;
   void* ptrs[] = {d.terms, d.termsT, d.mats, d.mats32, d.vgrid, d.vgrid32, d.map, d.csr_ptr, d.csr_src, d.csr_w,
-                  d.G0, d.g, d.mono_coef, d.mono_idx, d.mono_elec, d.e0diag, c->dp_ggrid, c->dp_ggrid32};
+                  d.G0, d.g, d.G032, d.g32, d.mono_coef, d.mono_idx, d.mono_elec, d.e0diag, c->dp_ggrid,
+                  c->dp_ggrid32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   d = DeviceProblem();
@@ -542,48 +845,55 @@ void free_problem(evr_ctx* c) {
 
 void free_workspace(evr_ctx* c) {
   Workspace& w = c->ws;
-  for (ItemSet& s : w.sets)
+  for (ItemSet& s : w.sets) {
     if (s.items) cudaFree(s.items);
+    if (s.items_slab) cudaFree(s.items_slab);
+  }
   void* ptrs[] = {w.counter, w.slab, w.ht, w.ht2, w.xin, w.xout};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   w = Workspace();
 }
 
-static int smem_budget_bytes(evr_ctx* c) {
-  int optin = 0;
-  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device) != cudaSuccess) return 0;
-  const int ctas_per_sm = 2;
-  return std::min(optin, (int)(228 * 1024 / ctas_per_sm) - 2048);
+// elements of shared memory the slab kernel needs for a term and a vector tile
+static size_t slab_need_elems(const HostProblem& P, const TermDesc& Tm, int vt) {
+  const int L = P.D - 1;
+  const size_t ss = (size_t)(Tm.NQ / Tm.nq[L]) * vt, tsz = ss * Tm.nb[L];
+  const size_t ny = (P.keo_type == 10) ? (size_t)L : 1;
+  return std::max(2 * tsz, tsz + (2 + ny) * ss);
 }
 
-// Work decomposition for a block of nvec vectors: per term the widest vector tile whose
-// buffers fit the shared-memory budget; terms that do not fit even with one vector run
-// from the CTA's global slab.  Items are ordered by decreasing cost.  Buffers are sized
-// once for kMaxBlock vectors in FP64 and shared by every decomposition.
+// Work decomposition for a block of nvec vectors.  Terms whose slab pipeline fits the
+// shared memory of one CTA (one electronic state) go to the slab kernel, with the widest
+// vector tile that fits; the others go to the general kernel, in shared memory when
+// their buffers fit, else in the CTA's global slab.  Items are ordered by decreasing
+// cost.  Buffers are sized once for kMaxBlock vectors in FP64.
 int ensure_workspace(evr_ctx* c, int nvec, int prec) {
   Workspace& w = c->ws;
   if (nvec < 1 || nvec > kMaxBlock) return set_error(c, EVR_EINVAL, "block of more than 64 vectors");
   const HostProblem& P = c->hp;
   int rc = EVR_OK;
   if (!w.counter) {
-    const int smem = smem_budget_bytes(c);
-    if (smem <= 0) return set_error(c, EVR_EDEVICE, "shared-memory attribute");
-    w.smem_bytes = smem;
+    int optin = 0;
+    EVR_CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attr");
+    w.smem_bytes = std::min(optin, 228 * 1024 / 2) - 2048;   // general kernel: 2 CTAs per SM
+    w.smem_slab_bytes = optin - 2048;                         // slab kernel: 1 CTA per SM
     w.grid = c->num_sms * 2;
+    w.grid_slab = c->num_sms;
     size_t slab = 0;
     for (const TermDesc& Tm : P.terms) {
       size_t fp1 = footprint_elems<double>(P, Tm, 1) * sizeof(double);
-      if (fp1 > (size_t)smem) slab = std::max(slab, fp1);
+      if (fp1 > (size_t)w.smem_bytes) slab = std::max(slab, fp1);
     }
-    // FP32 items use the same slab (half the bytes per element)
     w.slab_per_cta_bytes = slab;
-    w.counter = (int*)dev_alloc<int>(1, rc);
+    // the slab kernel keeps its partially transformed tensor (at most half of its shared
+    // memory) in global memory
+    w.slab_slab_bytes = (size_t)(w.smem_slab_bytes / 2 + 256) & ~(size_t)255;
+    const size_t total = std::max(slab * w.grid, w.slab_slab_bytes * w.grid_slab);
+    w.counter = (int*)dev_alloc<int>(2, rc);
     if (rc) return set_error(c, rc, "workspace allocation (counter)");
-    if (slab) {
-      w.slab = dev_alloc<unsigned char>(slab * w.grid, rc);
-      if (rc) return set_error(c, rc, "workspace allocation (slab)");
-    }
+    w.slab = dev_alloc<unsigned char>(total, rc);
+    if (rc) return set_error(c, rc, "workspace allocation (slab)");
     w.cap = kMaxBlock;
     w.ht = dev_alloc<double>((size_t)P.sum_nb * P.nb0 * w.cap, rc);
     if (rc) return set_error(c, rc, "workspace allocation (term-basis output)");
@@ -592,16 +902,30 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
     if (rc) return set_error(c, rc, "workspace allocation (xin)");
     w.xout = (double*)dev_alloc<double>(xe, rc);
     if (rc) return set_error(c, rc, "workspace allocation (xout)");
-    EVR_CU(cudaFuncSetAttribute(hpsi_items_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "attr");
-    EVR_CU(cudaFuncSetAttribute(hpsi_items_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem), "attr");
+    EVR_CU(cudaFuncSetAttribute(hpsi_items_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                w.smem_bytes), "attr");
+    EVR_CU(cudaFuncSetAttribute(hpsi_items_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                w.smem_bytes), "attr");
+    EVR_CU(cudaFuncSetAttribute(hpsi_slab_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                w.smem_slab_bytes), "attr");
+    EVR_CU(cudaFuncSetAttribute(hpsi_slab_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                w.smem_slab_bytes), "attr");
   }
   for (const ItemSet& s : w.sets)
     if (s.nvec == nvec && s.prec == prec) return EVR_OK;
   const size_t esz = prec == EVR_PREC_FP32 ? sizeof(float) : sizeof(double);
-  std::vector<WorkItem> items;
+  const bool slab_ok = P.nb0 == 1 && c->use_slab;
+  std::vector<WorkItem> items, sitems;
   for (int t = 0; t < (int)P.terms.size(); ++t) {
     const TermDesc& Tm = P.terms[t];
     if (Tm.weight == 0.0) continue;
+    if (slab_ok && slab_need_elems(P, Tm, 1) * esz <= (size_t)w.smem_slab_bytes) {
+      int vt = 1;
+      while (vt * 2 <= nvec && vt * 2 <= 32 && slab_need_elems(P, Tm, vt * 2) * esz <= (size_t)w.smem_slab_bytes)
+        vt *= 2;
+      for (int v0 = 0; v0 < nvec; v0 += vt) sitems.push_back(WorkItem{t, v0, std::min(vt, nvec - v0), 1});
+      continue;
+    }
     int vt = 1;
     const size_t fp1 = footprint_elems<double>(P, Tm, 1) * esz;
     const bool in_smem = fp1 <= (size_t)w.smem_bytes;
@@ -609,16 +933,25 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
       while (vt * 2 <= nvec && vt * 2 <= 32 && fp1 * (size_t)(vt * 2) <= (size_t)w.smem_bytes) vt *= 2;
     for (int v0 = 0; v0 < nvec; v0 += vt) items.push_back(WorkItem{t, v0, std::min(vt, nvec - v0), in_smem ? 1 : 0});
   }
-  std::stable_sort(items.begin(), items.end(), [&](const WorkItem& a, const WorkItem& b) {
+  auto by_cost = [&](const WorkItem& a, const WorkItem& b) {
     return (int64_t)P.terms[a.term].NQ * a.vt > (int64_t)P.terms[b.term].NQ * b.vt;
-  });
+  };
+  std::stable_sort(items.begin(), items.end(), by_cost);
+  std::stable_sort(sitems.begin(), sitems.end(), by_cost);
   ItemSet s;
   s.nvec = nvec;
   s.prec = prec;
   s.n_items = (int)items.size();
+  s.n_slab = (int)sitems.size();
   s.items = (WorkItem*)dev_alloc<WorkItem>(items.size(), rc);
   if (rc) return set_error(c, rc, "workspace allocation (items)");
-  EVR_CU(cudaMemcpy(s.items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice), "items");
+  s.items_slab = (WorkItem*)dev_alloc<WorkItem>(sitems.size(), rc);
+  if (rc) return set_error(c, rc, "workspace allocation (items)");
+  if (!items.empty())
+    EVR_CU(cudaMemcpy(s.items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice), "items");
+  if (!sitems.empty())
+    EVR_CU(cudaMemcpy(s.items_slab, sitems.data(), sitems.size() * sizeof(WorkItem), cudaMemcpyHostToDevice),
+           "items");
   w.sets.push_back(s);
   return EVR_OK;
 }
@@ -636,11 +969,8 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
   p.ggrid = f32 ? (const T*)c->dp_ggrid32 : (const T*)c->dp_ggrid;
   p.G0 = c->dp.G0;
   p.map = c->dp.map;
-  p.items = set.items;
-  p.n_items = set.n_items;
   p.counter = w.counter;
   p.slab = (T*)w.slab;
-  p.slab_per_cta = (int64_t)(w.slab_per_cta_bytes / sizeof(T));
   p.x = x;
   p.ldx = ldx;
   p.ht = ht;
@@ -654,9 +984,26 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
   if (P.keo_type == 1)
     for (int i = 0; i < P.D; ++i)
       for (int j = i + 1; j < P.D; ++j) p.has_offdiag |= (P.G0[i + (size_t)P.D * j] != 0.0);
-  EVR_CU(cudaMemsetAsync(w.counter, 0, sizeof(int), s), "memset counter");
-  hpsi_items_kernel<T><<<w.grid, kThreads, w.smem_bytes, s>>>(p);
-  EVR_CU(cudaGetLastError(), "hpsi_items_kernel launch");
+  // FP32: G(Q) on the fly from g (cheaper than reading the grid table); FP64: grid table
+  p.gT = (f32 && c->dp_ggrid32) ? (const T*)c->dp.g32 : nullptr;
+  p.G0T = f32 ? (const T*)c->dp.G032 : (const T*)c->dp.G0;
+  EVR_CU(cudaMemsetAsync(w.counter, 0, 2 * sizeof(int), s), "memset counter");
+  if (set.n_slab > 0) {
+    ItemParams<T> ps = p;
+    ps.items = set.items_slab;
+    ps.n_items = set.n_slab;
+    ps.counter = w.counter + 1;
+    ps.slab_per_cta = (int64_t)(w.slab_slab_bytes / sizeof(T));
+    hpsi_slab_kernel<T><<<w.grid_slab, kSlabThreads, w.smem_slab_bytes, s>>>(ps);
+    EVR_CU(cudaGetLastError(), "hpsi_slab_kernel launch");
+  }
+  if (set.n_items > 0) {
+    p.items = set.items;
+    p.n_items = set.n_items;
+    p.slab_per_cta = (int64_t)(w.slab_per_cta_bytes / sizeof(T));
+    hpsi_items_kernel<T><<<w.grid, kThreads, w.smem_bytes, s>>>(p);
+    EVR_CU(cudaGetLastError(), "hpsi_items_kernel launch");
+  }
   return EVR_OK;
 }
 
@@ -684,8 +1031,9 @@ static int run_items(evr_ctx* c, const ItemSet& set, const double* x, int64_t ld
                                                 op == OP_HSYM ? 0.5 : 1.0, y, ldy, N, nvec);
   EVR_CU(cudaGetLastError(), "csr_reduce_kernel launch");
   if (!c->capturing) EVR_CU(cudaEventRecord(c->ev[2], s), "event");
-  c->last_kernels = op == OP_HSYM ? 3 : 2;
-  c->last_items = (int64_t)set.n_items * (op == OP_HSYM ? 2 : 1);
+  const int per_op = (set.n_slab > 0 ? 1 : 0) + (set.n_items > 0 ? 1 : 0);
+  c->last_kernels = per_op * (op == OP_HSYM ? 2 : 1) + 1;
+  c->last_items = (int64_t)(set.n_items + set.n_slab) * (op == OP_HSYM ? 2 : 1);
   return EVR_OK;
 }
 

@@ -267,16 +267,33 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
   // grid, d1gg^T / d2gg^T on the grid and d0b^T on the way back
   std::vector<std::vector<int>> off_d0(D), off_bgw(D), off_d1(D), off_d2(D), off_x(D);
   std::vector<std::vector<int>> offT_in(D), offT_out(D), offT_d1(D), offT_d2(D);
+  // slab-mode products: d1.d0b, d2.d0b (nq x nb), bgw.d1, bgw.d2 (nb x nq), and the
+  // transposed operator's counterparts
+  std::vector<std::vector<int>> off_x1(D), off_x2(D), off_e1(D), off_e2(D);
+  std::vector<std::vector<int>> offT_x1(D), offT_x2(D), offT_e1(D), offT_e2(D);
   auto transpose = [](const std::vector<double>& a, int r, int cc) {
     std::vector<double> t((size_t)r * cc);
     for (int i = 0; i < r; ++i) for (int j = 0; j < cc; ++j) t[j + (size_t)cc * i] = a[i + (size_t)r * j];
     return t;
+  };
+  // (r x k) . (k x c), column-major, accumulated in long double
+  auto matmul = [](const std::vector<double>& a, const std::vector<double>& b, int r, int k, int c) {
+    std::vector<double> o((size_t)r * c);
+    for (int i = 0; i < r; ++i)
+      for (int j = 0; j < c; ++j) {
+        long double s = 0.0L;
+        for (int m = 0; m < k; ++m) s += (long double)a[i + (size_t)r * m] * b[m + (size_t)k * j];
+        o[i + (size_t)r * j] = (double)s;
+      }
+    return o;
   };
   P.symmetric = true;
   for (int i = 0; i < D; ++i) {
     int nl = (int)P.bas[i].size();
     off_d0[i].resize(nl); off_bgw[i].resize(nl); off_d1[i].resize(nl); off_d2[i].resize(nl); off_x[i].resize(nl);
     offT_in[i].resize(nl); offT_out[i].resize(nl); offT_d1[i].resize(nl); offT_d2[i].resize(nl);
+    off_x1[i].resize(nl); off_x2[i].resize(nl); off_e1[i].resize(nl); off_e2[i].resize(nl);
+    offT_x1[i].resize(nl); offT_x2[i].resize(nl); offT_e1[i].resize(nl); offT_e2[i].resize(nl);
     for (int L = 0; L < nl; ++L) {
       const Basis1D& b = P.bas[i][L];
       if (b.nq != b.nb) P.symmetric = false;
@@ -299,6 +316,17 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
       offT_out[i][L] = put(transpose(b.d0b, b.nq, b.nb), b.nb, b.nq);  // nb x nq
       offT_d1[i][L] = put(transpose(b.d1gg, b.nq, b.nq), b.nq, b.nq);
       offT_d2[i][L] = put(transpose(b.d2gg, b.nq, b.nq), b.nq, b.nq);
+      const std::vector<double> wd0b = transpose(b.bgw, b.nb, b.nq);  // w.d0b (nq x nb)
+      const std::vector<double> d1T = transpose(b.d1gg, b.nq, b.nq), d2T = transpose(b.d2gg, b.nq, b.nq);
+      const std::vector<double> d0bT = transpose(b.d0b, b.nq, b.nb);
+      off_x1[i][L] = put(matmul(b.d1gg, b.d0b, b.nq, b.nq, b.nb), b.nq, b.nb);
+      off_x2[i][L] = put(matmul(b.d2gg, b.d0b, b.nq, b.nq, b.nb), b.nq, b.nb);
+      off_e1[i][L] = put(matmul(b.bgw, b.d1gg, b.nb, b.nq, b.nq), b.nb, b.nq);
+      off_e2[i][L] = put(matmul(b.bgw, b.d2gg, b.nb, b.nq, b.nq), b.nb, b.nq);
+      offT_x1[i][L] = put(matmul(d1T, wd0b, b.nq, b.nq, b.nb), b.nq, b.nb);
+      offT_x2[i][L] = put(matmul(d2T, wd0b, b.nq, b.nq, b.nb), b.nq, b.nb);
+      offT_e1[i][L] = put(matmul(d0bT, d1T, b.nb, b.nq, b.nq), b.nb, b.nq);
+      offT_e2[i][L] = put(matmul(d0bT, d2T, b.nb, b.nq, b.nq), b.nb, b.nq);
     }
   }
 
@@ -306,19 +334,34 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
   const int nterm = (int)(P.term_l.size() / D);
   P.terms.resize(nterm); P.weight.resize(nterm);
   int64_t onb = 0, onq = 0;
+  std::vector<std::vector<int>> perms(nterm);
   for (int t = 0; t < nterm; ++t) {
     TermDesc& T = P.terms[t];
     std::memset(&T, 0, sizeof(T));
     int64_t NB = 1, NQ = 1;
     int s = 0;
-    for (int i = 0; i < D; ++i) {
+    // mode order: every mode but the one with the most grid points (the last such), then it
+    int slab = 0;
+    for (int i = 0; i < D; ++i)
+      if (P.bas[i][P.term_l[(size_t)t * D + i]].nq >= P.bas[slab][P.term_l[(size_t)t * D + slab]].nq) slab = i;
+    std::vector<int>& pm = perms[t];
+    for (int i = 0; i < D; ++i)
+      if (i != slab) pm.push_back(i);
+    pm.push_back(slab);
+    for (int p = 0; p < D; ++p) {
+      const int i = pm[p];
       int L = P.term_l[(size_t)t * D + i];
       s += L;
       const Basis1D& b = P.bas[i][L];
-      T.nb[i] = b.nb; T.nq[i] = b.nq;
-      T.m_d0b[i] = off_d0[i][L]; T.m_bgw[i] = off_bgw[i][L]; T.m_d1[i] = off_d1[i][L];
-      T.m_d2[i] = off_d2[i][L]; T.m_x[i] = off_x[i][L];
+      T.perm[p] = i;
+      T.nb[p] = b.nb; T.nq[p] = b.nq;
+      T.m_d0b[p] = off_d0[i][L]; T.m_bgw[p] = off_bgw[i][L]; T.m_d1[p] = off_d1[i][L];
+      T.m_d2[p] = off_d2[i][L]; T.m_x[p] = off_x[i][L];
       NB *= b.nb; NQ *= b.nq;
+    }
+    {
+      const int L = P.term_l[(size_t)t * D + slab];
+      T.m_x1L = off_x1[slab][L]; T.m_x2L = off_x2[slab][L]; T.m_e1L = off_e1[slab][L]; T.m_e2L = off_e2[slab][L];
     }
     if (NB > (1 << 30) || NQ > (1 << 30)) { err = "term too large"; return EVR_EINVAL; }
     T.NB = (int32_t)NB; T.NQ = (int32_t)NQ; T.off_nb = onb; T.off_nq = onq;
@@ -334,10 +377,14 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
   P.termsT = P.terms;
   for (int t = 0; t < nterm; ++t) {
     TermDesc& T = P.termsT[t];
-    for (int i = 0; i < D; ++i) {
+    for (int p = 0; p < D; ++p) {
+      const int i = perms[t][p];
       int L = P.term_l[(size_t)t * D + i];
-      T.m_d0b[i] = offT_in[i][L]; T.m_bgw[i] = offT_out[i][L]; T.m_d1[i] = offT_d1[i][L]; T.m_d2[i] = offT_d2[i][L];
+      T.m_d0b[p] = offT_in[i][L]; T.m_bgw[p] = offT_out[i][L]; T.m_d1[p] = offT_d1[i][L]; T.m_d2[p] = offT_d2[i][L];
     }
+    const int i = perms[t][D - 1];
+    const int L = P.term_l[(size_t)t * D + i];
+    T.m_x1L = offT_x1[i][L]; T.m_x2L = offT_x2[i][L]; T.m_e1L = offT_e1[i][L]; T.m_e2L = offT_e2[i][L];
   }
 
   // packed basis: SG4 -> all n with sum l(n_i) <= LB, last index fastest
@@ -382,19 +429,42 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
   rank.reserve((size_t)P.Np * 2);
   for (int64_t k = 0; k < P.Np; ++k) rank[key_of(&P.packed[(size_t)k * D])] = (int)k;
 
-  // map: term-local tuples, first mode fastest; excluded when sum l > LB
+  // map: term-local tuples, first mode fastest; excluded when sum l > LB.  map keeps the
+  // reference's term-local order, map_perm the device's (permuted modes, first fastest);
+  // grid_perm sends a device grid point to the reference's point of the same term.
   P.map.assign((size_t)P.sum_nb, -1);
+  P.map_perm.assign((size_t)P.sum_nb, -1);
+  P.grid_perm.assign((size_t)P.sum_nq, 0);
   for (int t = 0; t < nterm; ++t) {
     const TermDesc& T = P.terms[t];
+    std::vector<int> nbo(D), nqo(D);
+    for (int i = 0; i < D; ++i) {
+      const Basis1D& b = P.bas[i][P.term_l[(size_t)t * D + i]];
+      nbo[i] = b.nb; nqo[i] = b.nq;
+    }
+    std::vector<int64_t> sb(D), sq(D);  // strides of the reference modes in the device order
+    int64_t acc_b = 1, acc_q = 1;
+    for (int p = 0; p < D; ++p) { sb[T.perm[p]] = acc_b; sq[T.perm[p]] = acc_q; acc_b *= T.nb[p]; acc_q *= T.nq[p]; }
     std::vector<int> ib(D, 1);
     for (int64_t iB = 0; iB < T.NB; ++iB) {
       int s = 0;
-      for (int i = 0; i < D; ++i) s += P.ltab[i][ib[i]];
+      int64_t iBp = 0;
+      for (int i = 0; i < D; ++i) { s += P.ltab[i][ib[i]]; iBp += (int64_t)(ib[i] - 1) * sb[i]; }
       if (P.kind == EVR_BASIS_DP || s <= P.LB) {
         auto it = rank.find(key_of(ib.data()));
-        if (it != rank.end()) P.map[(size_t)T.off_nb + iB] = it->second;
+        if (it != rank.end()) {
+          P.map[(size_t)T.off_nb + iB] = it->second;
+          P.map_perm[(size_t)T.off_nb + iBp] = it->second;
+        }
       }
-      for (int i = 0; i < D; ++i) { if (++ib[i] <= T.nb[i]) break; ib[i] = 1; }
+      for (int i = 0; i < D; ++i) { if (++ib[i] <= nbo[i]) break; ib[i] = 1; }
+    }
+    std::vector<int> iq(D, 0);
+    for (int64_t q = 0; q < T.NQ; ++q) {
+      int64_t qp = 0;
+      for (int i = 0; i < D; ++i) qp += (int64_t)iq[i] * sq[i];
+      P.grid_perm[(size_t)T.off_nq + qp] = T.off_nq + q;
+      for (int i = 0; i < D; ++i) { if (++iq[i] < nqo[i]) break; iq[i] = 0; }
     }
   }
 
@@ -406,7 +476,7 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
     const TermDesc& T = P.terms[t];
     if (T.weight == 0.0) continue;
     for (int64_t iB = 0; iB < T.NB; ++iB) {
-      int k = P.map[(size_t)T.off_nb + iB];
+      int k = P.map_perm[(size_t)T.off_nb + iB];
       if (k < 0) continue;
       for (int a = 0; a < nb0; ++a) cnt[k + P.Np * a + 1]++;
     }
@@ -420,7 +490,7 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
     if (T.weight == 0.0) continue;
     for (int a = 0; a < nb0; ++a)
       for (int64_t iB = 0; iB < T.NB; ++iB) {
-        int k = P.map[(size_t)T.off_nb + iB];
+        int k = P.map_perm[(size_t)T.off_nb + iB];
         if (k < 0) continue;
         int64_t row = k + P.Np * a, pos = fill[row]++;
         P.csr_src[pos] = T.off_nb * nb0 + (int64_t)a * T.NB + iB;

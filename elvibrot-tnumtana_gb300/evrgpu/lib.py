@@ -53,7 +53,8 @@ class DavidsonOpts(C.Structure):
 
 
 EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_tables", "evr_get_basis",
-           "evr_get_vgrid", "evr_hpsi_host", "evr_hpsi_device", "evr_set_operator", "evr_last_launch_count",
+           "evr_get_vgrid", "evr_hpsi_host", "evr_hpsi_device", "evr_set_operator", "evr_set_kernel_path",
+           "evr_last_launch_count",
            "evr_last_kernel_ms",
            "evr_davidson",
            "evr_cheby_propagate", "evr_fma_peak"]
@@ -89,6 +90,7 @@ def load(build: bool = True):
     L.evr_last_launch_count.argtypes = [vp, _lp, _lp]
     L.evr_last_kernel_ms.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.evr_set_operator.argtypes = [vp, C.c_int]
+    L.evr_set_kernel_path.argtypes = [vp, C.c_int]
     L.evr_fma_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     if hasattr(L, "evr_davidson"):
         L.evr_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _dp, _dp, _dp, _lp]
@@ -269,6 +271,10 @@ class Problem:
         if rc not in (0, EVR_ENOCONV):
             self._check(rc)
         return eig, vec, stats
+
+    def set_kernel_path(self, slab: bool):
+        """True: slab-streaming kernel for the terms that fit (default); False: general kernel."""
+        self._check(load().evr_set_kernel_path(self.h, 1 if slab else 0))
 
     def set_operator(self, form):
         """'H' (the reference's OpPsi), 'HT' (its transpose) or 'HSYM' ((H+H^T)/2)."""

@@ -134,6 +134,11 @@ int evr_hpsi_device(evr_ctx *ctx, const double *psi, int64_t ld_psi, double *hps
 #define EVR_OP_HSYM 2
 int evr_set_operator(evr_ctx *ctx, int form);
 
+/* Kernel path of evr_hpsi_*: 1 (default) runs every term whose slab pipeline fits one
+ * CTA's shared memory in the slab-streaming kernel and the rest in the general kernel;
+ * 0 runs every term in the general kernel.  Both compute the same operator. */
+int evr_set_kernel_path(evr_ctx *ctx, int slab);
+
 /* Launch statistics of the last evr_hpsi_* call (kernels launched, work items). */
 int evr_last_launch_count(const evr_ctx *ctx, int64_t *kernels, int64_t *items);
 /* Device time (ms) of the term-pipeline kernel and of the weighted reduction of the last

@@ -39,10 +39,12 @@ def rel(a, b):
     return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
 
 
+@pytest.mark.parametrize("slab", [True, False], ids=["slab", "general"])
 @pytest.mark.parametrize("name", list(CASES))
 @pytest.mark.parametrize("nvec", [1, 5, 64])
-def test_hpsi_fp64_matches_oracle(name, nvec):
+def test_hpsi_fp64_matches_oracle(name, nvec, slab):
     spec, pg, po = problems(name)
+    pg.set_kernel_path(slab)
     rng = np.random.default_rng(123 + nvec)
     psi = rng.standard_normal((pg.N, nvec))
     ref = po.hpsi(psi)
@@ -50,9 +52,12 @@ def test_hpsi_fp64_matches_oracle(name, nvec):
     assert rel(out, ref) <= FP64_TOL
 
 
-@pytest.mark.parametrize("name", ["hh6d_l3_type1", "dp3_type10_g", "sg4_d6_l4_type10_g", "pyrazine12d_nb0_2"])
-def test_hpsi_fp32_matches_oracle(name):
+@pytest.mark.parametrize("slab", [True, False], ids=["slab", "general"])
+@pytest.mark.parametrize("name", ["hh6d_l3_type1", "dp3_type10_g", "sg4_d6_l4_type10_g", "pyrazine12d_nb0_2",
+                                  "sg4_d12_l2"])
+def test_hpsi_fp32_matches_oracle(name, slab):
     spec, pg, po = problems(name)
+    pg.set_kernel_path(slab)
     rng = np.random.default_rng(7)
     psi = rng.standard_normal((pg.N, 16))
     ref = po.hpsi(psi)
@@ -108,7 +113,11 @@ def test_linearity_and_oracle_sg4_6d_l8():
     hb = pg.hpsi(a[:, :1] * 2.0 - a[:, 1:] * 0.5)
     assert rel(hb[:, 0], 2.0 * ha[:, 0] - 0.5 * ha[:, 1]) <= 1e-12
     po = O.OracleProblem(spec)
-    assert rel(ha, po.hpsi(a)) <= FP64_TOL
+    ref = po.hpsi(a)
+    assert rel(ha, ref) <= FP64_TOL
+    assert rel(pg.hpsi(a, prec="fp32"), ref) <= FP32_TOL
+    pg.set_kernel_path(False)
+    assert rel(pg.hpsi(a), ref) <= FP64_TOL
 
 
 def test_errors_are_reported_not_fatal():
