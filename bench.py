@@ -150,15 +150,16 @@ def run_profile(args):
     y = torch.empty_like(x)
     st = torch.cuda.Stream()
     torch.cuda.set_stream(st)
-    out = {}
-    for prec in ("fp64", "fp32"):
+    out, launches = {}, {}
+    for prec in (("fp64", "fp32") if args.prec == "both" else (args.prec,)):
         for _ in range(args.steps):
             p.hpsi_device(x.data_ptr(), NVEC, y.data_ptr(), NVEC, NVEC, layout=E.LAYOUT_INTERLEAVED, prec=prec,
                           stream=st.cuda_stream)
         torch.cuda.synchronize()
         out[prec] = p.last_kernel_ms()[0]
+        launches[prec] = p.last_launch_count()
     print(json.dumps({"profile": args.profile, "N": p.N, "terms": p.nterm, "gflop_per_hpsi": p.flop_per_hpsi / 1e9,
-                      "items_ms": out}))
+                      "items_ms": out, "kernels_items": launches}))
     return 0
 
 
@@ -188,6 +189,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", default=None, choices=["sg4_6d_l6", "sg4_6d_l8"],
                     help="profiling mode: a few H.psi launches of the named workload, nothing else")
+    ap.add_argument("--prec", default="both", choices=["both", "fp64", "fp32"], help="precision(s) in profiling mode")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
