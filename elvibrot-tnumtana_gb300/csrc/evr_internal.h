@@ -105,8 +105,6 @@ struct DeviceProblem {
   double* csr_w = nullptr;
   double* G0 = nullptr;
   double* g = nullptr;
-  float* G032 = nullptr;
-  float* g32 = nullptr;
   double* mono_coef = nullptr;
   int* mono_idx = nullptr;
   int* mono_elec = nullptr;

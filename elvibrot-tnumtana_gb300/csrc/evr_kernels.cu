@@ -50,8 +50,6 @@ struct ItemParams {
   int D, nb0, keo_type;
   int has_offdiag;         // type 1 with off-diagonal F2 terms
   int vtrans;              // 1: V_ab read as V_ba (transposed operator)
-  const T* gT;             // g in T precision (on-the-fly G(Q) in the slab kernel), or nullptr
-  const T* G0T;            // G0 in T precision
 };
 
 constexpr int kSlabThreads = 512;
@@ -84,49 +82,96 @@ __device__ __forceinline__ void fma_column(T (&accv)[MAXM], const T* __restrict_
     }
 }
 
-// Loads of a fibre are issued eight at a time so that each thread keeps eight memory
-// requests in flight before the FMAs that consume them.
-template <typename T, int MAXM>
+// Division by a loop-invariant divisor d >= 1 for 0 <= n < 2^31 with one multiply-high:
+// q = (umulhi(m, n) + n) >> l, l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1.
+struct FastDiv {
+  uint32_t d, m, l;
+  __device__ __forceinline__ explicit FastDiv(uint32_t dd) : d(dd), l(0) {
+    while ((1u << l) < d) ++l;
+    m = (uint32_t)((((uint64_t)1 << 32) * (((uint64_t)1 << l) - d)) / d + 1);
+  }
+  __device__ __forceinline__ uint32_t div(uint32_t n) const { return (__umulhi(m, n) + n) >> l; }
+};
+
+// Loads of a fibre are issued four at a time so that each thread keeps several memory
+// requests in flight before the FMAs that consume them; in FP32 a thread carries two
+// columns so that every matrix load feeds eight FMAs.
+template <typename T, int MAXM, int COLS>
 __device__ __forceinline__ void contract_m(const T* __restrict__ in, int64_t ldi, T* __restrict__ out, int64_t ldo,
                                            int A, int K, int M, int B, int Vt, const T* __restrict__ mat, T alpha,
                                            bool acc) {
   const int ncol = A * B * Vt;
   const int ldm = (M + 3) & ~3;
-  for (int col = threadIdx.x; col < ncol; col += blockDim.x) {
-    const int v = col % Vt;
-    const int r = col / Vt;
-    const int a = r % A, b = r / A;
-    const T* ip = in + (int64_t)(a + (int64_t)A * K * b) * ldi + v;
-    const int64_t istr = (int64_t)A * ldi;
-    T accv[MAXM];
+  const FastDiv dv((uint32_t)Vt), da((uint32_t)A);
+  const int64_t istr = (int64_t)A * ldi, ostr = (int64_t)A * ldo;
+  for (int col0 = threadIdx.x; col0 < ncol; col0 += COLS * blockDim.x) {
+    const T* ip[COLS];
+    T* op[COLS];
+    bool on[COLS];
 #pragma unroll
-    for (int m = 0; m < MAXM; ++m) accv[m] = T(0);
-    for (int k0 = 0; k0 < K; k0 += 8) {
-      T x[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) x[j] = (k0 + j < K) ? ip[(k0 + j) * istr] : T(0);
-#pragma unroll
-      for (int j = 0; j < 8; ++j)
-        if (k0 + j < K) fma_column<T, MAXM>(accv, mat + ldm * (k0 + j), x[j], M);
+    for (int c = 0; c < COLS; ++c) {
+      const int col = col0 + c * blockDim.x;
+      on[c] = col < ncol;
+      const int cc = on[c] ? col : col0;
+      const int r = (int)dv.div((uint32_t)cc);
+      const int v = cc - r * Vt;
+      const int b = (int)da.div((uint32_t)r);
+      const int a = r - b * A;
+      ip[c] = in + (int64_t)(a + (int64_t)A * K * b) * ldi + v;
+      op[c] = out + (int64_t)(a + (int64_t)A * M * b) * ldo + v;
     }
-    T* op = out + (int64_t)(a + (int64_t)A * M * b) * ldo + v;
-    const int64_t ostr = (int64_t)A * ldo;
+    T accv[COLS][MAXM];
 #pragma unroll
-    for (int m = 0; m < MAXM; ++m)
-      if (m < M) {
-        T val = alpha * accv[m];
-        if (acc) val += op[m * ostr];
-        op[m * ostr] = val;
+    for (int c = 0; c < COLS; ++c)
+#pragma unroll
+      for (int m = 0; m < MAXM; ++m) accv[c][m] = T(0);
+    for (int k0 = 0; k0 < K; k0 += 4) {
+      T x[COLS][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int c = 0; c < COLS; ++c) x[c][j] = (k0 + j < K) ? ip[c][(k0 + j) * istr] : T(0);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (k0 + j < K) {
+          const T* mk = mat + ldm * (k0 + j);
+#pragma unroll
+          for (int m4 = 0; m4 < MAXM; m4 += 4)
+            if (m4 < M) {
+              T c0, c1, c2, c3;
+              load4(mk + m4, c0, c1, c2, c3);
+#pragma unroll
+              for (int c = 0; c < COLS; ++c) {
+                accv[c][m4] = fma(c0, x[c][j], accv[c][m4]);
+                accv[c][m4 + 1] = fma(c1, x[c][j], accv[c][m4 + 1]);
+                accv[c][m4 + 2] = fma(c2, x[c][j], accv[c][m4 + 2]);
+                accv[c][m4 + 3] = fma(c3, x[c][j], accv[c][m4 + 3]);
+              }
+            }
+        }
       }
+    }
+#pragma unroll
+    for (int c = 0; c < COLS; ++c)
+      if (on[c])
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m)
+          if (m < M) {
+            T val = alpha * accv[c][m];
+            if (acc) val += op[c][m * ostr];
+            op[c][m * ostr] = val;
+          }
   }
 }
 
 template <typename T>
 __device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64_t ldo, int A, int K, int M, int B,
                                          int Vt, const T* mat, T alpha, bool acc) {
-  if (M <= 8) contract_m<T, 8>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
-  else if (M <= 16) contract_m<T, 16>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
-  else contract_m<T, 24>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  constexpr int C = sizeof(T) == 4 ? 2 : 1;
+  if (M <= 4) contract_m<T, 4, C>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  else if (M <= 8) contract_m<T, 8, C>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  else if (M <= 16) contract_m<T, 16, C>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  else contract_m<T, 24, C>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
 }
 
 // First B->G mode fused with the gather from the packed vector block:
@@ -137,21 +182,22 @@ __device__ __forceinline__ void gather_contract_m(const double* __restrict__ x, 
                                                   const T* __restrict__ mat) {
   const int ncol = B * Vt;
   const int ldm = (M + 3) & ~3;
+  const FastDiv dv((uint32_t)Vt);
   for (int col = threadIdx.x; col < ncol; col += blockDim.x) {
-    const int v = col % Vt;
-    const int b = col / Vt;
+    const int b = (int)dv.div((uint32_t)col);
+    const int v = col - b * Vt;
     T accv[MAXM];
 #pragma unroll
     for (int m = 0; m < MAXM; ++m) accv[m] = T(0);
-    for (int k0 = 0; k0 < K; k0 += 8) {
-      int pk[8];
+    for (int k0 = 0; k0 < K; k0 += 4) {
+      int pk[4];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) pk[j] = (k0 + j < K) ? __ldg(mp + k0 + j + K * b) : -1;
-      T xv[8];
+      for (int j = 0; j < 4; ++j) pk[j] = (k0 + j < K) ? __ldg(mp + k0 + j + K * b) : -1;
+      T xv[4];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) xv[j] = (pk[j] >= 0) ? (T)__ldg(x + (pk[j] + eoff) * ldx + v) : T(0);
+      for (int j = 0; j < 4; ++j) xv[j] = (pk[j] >= 0) ? (T)__ldg(x + (pk[j] + eoff) * ldx + v) : T(0);
 #pragma unroll
-      for (int j = 0; j < 8; ++j)
+      for (int j = 0; j < 4; ++j)
         if (k0 + j < K) fma_column<T, MAXM>(accv, mat + ldm * (k0 + j), xv[j], M);
     }
     T* op = out + (int64_t)M * b * Vt + v;
@@ -164,7 +210,8 @@ __device__ __forceinline__ void gather_contract_m(const double* __restrict__ x, 
 template <typename T>
 __device__ __forceinline__ void gather_contract(const double* x, int64_t ldx, const int* mp, int64_t eoff, T* out,
                                                 int K, int M, int B, int Vt, const T* mat) {
-  if (M <= 8) gather_contract_m<T, 8>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+  if (M <= 4) gather_contract_m<T, 4>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+  else if (M <= 8) gather_contract_m<T, 8>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
   else if (M <= 16) gather_contract_m<T, 16>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
   else gather_contract_m<T, 24>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
 }
@@ -388,70 +435,53 @@ __device__ __forceinline__ void slab_accumulate(T* __restrict__ W, int64_t ss, i
 }
 
 // Phi_i = sum_j G_ij(Q) y_j on one slab, in place: y_j = Y[j] (j < L) and P (j = L).
-// G(Q) = G0 + sum_k g_ijk Q_k is formed on the fly (gT), read from the grid table
-// (ggrid) or constant (G0); symmetric pairs are visited once.
+// One thread per grid point: G(Q) (symmetric pairs, from the grid table or the constant
+// G0) is read once and applied to the Vt vectors of the tile.
 template <typename T, int DM>
 __device__ __forceinline__ void slab_pointwise_G(const ItemParams<T>& p, const TermDesc& Tm, T* Y, T* P, int64_t ss,
                                                  int Vt, int q, int NQs, int nG) {
   const int D = p.D, L = D - 1;
-  for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) {
-    const int pt = (int)(a / Vt);
-    T y[DM], z[DM], Qp[DM];
-#pragma unroll
-    for (int j = 0; j < DM; ++j) {
-      y[j] = (j < L) ? Y[j * ss + a] : ((j == L) ? P[a] : T(0));
-      z[j] = T(0);
-    }
-    if (sizeof(T) == 4 && p.gT) {  // coordinates of the point, by position
-      int r = pt;
-#pragma unroll
-      for (int d = 0; d < DM; ++d) {
-        if (d < L) {
-          Qp[d] = __ldg(p.mats + Tm.m_x[d] + r % Tm.nq[d]);
-          r /= Tm.nq[d];
-        } else if (d == L) {
-          Qp[d] = __ldg(p.mats + Tm.m_x[d] + q);
-        } else {
-          Qp[d] = T(0);
-        }
-      }
-    }
+  // registers hold the point's G for the vector loop when it is small (FP32, D <= 8)
+  constexpr bool kCache = sizeof(T) == 4 && DM <= 8;
+  constexpr int kG = kCache ? DM * (DM + 1) / 2 : 1;
+  for (int pt = threadIdx.x; pt < NQs; pt += blockDim.x) {
+    T G[kG];
     const T* Gp = p.ggrid ? p.ggrid + Tm.off_nq * nG + (int64_t)q * NQs + pt : nullptr;
-    int c = 0;
+    // packed slot of (i, j), i <= j < D, in the table's order
+    auto slot = [D](int i, int j) { return i * D - i * (i - 1) / 2 + (j - i); };
+    auto gload = [&](int i, int j) -> T {
+      if (i >= D || j >= D) return T(0);
+      return Gp ? __ldg(Gp + (int64_t)slot(i, j) * Tm.NQ) : (T)__ldg(p.G0 + Tm.perm[i] + D * Tm.perm[j]);
+    };
+    if constexpr (kCache) {
 #pragma unroll
-    for (int i = 0; i < DM; ++i) {
-      if (i >= D) break;
+      for (int i = 0; i < DM; ++i)
 #pragma unroll
-      for (int j = i; j < DM; ++j) {
-        if (j >= D) break;
-        const int oi = Tm.perm[i], oj = Tm.perm[j];
-        T gij = T(0);
-        bool done = false;
-        if constexpr (sizeof(T) == 4) {  // FP32 forms G on the fly; FP64 reads the grid table
-          if (p.gT) {
-            gij = __ldg(p.G0T + oi + D * oj);
-            const T* gp = p.gT + oi + D * oj;
-#pragma unroll
-            for (int k = 0; k < DM; ++k)
-              if (k < D) gij = fma(__ldg(gp + D * D * Tm.perm[k]), Qp[k], gij);
-            done = true;
-          }
-        }
-        if (done) {
-        } else if (Gp) {
-          gij = __ldg(Gp + (int64_t)c * Tm.NQ);
-        } else {
-          gij = (T)__ldg(p.G0 + oi + D * oj);
-        }
-        ++c;
-        z[i] = fma(gij, y[j], z[i]);
-        if (j != i) z[j] = fma(gij, y[i], z[j]);
-      }
+        for (int j = i; j < DM; ++j) G[i * DM - i * (i - 1) / 2 + (j - i)] = gload(i, j);
     }
+    for (int v = 0; v < Vt; ++v) {
+      const int64_t a = (int64_t)pt * Vt + v;
+      T y[DM], z[DM];
 #pragma unroll
-    for (int i = 0; i < DM; ++i) {
-      if (i < L) Y[i * ss + a] = z[i];
-      else if (i == L) P[a] = z[i];
+      for (int j = 0; j < DM; ++j) {
+        y[j] = (j < L) ? Y[j * ss + a] : ((j == L) ? P[a] : T(0));
+        z[j] = T(0);
+      }
+#pragma unroll
+      for (int i = 0; i < DM; ++i)
+#pragma unroll
+        for (int j = i; j < DM; ++j) {
+          T gij;
+          if constexpr (kCache) gij = G[i * DM - i * (i - 1) / 2 + (j - i)];
+          else gij = gload(i, j);
+          z[i] = fma(gij, y[j], z[i]);
+          if (j != i) z[j] = fma(gij, y[i], z[j]);
+        }
+#pragma unroll
+      for (int i = 0; i < DM; ++i) {
+        if (i < L) Y[i * ss + a] = z[i];
+        else if (i == L) P[a] = z[i];
+      }
     }
   }
 }
@@ -822,10 +852,6 @@ int upload_problem(evr_ctx* c) {
     EVR_CU(cudaMalloc((void**)&c->dp_ggrid32, ng * sizeof(float)), "cudaMalloc ggrid32");
     to_float_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(gg, c->dp_ggrid32, ng);
   }
-  EVR_CU(cudaMalloc((void**)&d.G032, sizeof(float) * D * D), "cudaMalloc G032");
-  EVR_CU(cudaMalloc((void**)&d.g32, sizeof(float) * D * D * D), "cudaMalloc g32");
-  to_float_kernel<<<1, 256, 0, c->stream>>>(d.G0, d.G032, (int64_t)D * D);
-  to_float_kernel<<<4, 256, 0, c->stream>>>(d.g, d.g32, (int64_t)D * D * D);
   EVR_CU(cudaGetLastError(), "to_float_kernel");
   EVR_CU(cudaStreamSynchronize(c->stream), "grid set-up");
   return EVR_OK;
@@ -834,8 +860,7 @@ int upload_problem(evr_ctx* c) {
 void free_problem(evr_ctx* c) {
   DeviceProblem& d = c->dp;
   void* ptrs[] = {d.terms, d.termsT, d.mats, d.mats32, d.vgrid, d.vgrid32, d.map, d.csr_ptr, d.csr_src, d.csr_w,
-                  d.G0, d.g, d.G032, d.g32, d.mono_coef, d.mono_idx, d.mono_elec, d.e0diag, c->dp_ggrid,
-                  c->dp_ggrid32};
+                  d.G0, d.g, d.mono_coef, d.mono_idx, d.mono_elec, d.e0diag, c->dp_ggrid, c->dp_ggrid32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   d = DeviceProblem();
@@ -984,9 +1009,6 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
   if (P.keo_type == 1)
     for (int i = 0; i < P.D; ++i)
       for (int j = i + 1; j < P.D; ++j) p.has_offdiag |= (P.G0[i + (size_t)P.D * j] != 0.0);
-  // FP32: G(Q) on the fly from g (cheaper than reading the grid table); FP64: grid table
-  p.gT = (f32 && c->dp_ggrid32) ? (const T*)c->dp.g32 : nullptr;
-  p.G0T = f32 ? (const T*)c->dp.G032 : (const T*)c->dp.G0;
   EVR_CU(cudaMemsetAsync(w.counter, 0, 2 * sizeof(int), s), "memset counter");
   if (set.n_slab > 0) {
     ItemParams<T> ps = p;
