@@ -93,85 +93,70 @@ struct FastDiv {
   __device__ __forceinline__ uint32_t div(uint32_t n) const { return (__umulhi(m, n) + n) >> l; }
 };
 
-// Loads of a fibre are issued four at a time so that each thread keeps several memory
-// requests in flight before the FMAs that consume them; in FP32 a thread carries two
-// columns so that every matrix load feeds eight FMAs.
-template <typename T, int MAXM, int COLS>
-__device__ __forceinline__ void contract_m(const T* __restrict__ in, int64_t ldi, T* __restrict__ out, int64_t ldo,
-                                           int A, int K, int M, int B, int Vt, const T* __restrict__ mat, T alpha,
-                                           bool acc) {
-  const int ncol = A * B * Vt;
+// Matrix-stationary contraction: a thread owns MG consecutive output rows m0.. of the 1-D
+// matrix (held in registers) and one (a, v) lane, and walks the B dimension; each step
+// loads the K inputs of one fibre and issues MG*K FMAs.  Lanes are (a, v, row group);
+// when there are fewer lanes than threads the B dimension is split among them.
+template <typename T, int MAXK, int MG>
+__device__ __forceinline__ void contract_ms(const T* __restrict__ in, int64_t ldi, T* __restrict__ out, int64_t ldo,
+                                            int A, int K, int M, int B, int Vt, const T* __restrict__ mat, T alpha,
+                                            bool acc) {
   const int ldm = (M + 3) & ~3;
-  const FastDiv dv((uint32_t)Vt), da((uint32_t)A);
+  const int nmg = (M + MG - 1) / MG;
+  const int AV = A * Vt;
+  const int lanes = AV * nmg;
+  const int nthr = blockDim.x;
+  int nbg = nthr / lanes;  // B groups when lanes < threads
+  if (nbg < 1) nbg = 1;
+  if (nbg > B) nbg = B;
+  const int tasks = lanes * nbg;
+  const FastDiv dvt((uint32_t)Vt), dlanes((uint32_t)lanes), dav((uint32_t)AV);
   const int64_t istr = (int64_t)A * ldi, ostr = (int64_t)A * ldo;
-  for (int col0 = threadIdx.x; col0 < ncol; col0 += COLS * blockDim.x) {
-    const T* ip[COLS];
-    T* op[COLS];
-    bool on[COLS];
+  for (int task = threadIdx.x; task < tasks; task += nthr) {
+    const int bg = (int)dlanes.div((uint32_t)task);
+    const int lane = task - bg * lanes;
+    const int mg = (int)dav.div((uint32_t)lane);
+    const int av = lane - mg * AV;
+    const int a = (int)dvt.div((uint32_t)av);
+    const int v = av - a * Vt;
+    const int m0 = mg * MG;
+    T strip[MG][MAXK];
 #pragma unroll
-    for (int c = 0; c < COLS; ++c) {
-      const int col = col0 + c * blockDim.x;
-      on[c] = col < ncol;
-      const int cc = on[c] ? col : col0;
-      const int r = (int)dv.div((uint32_t)cc);
-      const int v = cc - r * Vt;
-      const int b = (int)da.div((uint32_t)r);
-      const int a = r - b * A;
-      ip[c] = in + (int64_t)(a + (int64_t)A * K * b) * ldi + v;
-      op[c] = out + (int64_t)(a + (int64_t)A * M * b) * ldo + v;
-    }
-    T accv[COLS][MAXM];
+    for (int mm = 0; mm < MG; ++mm)
 #pragma unroll
-    for (int c = 0; c < COLS; ++c)
+      for (int k = 0; k < MAXK; ++k)
+        strip[mm][k] = (k < K && m0 + mm < M) ? __ldg(mat + (m0 + mm) + ldm * k) : T(0);
+    const T* ip = in + (int64_t)a * ldi + v + (int64_t)bg * K * istr;
+    T* op = out + (int64_t)a * ldo + v + (int64_t)m0 * ostr + (int64_t)bg * M * ostr;
+    const int64_t istep = (int64_t)nbg * K * istr, ostep = (int64_t)nbg * M * ostr;
+    for (int b = bg; b < B; b += nbg, ip += istep, op += ostep) {
+      T x[MAXK];
 #pragma unroll
-      for (int m = 0; m < MAXM; ++m) accv[c][m] = T(0);
-    for (int k0 = 0; k0 < K; k0 += 4) {
-      T x[COLS][4];
+      for (int k = 0; k < MAXK; ++k) x[k] = (k < K) ? ip[k * istr] : T(0);
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
+      for (int mm = 0; mm < MG; ++mm) {
+        T s = T(0);
 #pragma unroll
-        for (int c = 0; c < COLS; ++c) x[c][j] = (k0 + j < K) ? ip[c][(k0 + j) * istr] : T(0);
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        if (k0 + j < K) {
-          const T* mk = mat + ldm * (k0 + j);
-#pragma unroll
-          for (int m4 = 0; m4 < MAXM; m4 += 4)
-            if (m4 < M) {
-              T c0, c1, c2, c3;
-              load4(mk + m4, c0, c1, c2, c3);
-#pragma unroll
-              for (int c = 0; c < COLS; ++c) {
-                accv[c][m4] = fma(c0, x[c][j], accv[c][m4]);
-                accv[c][m4 + 1] = fma(c1, x[c][j], accv[c][m4 + 1]);
-                accv[c][m4 + 2] = fma(c2, x[c][j], accv[c][m4 + 2]);
-                accv[c][m4 + 3] = fma(c3, x[c][j], accv[c][m4 + 3]);
-              }
-            }
+        for (int k = 0; k < MAXK; ++k) s = fma(strip[mm][k], x[k], s);
+        if (m0 + mm < M) {
+          T val = alpha * s;
+          if (acc) val += op[mm * ostr];
+          op[mm * ostr] = val;
         }
       }
     }
-#pragma unroll
-    for (int c = 0; c < COLS; ++c)
-      if (on[c])
-#pragma unroll
-        for (int m = 0; m < MAXM; ++m)
-          if (m < M) {
-            T val = alpha * accv[c][m];
-            if (acc) val += op[c][m * ostr];
-            op[c][m * ostr] = val;
-          }
   }
 }
 
 template <typename T>
 __device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64_t ldo, int A, int K, int M, int B,
                                          int Vt, const T* mat, T alpha, bool acc) {
-  constexpr int C = sizeof(T) == 4 ? 2 : 1;
-  if (M <= 4) contract_m<T, 4, C>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
-  else if (M <= 8) contract_m<T, 8, C>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
-  else if (M <= 16) contract_m<T, 16, C>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
-  else contract_m<T, 24, C>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  // register budget of the matrix strip: MG*MAXK values (FP32 up to 64, FP64 up to 24)
+  constexpr bool f32 = sizeof(T) == 4;
+  if (K <= 4) contract_ms<T, 4, f32 ? 8 : 4>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  else if (K <= 8) contract_ms<T, 8, f32 ? 8 : 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  else if (K <= 16) contract_ms<T, 16, f32 ? 4 : 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  else contract_ms<T, 24, f32 ? 2 : 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
 }
 
 // First B->G mode fused with the gather from the packed vector block:
