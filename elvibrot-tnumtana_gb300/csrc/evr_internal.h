@@ -48,8 +48,23 @@ struct TermDesc {
   // last-position (slab) mode: d1.d0b, d2.d0b (grid <- basis) and bgw.d1, bgw.d2
   // (basis <- grid), padded like the others
   int32_t m_x1L, m_x2L, m_e1L, m_e2L;
+  int32_t msz;           // elements of the term's 1-D matrices staged in shared memory
+  int32_t pad_;
   double weight;
 };
+
+// elements of one staged matrix block: rows padded to 4, times the columns
+__host__ __device__ inline int mat_block(int rows, int cols) { return ((rows + 3) & ~3) * cols; }
+// shared-memory elements of a term's matrices (d0b, bgw, d1, d2 per position, and the
+// last position's d1.d0b, bgw.d1, bgw.d2), in the order the kernels stage them
+__host__ __device__ inline int term_matrix_elems(const TermDesc& T, int D) {
+  int s = 0;
+  for (int p = 0; p < D; ++p)
+    s += mat_block(T.nq[p], T.nb[p]) + mat_block(T.nb[p], T.nq[p]) + 2 * mat_block(T.nq[p], T.nq[p]);
+  const int L = D - 1;
+  s += mat_block(T.nq[L], T.nb[L]) + 2 * mat_block(T.nb[L], T.nq[L]);
+  return s;
+}
 
 // One unit of work of the H.psi kernel: one term, a tile of vectors.
 struct WorkItem {

@@ -56,14 +56,14 @@ constexpr int kSlabThreads = 512;
 
 // out(a, m, b, v) = alpha * sum_k mat[m + M*k] * in(a, k, b, v)  (+ out if acc)
 // element (a, k, b, v) of a tensor with vector stride ld lives at ((a + A*(k + K*b))*ld + v).
-// four consecutive matrix coefficients in one 16-byte read-only load
+// four consecutive matrix coefficients (staged in shared memory) in one 16-byte load
 __device__ __forceinline__ void load4(const float* p, float& a, float& b, float& c, float& d) {
-  const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+  const float4 v = *reinterpret_cast<const float4*>(p);
   a = v.x; b = v.y; c = v.z; d = v.w;
 }
 __device__ __forceinline__ void load4(const double* p, double& a, double& b, double& c, double& d) {
-  const double2 u = __ldg(reinterpret_cast<const double2*>(p));
-  const double2 w = __ldg(reinterpret_cast<const double2*>(p) + 1);
+  const double2 u = reinterpret_cast<const double2*>(p)[0];
+  const double2 w = reinterpret_cast<const double2*>(p)[1];
   a = u.x; b = u.y; c = w.x; d = w.y;
 }
 
@@ -125,7 +125,7 @@ __device__ __forceinline__ void contract_ms(const T* __restrict__ in, int64_t ld
     for (int mm = 0; mm < MG; ++mm)
 #pragma unroll
       for (int k = 0; k < MAXK; ++k)
-        strip[mm][k] = (k < K && m0 + mm < M) ? __ldg(mat + (m0 + mm) + ldm * k) : T(0);
+        strip[mm][k] = (k < K && m0 + mm < M) ? mat[(m0 + mm) + ldm * k] : T(0);
     const T* ip = in + (int64_t)a * ldi + v + (int64_t)bg * K * istr;
     T* op = out + (int64_t)a * ldo + v + (int64_t)m0 * ostr + (int64_t)bg * M * ostr;
     const int64_t istep = (int64_t)nbg * K * istr, ostep = (int64_t)nbg * M * ostr;
@@ -148,15 +148,91 @@ __device__ __forceinline__ void contract_ms(const T* __restrict__ in, int64_t ld
   }
 }
 
+// Loads of a fibre are issued four at a time so that each thread keeps several memory
+// requests in flight before the FMAs that consume them; in FP32 a thread carries two
+// columns so that every matrix load feeds eight FMAs.
+template <typename T, int MAXM, int COLS>
+__device__ __forceinline__ void contract_m(const T* __restrict__ in, int64_t ldi, T* __restrict__ out, int64_t ldo,
+                                           int A, int K, int M, int B, int Vt, const T* __restrict__ mat, T alpha,
+                                           bool acc) {
+  const int ncol = A * B * Vt;
+  const int ldm = (M + 3) & ~3;
+  const FastDiv dv((uint32_t)Vt), da((uint32_t)A);
+  const int64_t istr = (int64_t)A * ldi, ostr = (int64_t)A * ldo;
+  for (int col0 = threadIdx.x; col0 < ncol; col0 += COLS * blockDim.x) {
+    const T* ip[COLS];
+    T* op[COLS];
+    bool on[COLS];
+#pragma unroll
+    for (int c = 0; c < COLS; ++c) {
+      const int col = col0 + c * blockDim.x;
+      on[c] = col < ncol;
+      const int cc = on[c] ? col : col0;
+      const int r = (int)dv.div((uint32_t)cc);
+      const int v = cc - r * Vt;
+      const int b = (int)da.div((uint32_t)r);
+      const int a = r - b * A;
+      ip[c] = in + (int64_t)(a + (int64_t)A * K * b) * ldi + v;
+      op[c] = out + (int64_t)(a + (int64_t)A * M * b) * ldo + v;
+    }
+    T accv[COLS][MAXM];
+#pragma unroll
+    for (int c = 0; c < COLS; ++c)
+#pragma unroll
+      for (int m = 0; m < MAXM; ++m) accv[c][m] = T(0);
+    for (int k0 = 0; k0 < K; k0 += 4) {
+      T x[COLS][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int c = 0; c < COLS; ++c) x[c][j] = (k0 + j < K) ? ip[c][(k0 + j) * istr] : T(0);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (k0 + j < K) {
+          const T* mk = mat + ldm * (k0 + j);
+#pragma unroll
+          for (int m4 = 0; m4 < MAXM; m4 += 4)
+            if (m4 < M) {
+              T c0, c1, c2, c3;
+              load4(mk + m4, c0, c1, c2, c3);
+#pragma unroll
+              for (int c = 0; c < COLS; ++c) {
+                accv[c][m4] = fma(c0, x[c][j], accv[c][m4]);
+                accv[c][m4 + 1] = fma(c1, x[c][j], accv[c][m4 + 1]);
+                accv[c][m4 + 2] = fma(c2, x[c][j], accv[c][m4 + 2]);
+                accv[c][m4 + 3] = fma(c3, x[c][j], accv[c][m4 + 3]);
+              }
+            }
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < COLS; ++c)
+      if (on[c])
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m)
+          if (m < M) {
+            T val = alpha * accv[c][m];
+            if (acc) val += op[c][m * ostr];
+            op[c][m * ostr] = val;
+          }
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64_t ldo, int A, int K, int M, int B,
                                          int Vt, const T* mat, T alpha, bool acc) {
-  // register budget of the matrix strip: MG*MAXK values (FP32 up to 64, FP64 up to 24)
-  constexpr bool f32 = sizeof(T) == 4;
-  if (K <= 4) contract_ms<T, 4, f32 ? 8 : 4>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
-  else if (K <= 8) contract_ms<T, 8, f32 ? 8 : 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
-  else if (K <= 16) contract_ms<T, 16, f32 ? 4 : 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
-  else contract_ms<T, 24, f32 ? 2 : 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  if constexpr (sizeof(T) == 4) {  // FP32: two columns per thread, matrix coefficients from L1
+    if (M <= 4) contract_m<T, 4, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (M <= 8) contract_m<T, 8, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (M <= 16) contract_m<T, 16, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else contract_m<T, 24, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  } else {  // FP64: matrix strip in registers (register budget MG*MAXK <= 24 doubles)
+    if (K <= 4) contract_ms<T, 4, 4>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (K <= 8) contract_ms<T, 8, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (K <= 16) contract_ms<T, 16, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else contract_ms<T, 24, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  }
 }
 
 // First B->G mode fused with the gather from the packed vector block:
@@ -201,11 +277,55 @@ __device__ __forceinline__ void gather_contract(const double* x, int64_t ldx, co
   else gather_contract_m<T, 24>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
 }
 
+// Copies the item's 1-D matrices from the global pool into shared memory (the layout of
+// term_matrix_elems) and points the shared TermDesc's offsets at the copies, so that every
+// contraction reads its coefficients from shared memory instead of a small, easily evicted
+// L1.
+struct StageBlocks {
+  int src[4 * kMaxD + 3], dst[4 * kMaxD + 3], n[4 * kMaxD + 3];
+  int count;
+};
+
+template <typename T>
+__device__ __forceinline__ void stage_matrices(TermDesc& Tm, int D, const T* __restrict__ pool, T* msm,
+                                               StageBlocks& sb) {
+  if (threadIdx.x == 0) {
+    int o = 0, c = 0;
+    auto add = [&](int32_t& off, int n) {
+      sb.src[c] = off;
+      sb.dst[c] = o;
+      sb.n[c] = n;
+      off = o;
+      o += n;
+      ++c;
+    };
+    for (int q = 0; q < D; ++q) {
+      add(Tm.m_d0b[q], mat_block(Tm.nq[q], Tm.nb[q]));
+      add(Tm.m_bgw[q], mat_block(Tm.nb[q], Tm.nq[q]));
+      add(Tm.m_d1[q], mat_block(Tm.nq[q], Tm.nq[q]));
+      add(Tm.m_d2[q], mat_block(Tm.nq[q], Tm.nq[q]));
+    }
+    const int L = D - 1;
+    add(Tm.m_x1L, mat_block(Tm.nq[L], Tm.nb[L]));
+    add(Tm.m_e1L, mat_block(Tm.nb[L], Tm.nq[L]));
+    add(Tm.m_e2L, mat_block(Tm.nb[L], Tm.nq[L]));
+    sb.count = c;
+  }
+  __syncthreads();
+  for (int b = 0; b < sb.count; ++b) {
+    const T* src = pool + sb.src[b];
+    T* dst = msm + sb.dst[b];
+    for (int i = threadIdx.x; i < sb.n[b]; i += blockDim.x) dst[i] = __ldg(src + i);
+  }
+  __syncthreads();
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   __shared__ TermDesc s_term;
+  __shared__ StageBlocks s_blocks;
   const int D = p.D, nb0 = p.nb0;
   while (true) {
     if (threadIdx.x == 0) s_item = atomicAdd(p.counter, 1);
@@ -219,9 +339,12 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
       for (int i = threadIdx.x; i < (int)(sizeof(TermDesc) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
+    T* const mb = reinterpret_cast<T*>(smem_raw);
+    stage_matrices<T>(s_term, D, p.mats, mb, s_blocks);
     const TermDesc& Tm = s_term;
     const int NQ = Tm.NQ, NB = Tm.NB, Vt = w.vt;
-    T* buf = w.smem ? reinterpret_cast<T*>(smem_raw) : p.slab + (int64_t)blockIdx.x * p.slab_per_cta;
+    const int mpad = (Tm.msz + 3) & ~3;
+    T* buf = w.smem ? reinterpret_cast<T*>(smem_raw) + mpad : p.slab + (int64_t)blockIdx.x * p.slab_per_cta;
     const int64_t stride = (int64_t)NQ * Vt;
     T* X0 = buf;                     // psi on the grid, nb0 components
     T* X1 = buf + nb0 * stride;      // H.psi accumulator, nb0 components
@@ -234,13 +357,13 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
       T* cur = (D % 2) ? A0 : A1;   // so that the chain ends in A0
       int nb_rest = NB / Tm.nb[0];
       gather_contract<T>(p.x + w.v0, p.ldx, p.map + Tm.off_nb, p.Np * e, cur, Tm.nb[0], Tm.nq[0], nb_rest, Vt,
-                         p.mats + Tm.m_d0b[0]);
+                         mb + Tm.m_d0b[0]);
       __syncthreads();
       int A = Tm.nq[0];
       for (int i = 1; i < D; ++i) {
         nb_rest /= Tm.nb[i];
         T* nxt = (cur == A0) ? A1 : A0;
-        contract<T>(cur, Vt, nxt, Vt, A, Tm.nb[i], Tm.nq[i], nb_rest, Vt, p.mats + Tm.m_d0b[i], T(1), false);
+        contract<T>(cur, Vt, nxt, Vt, A, Tm.nb[i], Tm.nq[i], nb_rest, Vt, mb + Tm.m_d0b[i], T(1), false);
         __syncthreads();
         cur = nxt;
         A *= Tm.nq[i];
@@ -273,7 +396,7 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
         int A = 1, Bq = NQ;
         for (int j = 0; j < D; ++j) {  // Y[j] = d1_j . psi_G
           Bq /= Tm.nq[j];
-          contract<T>(P0, Vt, Y + j * stride, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, p.mats + Tm.m_d1[j], T(1), false);
+          contract<T>(P0, Vt, Y + j * stride, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, mb + Tm.m_d1[j], T(1), false);
           A *= Tm.nq[j];
         }
         __syncthreads();
@@ -318,7 +441,7 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
         A = 1; Bq = NQ;
         for (int i = 0; i < D; ++i) {  // Acc += -1/2 d1_i . Y[i]; same-fibre updates per mode
           Bq /= Tm.nq[i];
-          contract<T>(Y + i * stride, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, p.mats + Tm.m_d1[i], T(-0.5), true);
+          contract<T>(Y + i * stride, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d1[i], T(-0.5), true);
           __syncthreads();
           A *= Tm.nq[i];
         }
@@ -333,7 +456,7 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
           Bq /= Tm.nq[i];
           const T f = (T)(-0.5 * __ldg(p.G0 + Tm.perm[i] + D * Tm.perm[i]));
           if (f != T(0))
-            contract<T>(P0, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, p.mats + Tm.m_d2[i], f, true);
+            contract<T>(P0, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d2[i], f, true);
           __syncthreads();
           A *= Tm.nq[i];
         }
@@ -346,9 +469,9 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
               const int Bj = NQ / (Aj * Tm.nq[j]);
               const T f = (T)(-__ldg(p.G0 + Tm.perm[i] + D * Tm.perm[j]));
               if (f != T(0)) {
-                contract<T>(P0, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, p.mats + Tm.m_d1[i], T(1), false);
+                contract<T>(P0, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, mb + Tm.m_d1[i], T(1), false);
                 __syncthreads();
-                contract<T>(Y, Vt, Acc, Vt, Aj, Tm.nq[j], Tm.nq[j], Bj, Vt, p.mats + Tm.m_d1[j], f, true);
+                contract<T>(Y, Vt, Acc, Vt, Aj, Tm.nq[j], Tm.nq[j], Bj, Vt, mb + Tm.m_d1[j], f, true);
                 __syncthreads();
               }
               Aj *= Tm.nq[j];
@@ -369,10 +492,10 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
         Bq /= Tm.nq[i];
         if (i == D - 1) {
           T* dst = p.ht + (Tm.off_nb * nb0 + (int64_t)e * NB) * p.ldh + w.v0;
-          contract<T>(cur, Vt, dst, p.ldh, A, Tm.nq[i], Tm.nb[i], Bq, Vt, p.mats + Tm.m_bgw[i], T(1), false);
+          contract<T>(cur, Vt, dst, p.ldh, A, Tm.nq[i], Tm.nb[i], Bq, Vt, mb + Tm.m_bgw[i], T(1), false);
         } else {
           T* nxt = (cur == A0) ? A1 : A0;
-          contract<T>(cur, Vt, nxt, Vt, A, Tm.nq[i], Tm.nb[i], Bq, Vt, p.mats + Tm.m_bgw[i], T(1), false);
+          contract<T>(cur, Vt, nxt, Vt, A, Tm.nq[i], Tm.nb[i], Bq, Vt, mb + Tm.m_bgw[i], T(1), false);
           cur = nxt;
         }
         __syncthreads();
@@ -395,7 +518,7 @@ __device__ __forceinline__ void slab_extract(const T* __restrict__ Tg, int64_t s
       for (int j = 0; j < 8; ++j) t[j] = (k0 + j < nL) ? Tg[a + ss * (k0 + j)] : T(0);
 #pragma unroll
       for (int j = 0; j < 8; ++j)
-        if (k0 + j < nL) s = fma(__ldg(X + ldx * (k0 + j)), t[j], s);
+        if (k0 + j < nL) s = fma(X[ldx * (k0 + j)], t[j], s);
     }
     P[a] = s;
   }
@@ -412,8 +535,8 @@ __device__ __forceinline__ void slab_accumulate(T* __restrict__ W, int64_t ss, i
     const T z = A2 ? c2 * A2[a] : T(0);
     for (int k = 0; k < nL; ++k) {
       T wv = W[a + ss * k];
-      wv = fma(__ldg(O + k), u, wv);
-      if (A2) wv = fma(__ldg(E + k), z, wv);
+      wv = fma(O[k], u, wv);
+      if (A2) wv = fma(E[k], z, wv);
       W[a + ss * k] = wv;
     }
   }
@@ -489,6 +612,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   __shared__ TermDesc s_term;
+  __shared__ StageBlocks s_blocks;
   const int D = p.D, L = D - 1;
   while (true) {
     if (threadIdx.x == 0) s_item = atomicAdd(p.counter, 1);
@@ -502,13 +626,15 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
       for (int i = threadIdx.x; i < (int)(sizeof(TermDesc) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
+    T* const mb = reinterpret_cast<T*>(smem_raw);
+    stage_matrices<T>(s_term, D, p.mats, mb, s_blocks);
     const TermDesc& Tm = s_term;
     const int Vt = w.vt;
     const int gL = Tm.nq[L], nL = Tm.nb[L];
     const int NQs = Tm.NQ / gL;
     const int64_t ss = (int64_t)NQs * Vt;  // one slab array
     const int64_t tsz = ss * nL;           // T and W
-    T* sm = reinterpret_cast<T*>(smem_raw);
+    T* sm = reinterpret_cast<T*>(smem_raw) + ((Tm.msz + 3) & ~3);
     T* Tg = p.slab + (int64_t)blockIdx.x * p.slab_per_cta;
 
     // ---- A: gather + B->G over positions 0..L-1
@@ -524,13 +650,13 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
       int nb_rest = Tm.NB / Tm.nb[0];
       T* cur = (L == 1) ? Tg : b0;
       gather_contract<T>(p.x + w.v0, p.ldx, p.map + Tm.off_nb, 0, cur, Tm.nb[0], Tm.nq[0], nb_rest, Vt,
-                         p.mats + Tm.m_d0b[0]);
+                         mb + Tm.m_d0b[0]);
       __syncthreads();
       int A = Tm.nq[0];
       for (int i = 1; i < L; ++i) {
         nb_rest /= Tm.nb[i];
         T* nxt = (i == L - 1) ? Tg : (cur == b0 ? b1 : b0);
-        contract<T>(cur, Vt, nxt, Vt, A, Tm.nb[i], Tm.nq[i], nb_rest, Vt, p.mats + Tm.m_d0b[i], T(1), false);
+        contract<T>(cur, Vt, nxt, Vt, A, Tm.nb[i], Tm.nq[i], nb_rest, Vt, mb + Tm.m_d0b[i], T(1), false);
         __syncthreads();
         cur = nxt;
         A *= Tm.nq[i];
@@ -545,8 +671,8 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
     T* Y = P + ss;
     for (int64_t i = threadIdx.x; i < tsz; i += blockDim.x) W[i] = T(0);
     const int ldx0 = (gL + 3) & ~3, ldo = (nL + 3) & ~3;
-    const T* X0 = p.mats + Tm.m_d0b[L];
-    const T* OUT = p.mats + Tm.m_bgw[L];
+    const T* X0 = mb + Tm.m_d0b[L];
+    const T* OUT = mb + Tm.m_bgw[L];
     const int nG = D * (D + 1) / 2;
     for (int q = 0; q < gL; ++q) {
       __syncthreads();
@@ -558,11 +684,11 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         int A = 1, Bq = NQs;
         for (int j = 0; j < L; ++j) {  // Y[j] = d1_j P
           Bq /= Tm.nq[j];
-          contract<T>(P, Vt, Y + j * ss, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, p.mats + Tm.m_d1[j], T(1), false);
+          contract<T>(P, Vt, Y + j * ss, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, mb + Tm.m_d1[j], T(1), false);
           A *= Tm.nq[j];
         }
         __syncthreads();
-        slab_extract<T>(Tg, ss, nL, p.mats + Tm.m_x1L + q, ldx0, P);  // P <- d_L psi on the slab
+        slab_extract<T>(Tg, ss, nL, mb + Tm.m_x1L + q, ldx0, P);  // P <- d_L psi on the slab
         __syncthreads();
         // Phi_i = sum_j G_ij(Q) y_j, in place (Y[i] for i < L, P for i = L)
         if (D <= 4) slab_pointwise_G<T, 4>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
@@ -574,11 +700,11 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         Bq = NQs;
         for (int i = 0; i < L; ++i) {  // Acc += -1/2 d1_i Phi_i
           Bq /= Tm.nq[i];
-          contract<T>(Y + i * ss, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, p.mats + Tm.m_d1[i], T(-0.5), true);
+          contract<T>(Y + i * ss, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d1[i], T(-0.5), true);
           __syncthreads();
           A *= Tm.nq[i];
         }
-        slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), p.mats + Tm.m_e1L + (int64_t)ldo * q, P,
+        slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), mb + Tm.m_e1L + (int64_t)ldo * q, P,
                            T(-0.5));
       } else {
         __syncthreads();
@@ -587,7 +713,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
           Bq /= Tm.nq[i];
           const T f = (T)(-0.5 * __ldg(p.G0 + Tm.perm[i] + D * Tm.perm[i]));
           if (f != T(0))
-            contract<T>(P, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, p.mats + Tm.m_d2[i], f, true);
+            contract<T>(P, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d2[i], f, true);
           __syncthreads();
           A *= Tm.nq[i];
         }
@@ -600,9 +726,9 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
               const int Bj = NQs / (Aj * Tm.nq[j]);
               const T f = (T)(-__ldg(p.G0 + Tm.perm[i] + D * Tm.perm[j]));
               if (f != T(0)) {
-                contract<T>(P, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, p.mats + Tm.m_d1[i], T(1), false);
+                contract<T>(P, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, mb + Tm.m_d1[i], T(1), false);
                 __syncthreads();
-                contract<T>(Y, Vt, Acc, Vt, Aj, Tm.nq[j], Tm.nq[j], Bj, Vt, p.mats + Tm.m_d1[j], f, true);
+                contract<T>(Y, Vt, Acc, Vt, Aj, Tm.nq[j], Tm.nq[j], Bj, Vt, mb + Tm.m_d1[j], f, true);
                 __syncthreads();
               }
               Aj *= Tm.nq[j];
@@ -611,7 +737,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
           }
         }
         const T fLL = (T)(-0.5 * __ldg(p.G0 + Tm.perm[L] + D * Tm.perm[L]));
-        slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), p.mats + Tm.m_e2L + (int64_t)ldo * q, P,
+        slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), mb + Tm.m_e2L + (int64_t)ldo * q, P,
                            fLL);
         if (p.has_offdiag) {  // F2_iL d1_i d_L: d_L through (bgw.d1)_L on the way back
           int Ai = 1;
@@ -620,9 +746,9 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
             const T f = (T)(-__ldg(p.G0 + Tm.perm[i] + D * Tm.perm[L]));
             if (f != T(0)) {
               __syncthreads();
-              contract<T>(P, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, p.mats + Tm.m_d1[i], T(1), false);
+              contract<T>(P, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, mb + Tm.m_d1[i], T(1), false);
               __syncthreads();
-              slab_accumulate<T>(W, ss, nL, p.mats + Tm.m_e1L + (int64_t)ldo * q, Y, f, nullptr, nullptr, T(0));
+              slab_accumulate<T>(W, ss, nL, mb + Tm.m_e1L + (int64_t)ldo * q, Y, f, nullptr, nullptr, T(0));
             }
             Ai *= Tm.nq[i];
           }
@@ -647,10 +773,10 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         Bq /= Tm.nq[i];
         const int Bt = Bq * nL;
         if (i == L - 1) {
-          contract<T>(cur, Vt, dst, p.ldh, A, Tm.nq[i], Tm.nb[i], Bt, Vt, p.mats + Tm.m_bgw[i], T(1), false);
+          contract<T>(cur, Vt, dst, p.ldh, A, Tm.nq[i], Tm.nb[i], Bt, Vt, mb + Tm.m_bgw[i], T(1), false);
         } else {
           T* nxt = (cur == b0) ? b1 : b0;
-          contract<T>(cur, Vt, nxt, Vt, A, Tm.nq[i], Tm.nb[i], Bt, Vt, p.mats + Tm.m_bgw[i], T(1), false);
+          contract<T>(cur, Vt, nxt, Vt, A, Tm.nq[i], Tm.nb[i], Bt, Vt, mb + Tm.m_bgw[i], T(1), false);
           cur = nxt;
         }
         __syncthreads();
@@ -890,10 +1016,10 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
     w.smem_slab_bytes = optin - 2048;                         // slab kernel: 1 CTA per SM
     w.grid = c->num_sms * 2;
     w.grid_slab = c->num_sms;
-    size_t slab = 0;
+    size_t slab = 0;  // general kernel: FP64 buffers of the terms that run from global memory
     for (const TermDesc& Tm : P.terms) {
       size_t fp1 = footprint_elems<double>(P, Tm, 1) * sizeof(double);
-      if (fp1 > (size_t)w.smem_bytes) slab = std::max(slab, fp1);
+      slab = std::max(slab, fp1);
     }
     w.slab_per_cta_bytes = slab;
     // the slab kernel keeps its partially transformed tensor (at most half of its shared
@@ -929,18 +1055,21 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
   for (int t = 0; t < (int)P.terms.size(); ++t) {
     const TermDesc& Tm = P.terms[t];
     if (Tm.weight == 0.0) continue;
-    if (slab_ok && slab_need_elems(P, Tm, 1) * esz <= (size_t)w.smem_slab_bytes) {
+    const size_t mats = (size_t)((Tm.msz + 3) & ~3) * esz;  // staged 1-D matrices
+    if (mats > (size_t)w.smem_bytes) return set_error(c, EVR_EINVAL, "1-D matrices exceed shared memory");
+    if (slab_ok && slab_need_elems(P, Tm, 1) * esz + mats <= (size_t)w.smem_slab_bytes) {
       int vt = 1;
-      while (vt * 2 <= nvec && vt * 2 <= 32 && slab_need_elems(P, Tm, vt * 2) * esz <= (size_t)w.smem_slab_bytes)
+      while (vt * 2 <= nvec && vt * 2 <= 32 &&
+             slab_need_elems(P, Tm, vt * 2) * esz + mats <= (size_t)w.smem_slab_bytes)
         vt *= 2;
       for (int v0 = 0; v0 < nvec; v0 += vt) sitems.push_back(WorkItem{t, v0, std::min(vt, nvec - v0), 1});
       continue;
     }
     int vt = 1;
     const size_t fp1 = footprint_elems<double>(P, Tm, 1) * esz;
-    const bool in_smem = fp1 <= (size_t)w.smem_bytes;
+    const bool in_smem = fp1 + mats <= (size_t)w.smem_bytes;
     if (in_smem)
-      while (vt * 2 <= nvec && vt * 2 <= 32 && fp1 * (size_t)(vt * 2) <= (size_t)w.smem_bytes) vt *= 2;
+      while (vt * 2 <= nvec && vt * 2 <= 32 && fp1 * (size_t)(vt * 2) + mats <= (size_t)w.smem_bytes) vt *= 2;
     for (int v0 = 0; v0 < nvec; v0 += vt) items.push_back(WorkItem{t, v0, std::min(vt, nvec - v0), in_smem ? 1 : 0});
   }
   auto by_cost = [&](const WorkItem& a, const WorkItem& b) {
