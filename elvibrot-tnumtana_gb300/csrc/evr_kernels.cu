@@ -50,6 +50,8 @@ struct ItemParams {
   int D, nb0, keo_type;
   int has_offdiag;         // type 1 with off-diagonal F2 terms
   int vtrans;              // 1: V_ab read as V_ba (transposed operator)
+  int implicit_nvec;       // > 0: items are implicit, item = term * implicit_nvec + vector, one
+                           // vector each, buffers in the global slab (items == nullptr)
 };
 
 constexpr int kSlabThreads = 512;
@@ -222,10 +224,12 @@ __device__ __forceinline__ void contract_m(const T* __restrict__ in, int64_t ldi
 template <typename T>
 __device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64_t ldo, int A, int K, int M, int B,
                                          int Vt, const T* mat, T alpha, bool acc) {
-  if constexpr (sizeof(T) == 4) {  // FP32: two columns per thread, matrix coefficients from L1
+  if constexpr (sizeof(T) == 4) {  // FP32: two columns per thread, matrix coefficients from shared memory
     if (M <= 4) contract_m<T, 4, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else if (M <= 8) contract_m<T, 8, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (M <= 12) contract_m<T, 12, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else if (M <= 16) contract_m<T, 16, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (M <= 20) contract_m<T, 20, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else contract_m<T, 24, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
   } else {  // FP64: matrix strip in registers (register budget MG*MAXK <= 24 doubles)
     if (K <= 4) contract_ms<T, 4, 4>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
@@ -273,7 +277,9 @@ __device__ __forceinline__ void gather_contract(const double* x, int64_t ldx, co
                                                 int K, int M, int B, int Vt, const T* mat) {
   if (M <= 4) gather_contract_m<T, 4>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
   else if (M <= 8) gather_contract_m<T, 8>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+  else if (M <= 12) gather_contract_m<T, 12>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
   else if (M <= 16) gather_contract_m<T, 16>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+  else if (M <= 20) gather_contract_m<T, 20>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
   else gather_contract_m<T, 24>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
 }
 
@@ -332,7 +338,15 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
     __syncthreads();
     const int it = s_item;
     if (it >= p.n_items) break;
-    const WorkItem w = p.items[it];
+    WorkItem w;
+    if (p.implicit_nvec > 0) {
+      w.term = it / p.implicit_nvec;
+      w.v0 = it - w.term * p.implicit_nvec;
+      w.vt = 1;
+      w.smem = 0;
+    } else {
+      w = p.items[it];
+    }
     {
       const int* src = reinterpret_cast<const int*>(p.terms + w.term);
       int* dst = reinterpret_cast<int*>(&s_term);
@@ -526,20 +540,31 @@ __device__ __forceinline__ void slab_extract(const T* __restrict__ Tg, int64_t s
 
 // W[a + ss*k] += c1*O[k]*A1[a] + c2*E[k]*A2[a]  for k < nL (A2 may be null): the slab's
 // image under G->B of the streamed position
-template <typename T>
-__device__ __forceinline__ void slab_accumulate(T* __restrict__ W, int64_t ss, int nL, const T* __restrict__ O,
-                                                const T* __restrict__ A1, T c1, const T* __restrict__ E,
-                                                const T* __restrict__ A2, T c2) {
-  for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) {
-    const T u = c1 * A1[a];
-    const T z = A2 ? c2 * A2[a] : T(0);
-    for (int k = 0; k < nL; ++k) {
-      T wv = W[a + ss * k];
-      wv = fma(O[k], u, wv);
-      if (A2) wv = fma(E[k], z, wv);
-      W[a + ss * k] = wv;
-    }
+template <typename T, int MAXL>
+__device__ __forceinline__ void slab_accumulate_m(T* __restrict__ W, int64_t ss, int nL, const T* __restrict__ O,
+                                                  const T* __restrict__ A1, T c1, const T* __restrict__ E,
+                                                  const T* __restrict__ A2, T c2) {
+  T o[MAXL], e[MAXL];  // the slab's column of both matrices, in registers
+#pragma unroll
+  for (int k = 0; k < MAXL; ++k) {
+    o[k] = k < nL ? c1 * O[k] : T(0);
+    e[k] = (A2 && k < nL) ? c2 * E[k] : T(0);
   }
+  for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) {
+    const T u = A1[a];
+    const T z = A2 ? A2[a] : T(0);
+#pragma unroll
+    for (int k = 0; k < MAXL; ++k)
+      if (k < nL) W[a + ss * k] = fma(e[k], z, fma(o[k], u, W[a + ss * k]));
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void slab_accumulate(T* W, int64_t ss, int nL, const T* O, const T* A1, T c1, const T* E,
+                                                const T* A2, T c2) {
+  if (nL <= 8) slab_accumulate_m<T, 8>(W, ss, nL, O, A1, c1, E, A2, c2);
+  else if (nL <= 16) slab_accumulate_m<T, 16>(W, ss, nL, O, A1, c1, E, A2, c2);
+  else slab_accumulate_m<T, 24>(W, ss, nL, O, A1, c1, E, A2, c2);
 }
 
 // Phi_i = sum_j G_ij(Q) y_j on one slab, in place: y_j = Y[j] (j < L) and P (j = L).
@@ -692,6 +717,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         __syncthreads();
         // Phi_i = sum_j G_ij(Q) y_j, in place (Y[i] for i < L, P for i = L)
         if (D <= 4) slab_pointwise_G<T, 4>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
+        else if (D <= 6) slab_pointwise_G<T, 6>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
         else if (D <= 8) slab_pointwise_G<T, 8>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
         else if (D <= 12) slab_pointwise_G<T, 12>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
         else slab_pointwise_G<T, 16>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
@@ -1119,6 +1145,7 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
   p.nb0 = P.nb0;
   p.keo_type = P.keo_type;
   p.vtrans = vtrans;
+  p.implicit_nvec = 0;
   p.has_offdiag = 0;
   if (P.keo_type == 1)
     for (int i = 0; i < P.D; ++i)
@@ -1214,6 +1241,72 @@ int transpose_from_interleaved(const double* in, int64_t ld_in, double* out, int
   dim3 blk(32, 8), grd((unsigned)((nvec + 31) / 32), (unsigned)((N + 31) / 32));
   transpose_kernel<<<grd, blk, 0, s>>>(in, ld_in, out, ld_out, N, nvec);
   return cudaGetLastError() == cudaSuccess ? EVR_OK : EVR_EDEVICE;
+}
+
+
+// H.psi (FP64, the reference's operator H) on interleaved device blocks with all scratch
+// memory supplied by the caller: [item counter (256 B)][term-basis output][per-CTA
+// buffers].  Allocates nothing; every term runs one vector per item from the global
+// buffers.  Returns EVR_EINVAL when the scratch is too small.
+int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, unsigned char* scratch,
+                 size_t scratch_bytes, cudaStream_t s) {
+  const HostProblem& P = c->hp;
+  const int grid = c->num_sms * 2;
+  size_t slab = 0, msz = 0;
+  for (const TermDesc& Tm : P.terms) {
+    slab = std::max(slab, footprint_elems<double>(P, Tm, 1));
+    msz = std::max(msz, (size_t)((Tm.msz + 3) & ~3));
+  }
+  const size_t ht_bytes = ((size_t)P.sum_nb * P.nb0 * nvec * sizeof(double) + 255) & ~(size_t)255;
+  const size_t slab_bytes = slab * sizeof(double);
+  const size_t need = 256 + ht_bytes + slab_bytes * grid;
+  if (need > scratch_bytes)
+    return set_error(c, EVR_EINVAL, "evr_hpsi_noalloc: problem needs " + std::to_string(need) +
+                                        " bytes of scratch, the static buffer holds " + std::to_string(scratch_bytes));
+  const size_t smem = msz * sizeof(double);
+  int optin = 0;
+  EVR_CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attr");
+  if (smem > (size_t)optin / 2) return set_error(c, EVR_EINVAL, "evr_hpsi_noalloc: 1-D matrices too large");
+  EVR_CU(cudaFuncSetAttribute(hpsi_items_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin / 2),
+         "attr");
+  int* counter = reinterpret_cast<int*>(scratch);
+  double* ht = reinterpret_cast<double*>(scratch + 256);
+  double* slabp = reinterpret_cast<double*>(scratch + 256 + ht_bytes);
+  ItemParams<double> p;
+  p.terms = c->dp.terms;
+  p.mats = c->dp.mats;
+  p.vgrid = c->dp.vgrid;
+  p.ggrid = c->dp_ggrid;
+  p.G0 = c->dp.G0;
+  p.map = c->dp.map;
+  p.items = nullptr;
+  p.n_items = (int)P.terms.size() * nvec;
+  p.counter = counter;
+  p.slab = slabp;
+  p.slab_per_cta = (int64_t)slab;
+  p.x = x;
+  p.ldx = ldx;
+  p.ht = ht;
+  p.ldh = nvec;
+  p.Np = P.Np;
+  p.D = P.D;
+  p.nb0 = P.nb0;
+  p.keo_type = P.keo_type;
+  p.vtrans = 0;
+  p.implicit_nvec = nvec;
+  p.has_offdiag = 0;
+  if (P.keo_type == 1)
+    for (int i = 0; i < P.D; ++i)
+      for (int j = i + 1; j < P.D; ++j) p.has_offdiag |= (P.G0[i + (size_t)P.D * j] != 0.0);
+  EVR_CU(cudaMemsetAsync(counter, 0, sizeof(int), s), "memset counter");  // the buffer keeps old contents
+  hpsi_items_kernel<double><<<grid, kThreads, optin / 2, s>>>(p);
+  EVR_CU(cudaGetLastError(), "hpsi_items_kernel launch");
+  const int64_t N = P.Np * P.nb0;
+  int rblocks = (int)std::min<int64_t>((N * nvec + 255) / 256, (int64_t)c->num_sms * 16);
+  csr_reduce_kernel<double><<<rblocks, 256, 0, s>>>(c->dp.csr_ptr, c->dp.csr_src, c->dp.csr_w, ht, nullptr, nvec,
+                                                     1.0, y, ldy, N, nvec);
+  EVR_CU(cudaGetLastError(), "csr_reduce_kernel launch");
+  return EVR_OK;
 }
 
 }  // namespace evr
