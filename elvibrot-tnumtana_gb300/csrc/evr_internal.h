@@ -188,6 +188,9 @@ constexpr int kMaxBlock = 64;
 int hpsi_interleaved(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, int prec,
                      cudaStream_t s, int op = OP_H);
 // any nvec: splits into blocks of kMaxBlock vectors
+// FP64 H.psi with caller-provided scratch (no allocation); see evr_hpsi_noalloc
+int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, unsigned char* scratch,
+                 size_t scratch_bytes, cudaStream_t s);
 int hpsi_blocks(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, int prec,
                 cudaStream_t s, int op = OP_H);
 int transpose_to_interleaved(const double* in, int64_t ld_in, double* out, int64_t ld_out, int64_t N, int nvec,

@@ -57,7 +57,7 @@ EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_
            "evr_last_launch_count",
            "evr_last_kernel_ms",
            "evr_davidson",
-           "evr_cheby_propagate", "evr_fma_peak"]
+           "evr_cheby_propagate", "evr_fma_peak", "evr_hpsi_noalloc"]
 
 _lib = None
 
@@ -92,6 +92,7 @@ def load(build: bool = True):
     L.evr_set_operator.argtypes = [vp, C.c_int]
     L.evr_set_kernel_path.argtypes = [vp, C.c_int]
     L.evr_fma_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
+    L.evr_hpsi_noalloc.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.c_int, vp]
     if hasattr(L, "evr_davidson"):
         L.evr_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _dp, _dp, _dp, _lp]
     if hasattr(L, "evr_cheby_propagate"):
@@ -234,6 +235,12 @@ class Problem:
         """H.psi on DEVICE pointers (e.g. torch tensor data_ptr()), stream-ordered."""
         self._check(load().evr_hpsi_device(self.h, C.c_void_p(psi_ptr), ld_psi, C.c_void_p(hpsi_ptr), ld_hpsi, nvec,
                                            layout, PREC[prec], C.c_void_p(stream) if stream else None))
+
+    def hpsi_noalloc(self, psi_ptr, ld_psi, hpsi_ptr, ld_hpsi, nvec, stream=None):
+        """FP64 H.psi on DEVICE pointers (interleaved) using only the library's fixed
+        scratch array: no device allocation (see evr_hpsi_noalloc in include/evr_gpu.h)."""
+        self._check(load().evr_hpsi_noalloc(self.h, C.c_void_p(psi_ptr), ld_psi, C.c_void_p(hpsi_ptr), ld_hpsi, nvec,
+                                            C.c_void_p(stream) if stream else None))
 
     def last_launch_count(self):
         k = C.c_int64()

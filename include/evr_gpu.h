@@ -139,6 +139,21 @@ int evr_set_operator(evr_ctx *ctx, int form);
  * 0 runs every term in the general kernel.  Both compute the same operator. */
 int evr_set_kernel_path(evr_ctx *ctx, int slab);
 
+/* H.psi that allocates nothing (no counterpart in the reference).
+ * For callers that cannot let the library allocate device memory on the H.psi path --
+ * a host that owns every device buffer through its own memory pool, or code that must
+ * not enter the CUDA allocator at that point -- this variant of evr_hpsi_device takes its
+ * scratch (item counter, term-basis output, per-CTA work buffers) from one file-scope
+ * device array of 32 MiB that every GPU loading the library holds until the process
+ * exits.  psi/hpsi: DEVICE pointers, interleaved layout (ld >= nvec), FP64, operator H.
+ * Problems whose scratch exceeds 32 MiB are rejected with EVR_EINVAL (message gives the
+ * size needed).  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.  All calls
+ * share the one array: calls that overlap on the GPU (other streams, other threads)
+ * race and must be serialised by the caller. */
+int evr_hpsi_noalloc(evr_ctx *ctx, const double *psi, int64_t ld_psi, double *hpsi, int64_t ld_hpsi, int nvec,
+                     void *stream);
+
 /* Launch statistics of the last evr_hpsi_* call (kernels launched, work items). */
 int evr_last_launch_count(const evr_ctx *ctx, int64_t *kernels, int64_t *items);
 /* Device time (ms) of the term-pipeline kernel and of the weighted reduction of the last
