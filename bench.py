@@ -10,8 +10,12 @@ seed (synthetic inputs with the benchmark's shapes and distributions).
   e2e    : FP64 H.psi/s through the host entry point evr_hpsi_host with pinned host
            buffers (copies in and out inside the timed region)
   mixed  : the FP32-contraction path on the same block, with its error against FP64
-  roofline: the term-pipeline kernel (hpsi_items_kernel) against the measured FP64 GEMM
-           rate of this GPU (cuBLAS DGEMM, measured in this run)
+  roofline: the term-pipeline kernels (slab + general) against the FP64 FMA rate of this
+           GPU measured in this run (evr_fma_peak: independent FMA chains; the FP64 work of
+           the contractions runs on the CUDA-core FMA pipe)
+  davidson: time to converge the lowest 50 levels (residual 1e-7 au) in FP64 and in the
+           mixed form (FP32 contractions, FP64 residuals / Gram-Schmidt / Rayleigh-Ritz,
+           FP64 refinement), with the largest eigenvalue difference in cm-1
   cpu_baseline / --impl reference: the CPU oracle (C++/OpenMP restatement of the
            reference's OpPsi) on the host cores, bounded to a sample of the block.
 
@@ -163,6 +167,30 @@ def run_profile(args):
     return 0
 
 
+# DRAM bytes (read + write) of one FP64 64-vector launch of the term kernels, from the ncu
+# capture summarised in profiles/ (None until measured)
+TRAFFIC_PER_LAUNCH = None
+DAV_LEVELS, DAV_BLOCK, DAV_RESI = 50, 64, 1e-7
+
+
+def davidson_legs(p, S):
+    """Lowest 50 levels in FP64 and in the mixed form, timed end to end (host call)."""
+    out = {"levels": DAV_LEVELS, "block": DAV_BLOCK, "conv_resi_au": DAV_RESI}
+    res = {}
+    for prec in ("fp64", "fp32"):
+        t0 = time.perf_counter()
+        e, _, st = p.davidson(DAV_LEVELS, block=DAV_BLOCK, max_it=400, conv_resi=DAV_RESI, conv_ene=1e-10,
+                              prec=prec)
+        res[prec] = (e, time.perf_counter() - t0, st)
+    e64, t64, s64 = res["fp64"]
+    e32, t32, s32 = res["fp32"]
+    out.update({"fp64_s": t64, "mixed_s": t32, "speedup": t64 / t32,
+                "max_abs_diff_cm": float(np.abs(e64 - e32).max() * S.AU_TO_CM),
+                "fp64": {k: v for k, v in s64.items()}, "mixed": {k: v for k, v in s32.items()},
+                "e0_cm": float(e64[0] * S.AU_TO_CM), "e49_cm": float(e64[-1] * S.AU_TO_CM)})
+    return out
+
+
 def measure_dgemm_tflops(torch, dtype, n=4096, reps=5):
     a = torch.randn(n, n, dtype=dtype, device="cuda")
     b = torch.randn(n, n, dtype=dtype, device="cuda")
@@ -187,6 +215,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-davidson", action="store_true", help="skip the Davidson time-to-tolerance legs")
     ap.add_argument("--profile", default=None, choices=["sg4_6d_l6", "sg4_6d_l8"],
                     help="profiling mode: a few H.psi launches of the named workload, nothing else")
     ap.add_argument("--prec", default="both", choices=["both", "fp64", "fp32"], help="precision(s) in profiling mode")
@@ -248,7 +277,9 @@ def main():
 
     with ClockSampler(local) as clk:
         t64, k64 = timed("fp64", y)
+        launches = p.last_launch_count()[0] * args.steps
         t32, k32 = timed("fp32", y32)
+        launches += p.last_launch_count()[0] * args.steps
     total64 = sum(t64)
     if world > 1:
         tt = torch.tensor([total64], device="cuda")
@@ -274,14 +305,19 @@ def main():
     e2e = NVEC * args.steps / sum(te)
     e2e_err = float((hy.t().cuda() - y).abs().max() / y.abs().max())
 
-    # roofline of the dominant kernel
+    # roofline of the dominant kernel: algorithmic FLOPs of one 64-vector launch over the
+    # measured FP64 FMA rate
     items_ms = statistics.mean(k[0] for k in k64)
     flop_launch = p.flop_per_hpsi * NVEC
     achieved = flop_launch / (items_ms / 1e3) / 1e12
-    peak64 = measure_dgemm_tflops(torch, torch.float64)
+    fma64 = E.fma_peak(local, "fp64")
+    fma32 = E.fma_peak(local, "fp32")
+    dgemm = measure_dgemm_tflops(torch, torch.float64)
     items32 = statistics.mean(k[0] for k in k32)
-    torch.backends.cuda.matmul.allow_tf32 = False
-    peak32 = measure_dgemm_tflops(torch, torch.float32)
+
+    dav = None
+    if not args.no_davidson:
+        dav = davidson_legs(p, S)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total64 / args.steps, "higher_is_better": True,
@@ -291,14 +327,16 @@ def main():
                     "d2h_bytes_per_step": int(N * NVEC * 8), "rel_err_vs_device": e2e_err},
             "mixed": {"value": mixed, "unit": UNIT, "dtype": "f32 contractions, f64 reduction",
                       "rel_err_vs_fp64": err32, "items_kernel_ms": items32,
-                      "achieved_tflops": flop_launch / (items32 / 1e3) / 1e12, "fp32_sgemm_tflops": peak32},
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-                         "frac": achieved / peak64, "traffic": None,
-                         "kernel": "hpsi_items_kernel<double>", "items_kernel_ms": items_ms,
-                         "algorithmic_flop_per_launch": flop_launch,
-                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (no FP64 figure in the "
-                                        "driver's peak file)"},
-            "gpu_launches": 2 * args.steps,
+                      "achieved_tflops": flop_launch / (items32 / 1e3) / 1e12, "fp32_fma_peak_tflops": fma32,
+                      "frac_of_fp32_fma": flop_launch / (items32 / 1e3) / 1e12 / fma32},
+            "roofline": {"bound": "fp64-fma", "achieved": achieved, "peak": fma64, "unit": "TFLOP/s",
+                         "frac": achieved / fma64, "traffic": TRAFFIC_PER_LAUNCH,
+                         "kernel": "hpsi_slab_kernel<double> + hpsi_items_kernel<double>", "items_kernel_ms": items_ms,
+                         "algorithmic_flop_per_launch": flop_launch, "dgemm_tflops": dgemm,
+                         "peak_source": "FP64 FMA issue rate measured in this run (evr_fma_peak); no FP64 figure "
+                                        "in the measured-peaks file"},
+            "davidson": dav,
+            "gpu_launches": launches,
             "clocks": clk.summary()}
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

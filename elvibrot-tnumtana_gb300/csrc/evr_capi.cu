@@ -51,6 +51,7 @@ int evr_destroy(evr_ctx* c) {
   if (c->host_only) { delete c; return EVR_OK; }
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  free_control(c);
   free_workspace(c);
   free_problem(c);
   if (c->pinned) cudaFreeHost(c->pinned);
@@ -123,11 +124,13 @@ int evr_get_vgrid(const evr_ctx* c0, double* v) {
   return EVR_OK;
 }
 
-int evr_set_kernel_path(evr_ctx* c, int slab) {
+int evr_set_kernel_path(evr_ctx* c, int path) {
   if (!c) return EVR_EINVAL;
-  if (slab != 0 && slab != 1) return set_error(c, EVR_EINVAL, "evr_set_kernel_path: 0 or 1");
-  if (c->use_slab != (slab == 1)) {
-    c->use_slab = slab == 1;
+  if (path < 0 || path > 2) return set_error(c, EVR_EINVAL, "evr_set_kernel_path: 0, 1 or 2");
+  const bool slab = path >= 1, stages = path == 1;
+  if (c->use_slab != slab || c->use_stages != stages) {
+    c->use_slab = slab;
+    c->use_stages = stages;
     if (!c->host_only) {
       cudaSetDevice(c->device);
       cudaStreamSynchronize(c->stream);

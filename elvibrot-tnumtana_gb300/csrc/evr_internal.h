@@ -153,6 +153,23 @@ struct Workspace {
 // operator forms
 enum OpForm { OP_H = 0, OP_HT = 1, OP_HSYM = 2 };
 
+// Grid operator of one H.psi call: potential vw*V(Q) + mw*mu(Q) (mu: the dipole table of
+// evr_set_dipole; mw = -E for a field E) and the kinetic part when keo != 0.  The default
+// is the plain H.  mu_dev, when set, is a device scalar read in place of mw (a field
+// value that changes between replays of a captured launch sequence).
+struct OpExtras {
+  double vw = 1.0, mw = 0.0;
+  int keo = 1;
+  const double* mu_dev = nullptr;
+};
+
+// Stage buffers of the grid-wide single-term path (evr_stages.cu).
+struct StageBuffers {
+  void* buf = nullptr;
+  size_t elems = 0;   // elements per buffer (FP64), Smax * nb0 * kMaxBlock
+  int64_t smax = 0;   // largest intermediate tensor of one vector and state
+};
+
 }  // namespace evr
 
 struct evr_ctx {
@@ -161,6 +178,7 @@ struct evr_ctx {
   int op_form = 0;                  // EVR_OP_H, EVR_OP_HT or EVR_OP_HSYM
   bool capturing = false;           // inside a stream capture: no event records
   bool use_slab = true;             // slab kernel for the terms that fit (EVR_NO_SLAB=1 disables)
+  bool use_stages = true;           // grid-wide stage path for single-term problems
   cudaStream_t stream = nullptr;
   evr::HostProblem hp;
   evr::DeviceProblem dp;
@@ -171,6 +189,12 @@ struct evr_ctx {
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // around the items kernel and the reduction
   double* dp_ggrid = nullptr;      // symmetric G(Q) on the grid (type 10 with g != 0)
   float* dp_ggrid32 = nullptr;
+  double* dp_mugrid = nullptr;     // dipole mu(Q) on the grid (sum_nq * nb0^2), evr_set_dipole
+  float* dp_mugrid32 = nullptr;
+  double mu_max = 0.0;             // max over grid points of the row-sum norm of mu
+  evr::StageBuffers stg;
+  evr::OpExtras field;             // grid-operator extras of evr_hpsi_* / Davidson / Chebyshev (evr_set_field)
+  void* oc = nullptr;              // optimal-control state (evr_control.cu)
   // host staging for the host-pointer entry points
   double* pinned = nullptr;
   size_t pinned_bytes = 0;
@@ -186,13 +210,29 @@ void free_workspace(evr_ctx* c);
 // nvec <= kMaxBlock per call; returns a status.
 constexpr int kMaxBlock = 64;
 int hpsi_interleaved(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, int prec,
-                     cudaStream_t s, int op = OP_H);
+                     cudaStream_t s, int op = OP_H, const OpExtras* ex = nullptr);
 // any nvec: splits into blocks of kMaxBlock vectors
 // FP64 H.psi with caller-provided scratch (no allocation); see evr_hpsi_noalloc
 int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, unsigned char* scratch,
                  size_t scratch_bytes, cudaStream_t s);
 int hpsi_blocks(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, int prec,
-                cudaStream_t s, int op = OP_H);
+                cudaStream_t s, int op = OP_H, const OpExtras* ex = nullptr);
+// grid-wide path for problems of one term (evr_stages.cu); nvec <= kMaxBlock
+bool stages_apply(const evr_ctx* c);
+int hpsi_stages(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, int prec,
+                cudaStream_t s, int op, const OpExtras& ex);
+void free_stages(evr_ctx* c);
+void free_control(evr_ctx* c);
+// weighted CSR reduction of the term-basis output(s) into y (evr_kernels.cu)
+int reduce_terms(evr_ctx* c, int prec, const void* ht, const void* ht2, int nvec, double scale, double* y,
+                 int64_t ldy, cudaStream_t s);
+// evaluates monomials (device arrays) on every term grid into out (sum_nq * nb0^2) and
+// returns the largest row-sum norm over the points in *maxnorm
+int eval_grid_monomials(evr_ctx* c, int n_mono, const double* coef, const int* idx, const int* elec, double* out,
+                        double* maxnorm);
+// Chebyshev series of exp(-i r x) on [-1, 1]: c_0 = J_0(r), c_k = 2 J_k(r), k <= K, with K the
+// first order after which every |c_k| < tol (evr_propagate.cu); returns false when too long
+bool cheby_series(double r, double tol, std::vector<double>& coef);
 int transpose_to_interleaved(const double* in, int64_t ld_in, double* out, int64_t ld_out, int64_t N, int nvec,
                              cudaStream_t s);
 int transpose_from_interleaved(const double* in, int64_t ld_in, double* out, int64_t ld_out, int64_t N, int nvec,

@@ -19,6 +19,7 @@
 // (M values) per thread and the 1-D matrix read through the read-only cache.
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include "evr_internal.h"
@@ -52,7 +53,23 @@ struct ItemParams {
   int vtrans;              // 1: V_ab read as V_ba (transposed operator)
   int implicit_nvec;       // > 0: items are implicit, item = term * implicit_nvec + vector, one
                            // vector each, buffers in the global slab (items == nullptr)
+  // grid operator extras: pot = vw*V + mw*mu when mugrid != nullptr (mw read from mu_dev
+  // when that is set); keo_on = 0 drops the kinetic part
+  const T* mugrid;
+  T vw, mw;
+  const double* mu_dev;
+  int keo_on;
 };
+
+// plain H: no dipole term, kinetic part on
+template <typename T>
+void set_plain(ItemParams<T>& p) {
+  p.mugrid = nullptr;
+  p.vw = T(1);
+  p.mw = T(0);
+  p.mu_dev = nullptr;
+  p.keo_on = 1;
+}
 
 constexpr int kSlabThreads = 512;
 
@@ -384,9 +401,11 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
       }
     }
 
-    // ---- V.psi: X1[a] = sum_b V_ab X0[b]
+    // ---- V.psi: X1[a] = sum_b V_ab X0[b]   (V -> vw V + mw mu with a dipole term)
     {
       const T* Vt_ = p.vgrid + Tm.off_nq * nb0 * nb0;
+      const T* Mu_ = p.mugrid ? p.mugrid + Tm.off_nq * nb0 * nb0 : nullptr;
+      const T mw = p.mu_dev ? (T)__ldg(p.mu_dev) : p.mw;
       const int64_t n = stride;
       for (int64_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
         const int q = (int)(idx / Vt);
@@ -394,7 +413,9 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
           T s = T(0);
           for (int b = 0; b < nb0; ++b) {
             const int ab = p.vtrans ? (b + nb0 * a) : (a + nb0 * b);
-            s = fma(__ldg(Vt_ + (int64_t)ab * NQ + q), X0[b * stride + idx], s);
+            T vab = __ldg(Vt_ + (int64_t)ab * NQ + q);
+            if (Mu_) vab = fma(mw, __ldg(Mu_ + (int64_t)ab * NQ + q), p.vw * vab);
+            s = fma(vab, X0[b * stride + idx], s);
           }
           X1[a * stride + idx] = s;
         }
@@ -403,7 +424,8 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
     }
 
     // ---- KEO
-    if (p.keo_type == 10) {
+    if (!p.keo_on) {
+    } else if (p.keo_type == 10) {
       for (int e = 0; e < nb0; ++e) {
         const T* P0 = X0 + e * stride;
         T* Acc = X1 + e * stride;
@@ -704,8 +726,18 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
       slab_extract<T>(Tg, ss, nL, X0 + q, ldx0, P);
       __syncthreads();
       const T* Vq = p.vgrid + Tm.off_nq + (int64_t)q * NQs;
-      for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) Acc[a] = __ldg(Vq + a / Vt) * P[a];
-      if (p.keo_type == 10) {
+      if (p.mugrid) {
+        const T* Mq = p.mugrid + Tm.off_nq + (int64_t)q * NQs;
+        const T mw = p.mu_dev ? (T)__ldg(p.mu_dev) : p.mw;
+        for (int64_t a = threadIdx.x; a < ss; a += blockDim.x)
+          Acc[a] = fma(mw, __ldg(Mq + a / Vt), p.vw * __ldg(Vq + a / Vt)) * P[a];
+      } else {
+        for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) Acc[a] = __ldg(Vq + a / Vt) * P[a];
+      }
+      if (!p.keo_on) {
+        __syncthreads();
+        slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), nullptr, nullptr, T(0));
+      } else if (p.keo_type == 10) {
         int A = 1, Bq = NQs;
         for (int j = 0; j < L; ++j) {  // Y[j] = d1_j P
           Bq /= Tm.nq[j];
@@ -997,12 +1029,15 @@ int upload_problem(evr_ctx* c) {
 void free_problem(evr_ctx* c) {
   DeviceProblem& d = c->dp;
   void* ptrs[] = {d.terms, d.termsT, d.mats, d.mats32, d.vgrid, d.vgrid32, d.map, d.csr_ptr, d.csr_src, d.csr_w,
-                  d.G0, d.g, d.mono_coef, d.mono_idx, d.mono_elec, d.e0diag, c->dp_ggrid, c->dp_ggrid32};
+                  d.G0, d.g, d.mono_coef, d.mono_idx, d.mono_elec, d.e0diag, c->dp_ggrid, c->dp_ggrid32,
+                  c->dp_mugrid, c->dp_mugrid32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   d = DeviceProblem();
   c->dp_ggrid = nullptr;
   c->dp_ggrid32 = nullptr;
+  c->dp_mugrid = nullptr;
+  c->dp_mugrid32 = nullptr;
 }
 
 void free_workspace(evr_ctx* c) {
@@ -1015,6 +1050,7 @@ void free_workspace(evr_ctx* c) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   w = Workspace();
+  free_stages(c);
 }
 
 // elements of shared memory the slab kernel needs for a term and a vector tile
@@ -1123,7 +1159,7 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
 
 template <typename T>
 static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, int vtrans, T* ht, const double* x,
-                        int64_t ldx, int nvec, cudaStream_t s) {
+                        int64_t ldx, int nvec, cudaStream_t s, const OpExtras& ex) {
   const HostProblem& P = c->hp;
   Workspace& w = c->ws;
   ItemParams<T> p;
@@ -1150,6 +1186,15 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
   if (P.keo_type == 1)
     for (int i = 0; i < P.D; ++i)
       for (int j = i + 1; j < P.D; ++j) p.has_offdiag |= (P.G0[i + (size_t)P.D * j] != 0.0);
+  set_plain(p);
+  p.keo_on = ex.keo;
+  if (ex.mw != 0.0 || ex.vw != 1.0 || ex.mu_dev) {
+    if (!c->dp_mugrid) return set_error(c, EVR_EINVAL, "field term without a dipole (evr_set_dipole)");
+    p.mugrid = f32 ? (const T*)c->dp_mugrid32 : (const T*)c->dp_mugrid;
+    p.vw = (T)ex.vw;
+    p.mw = (T)ex.mw;
+    p.mu_dev = ex.mu_dev;
+  }
   EVR_CU(cudaMemsetAsync(w.counter, 0, 2 * sizeof(int), s), "memset counter");
   if (set.n_slab > 0) {
     ItemParams<T> ps = p;
@@ -1172,7 +1217,7 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
 
 template <typename T>
 static int run_items(evr_ctx* c, const ItemSet& set, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec,
-                     cudaStream_t s, int op) {
+                     cudaStream_t s, int op, const OpExtras& ex) {
   const HostProblem& P = c->hp;
   Workspace& w = c->ws;
   if (op == OP_HSYM && !w.ht2) {
@@ -1183,9 +1228,10 @@ static int run_items(evr_ctx* c, const ItemSet& set, const double* x, int64_t ld
   int rc;
   if (!c->capturing) EVR_CU(cudaEventRecord(c->ev[0], s), "event");
   if (op == OP_H || op == OP_HSYM)
-    if ((rc = launch_items<T>(c, set, c->dp.terms, 0, (T*)w.ht, x, ldx, nvec, s))) return rc;
+    if ((rc = launch_items<T>(c, set, c->dp.terms, 0, (T*)w.ht, x, ldx, nvec, s, ex))) return rc;
   if (op == OP_HT || op == OP_HSYM)
-    if ((rc = launch_items<T>(c, set, c->dp.termsT, 1, (T*)(op == OP_HT ? w.ht : w.ht2), x, ldx, nvec, s))) return rc;
+    if ((rc = launch_items<T>(c, set, c->dp.termsT, 1, (T*)(op == OP_HT ? w.ht : w.ht2), x, ldx, nvec, s, ex)))
+      return rc;
   if (!c->capturing) EVR_CU(cudaEventRecord(c->ev[1], s), "event");
   const int64_t N = P.Np * P.nb0;
   int rblocks = (int)std::min<int64_t>((N * nvec + 255) / 256, (int64_t)c->num_sms * 16);
@@ -1201,24 +1247,26 @@ static int run_items(evr_ctx* c, const ItemSet& set, const double* x, int64_t ld
 }
 
 int hpsi_interleaved(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, int prec,
-                     cudaStream_t s, int op) {
+                     cudaStream_t s, int op, const OpExtras* ex) {
+  const OpExtras& e = ex ? *ex : c->field;
   int rc = ensure_workspace(c, nvec, prec);
   if (rc) return rc;
+  if (stages_apply(c)) return hpsi_stages(c, x, ldx, y, ldy, nvec, prec, s, op, e);
   const ItemSet* set = nullptr;
   for (const ItemSet& it : c->ws.sets)
     if (it.nvec == nvec && it.prec == prec) set = &it;
   if (!set) return set_error(c, EVR_EINVAL, "no work decomposition");
   const ItemSet cp = *set;
-  if (prec == EVR_PREC_FP32) return run_items<float>(c, cp, x, ldx, y, ldy, nvec, s, op);
-  return run_items<double>(c, cp, x, ldx, y, ldy, nvec, s, op);
+  if (prec == EVR_PREC_FP32) return run_items<float>(c, cp, x, ldx, y, ldy, nvec, s, op, e);
+  return run_items<double>(c, cp, x, ldx, y, ldy, nvec, s, op, e);
 }
 
 int hpsi_blocks(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, int prec, cudaStream_t s,
-                int op) {
+                int op, const OpExtras* ex) {
   int64_t k = 0, items = 0;
   for (int v0 = 0; v0 < nvec; v0 += kMaxBlock) {
     const int nb = std::min(kMaxBlock, nvec - v0);
-    int rc = hpsi_interleaved(c, x + v0, ldx, y + v0, ldy, nb, prec, s, op);
+    int rc = hpsi_interleaved(c, x + v0, ldx, y + v0, ldy, nb, prec, s, op, ex);
     if (rc) return rc;
     k += c->last_kernels;
     items += c->last_items;
@@ -1243,6 +1291,61 @@ int transpose_from_interleaved(const double* in, int64_t ld_in, double* out, int
   return cudaGetLastError() == cudaSuccess ? EVR_OK : EVR_EDEVICE;
 }
 
+int reduce_terms(evr_ctx* c, int prec, const void* ht, const void* ht2, int nvec, double scale, double* y,
+                 int64_t ldy, cudaStream_t s) {
+  const int64_t N = c->hp.Np * c->hp.nb0;
+  const int rblocks = (int)std::min<int64_t>((N * nvec + 255) / 256, (int64_t)c->num_sms * 16);
+  if (prec == EVR_PREC_FP32)
+    csr_reduce_kernel<float><<<rblocks, 256, 0, s>>>(c->dp.csr_ptr, c->dp.csr_src, c->dp.csr_w, (const float*)ht,
+                                                      (const float*)ht2, nvec, scale, y, ldy, N, nvec);
+  else
+    csr_reduce_kernel<double><<<rblocks, 256, 0, s>>>(c->dp.csr_ptr, c->dp.csr_src, c->dp.csr_w, (const double*)ht,
+                                                       (const double*)ht2, nvec, scale, y, ldy, N, nvec);
+  return cuda_check(c, cudaGetLastError(), "csr_reduce_kernel launch");
+}
+
+namespace {
+// largest row-sum norm sum_b |m_ab(q)| over the grid points (non-negative doubles order
+// like their bit patterns, so the maximum is an integer atomicMax)
+__global__ void rownorm_max_kernel(const double* __restrict__ m, int64_t n, int nb0, unsigned long long* out) {
+  double best = 0.0;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    for (int a = 0; a < nb0; ++a) {
+      double r = 0.0;
+      for (int b = 0; b < nb0; ++b) r += fabs(m[(int64_t)(a + nb0 * b) * n + q]);
+      best = fmax(best, r);
+    }
+  atomicMax(out, (unsigned long long)__double_as_longlong(best));
+}
+}  // namespace
+
+int eval_grid_monomials(evr_ctx* c, int n_mono, const double* coef, const int* idx, const int* elec, double* out,
+                        double* maxnorm) {
+  const HostProblem& P = c->hp;
+  grid_eval_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(c->dp.terms, (int)P.terms.size(), c->dp.mats, P.sum_nq,
+                                                          P.D, P.nb0, n_mono, coef, idx, elec, c->dp.G0, c->dp.g,
+                                                          out, nullptr);
+  EVR_CU(cudaGetLastError(), "grid_eval_kernel");
+  if (maxnorm) {
+    unsigned long long* d = nullptr;
+    EVR_CU(cudaMalloc((void**)&d, sizeof(unsigned long long)), "cudaMalloc");
+    cudaMemsetAsync(d, 0, sizeof(unsigned long long), c->stream);
+    // the V table of term t starts at off_nq*nb0^2, with (a,b) blocks of NQ_t points; the
+    // norm scan runs per term
+    for (const TermDesc& Tm : P.terms)
+      rownorm_max_kernel<<<std::max(1, std::min(c->num_sms * 4, (Tm.NQ + 255) / 256)), 256, 0, c->stream>>>(
+          out + Tm.off_nq * P.nb0 * P.nb0, Tm.NQ, P.nb0, d);
+    unsigned long long h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    EVR_CU(e, "dipole norm");
+    double v;
+    memcpy(&v, &h, sizeof(v));
+    *maxnorm = v;
+  }
+  return EVR_OK;
+}
 
 // H.psi (FP64, the reference's operator H) on interleaved device blocks with all scratch
 // memory supplied by the caller: [item counter (256 B)][term-basis output][per-CTA
@@ -1293,6 +1396,7 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
   p.nb0 = P.nb0;
   p.keo_type = P.keo_type;
   p.vtrans = 0;
+  set_plain(p);
   p.implicit_nvec = nvec;
   p.has_offdiag = 0;
   if (P.keo_type == 1)

@@ -134,6 +134,26 @@ __global__ void cheby_overlap(const double* __restrict__ psi0, const double* __r
 
 }  // namespace
 
+namespace evr {
+bool cheby_series(double r, double tol, std::vector<double>& coef) {
+  int K = std::max(2, (int)std::ceil(r) + 8);
+  std::vector<double> J;
+  while (true) {
+    J = bessel_j(K + 20, r);
+    int last = 0;
+    for (int k = 0; k <= K + 20; ++k)
+      if ((k == 0 ? 1.0 : 2.0) * std::fabs(J[k]) >= tol) last = k;
+    if (last + 1 < K) { K = std::max(2, last + 1); break; }
+    K = 2 * K;
+    if (K > 200000) return false;
+  }
+  J = bessel_j(K, r);
+  coef.assign(K + 1, 0.0);
+  for (int k = 0; k <= K; ++k) coef[k] = (k == 0 ? 1.0 : 2.0) * J[k];
+  return true;
+}
+}  // namespace evr
+
 extern "C" int evr_cheby_propagate(evr_ctx* c, const double* psi0, int npsi, double dt, int nsteps, double emin,
                                    double emax, double poly_tol, int prec, double* autocorr, double* psi_out,
                                    int64_t* info) {
@@ -147,20 +167,10 @@ extern "C" int evr_cheby_propagate(evr_ctx* c, const double* psi0, int npsi, dou
   const int ncol = 2 * npsi;
   const double E0 = 0.5 * (emin + emax), Esc = 0.5 * (emax - emin), r = Esc * dt;
   // series length from the Bessel coefficients
-  int K = std::max(2, (int)std::ceil(r) + 8);
-  std::vector<double> J;
-  while (true) {
-    J = bessel_j(K + 20, r);
-    int last = 0;
-    for (int k = 0; k <= K + 20; ++k)
-      if ((k == 0 ? 1.0 : 2.0) * std::fabs(J[k]) >= poly_tol) last = k;
-    if (last + 1 < K) { K = std::max(2, last + 1); break; }
-    K = 2 * K;
-    if (K > 200000) return set_error(c, EVR_EINVAL, "evr_cheby_propagate: series too long (dt*dE too large)");
-  }
-  J = bessel_j(K, r);
-  std::vector<double> coef(K + 1);
-  for (int k = 0; k <= K; ++k) coef[k] = (k == 0 ? 1.0 : 2.0) * J[k];
+  std::vector<double> coef;
+  if (!cheby_series(r, poly_tol, coef))
+    return set_error(c, EVR_EINVAL, "evr_cheby_propagate: series too long (dt*dE too large)");
+  const int K = (int)coef.size() - 1;
 
   cudaStream_t s = c->stream;
   DevBuf d0, dpsi, dH, b0, b1, b2, dacc, dac;

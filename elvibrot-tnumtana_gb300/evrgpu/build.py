@@ -15,7 +15,7 @@ CSRC = os.path.join(PKG_ROOT, "csrc")
 BUILD = os.path.join(PKG_ROOT, "_build")
 LIB = os.path.join(BUILD, "libevrgpu.so")
 SOURCES = ["evr_setup.cpp", "evr_kernels.cu", "evr_capi.cu", "evr_davidson.cu", "evr_propagate.cu", "evr_peaks.cu",
-           "evr_noalloc.cu"]
+           "evr_noalloc.cu", "evr_stages.cu", "evr_control.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

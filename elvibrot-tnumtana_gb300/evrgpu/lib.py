@@ -52,12 +52,18 @@ class DavidsonOpts(C.Structure):
                 ("sym", C.c_int)]
 
 
+class OcOpts(C.Structure):
+    _fields_ = [("nsteps", C.c_int), ("dt", C.c_double), ("emin", C.c_double), ("emax", C.c_double),
+                ("poly_tol", C.c_double), ("checkpoint", C.c_int), ("prec", C.c_int)]
+
+
 EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_tables", "evr_get_basis",
            "evr_get_vgrid", "evr_hpsi_host", "evr_hpsi_device", "evr_set_operator", "evr_set_kernel_path",
            "evr_last_launch_count",
            "evr_last_kernel_ms",
            "evr_davidson",
-           "evr_cheby_propagate", "evr_fma_peak", "evr_hpsi_noalloc"]
+           "evr_cheby_propagate", "evr_fma_peak", "evr_hpsi_noalloc", "evr_set_dipole", "evr_set_field",
+           "evr_oc_forward", "evr_oc_backward"]
 
 _lib = None
 
@@ -93,6 +99,10 @@ def load(build: bool = True):
     L.evr_set_kernel_path.argtypes = [vp, C.c_int]
     L.evr_fma_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.evr_hpsi_noalloc.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.c_int, vp]
+    L.evr_set_dipole.argtypes = [vp, C.c_int, _dp, _ip, _ip]
+    L.evr_set_field.argtypes = [vp, C.c_double, C.c_double, C.c_int]
+    L.evr_oc_forward.argtypes = [vp, C.POINTER(OcOpts), _dp, _dp, _dp, _dp, _dp, _lp]
+    L.evr_oc_backward.argtypes = [vp, _dp, _dp, _lp]
     if hasattr(L, "evr_davidson"):
         L.evr_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _dp, _dp, _dp, _lp]
     if hasattr(L, "evr_cheby_propagate"):
@@ -170,6 +180,8 @@ class Problem:
         self.sum_nb, self.sum_nq, self.max_nq = s.sum_nb, s.sum_nq, s.max_nq_term
         self.flop_per_hpsi = s.flop_per_hpsi
         self.device = device
+        if getattr(spec, "dip_coef", None) is not None and device >= 0:
+            self.set_dipole(spec.dip_coef, spec.dip_idx, spec.dip_elec)
 
     def close(self):
         if getattr(self, "h", None):
@@ -279,9 +291,51 @@ class Problem:
             self._check(rc)
         return eig, vec, stats
 
-    def set_kernel_path(self, slab: bool):
-        """True: slab-streaming kernel for the terms that fit (default); False: general kernel."""
-        self._check(load().evr_set_kernel_path(self.h, 1 if slab else 0))
+    # ---- field coupling and optimal control ---------------------------------------
+    def set_dipole(self, coef, idx, elec=None):
+        """Dipole mu(Q) from monomials (coef[m], idx[m, 0:4] with -1 unused, elec[m] = (a, b))."""
+        coef = _darr(coef)
+        idx = _iarr(np.asarray(idx).reshape(-1, 4))
+        elec = _iarr(np.zeros((len(coef), 2)) if elec is None else np.asarray(elec).reshape(-1, 2))
+        self._check(load().evr_set_dipole(self.h, len(coef), _p(coef, _dp), _p(idx, _ip), _p(elec, _ip)))
+
+    def set_field(self, vw=1.0, mw=0.0, keo=True):
+        """Grid operator vw*V + mw*mu (+ kinetic part) of later H.psi / Davidson / Chebyshev calls."""
+        self._check(load().evr_set_field(self.h, float(vw), float(mw), 1 if keo else 0))
+
+    def oc_forward(self, field, psi0, target, dt, emin, emax, poly_tol=1e-14, checkpoint=0, prec="fp64",
+                   want_psi=False):
+        """J = |<target|psi(T)>|^2 under H0 - E_n mu; returns (J, overlap, psiT or None, info)."""
+        field = _darr(field)
+        o = OcOpts()
+        o.nsteps, o.dt, o.emin, o.emax = len(field), dt, emin, emax
+        o.poly_tol, o.checkpoint, o.prec = poly_tol, checkpoint, PREC[prec]
+        p0 = _darr(np.stack([np.real(psi0), np.imag(psi0)], axis=1))
+        tg = _darr(np.stack([np.real(target), np.imag(target)], axis=1))
+        out3 = np.zeros(3)
+        psiT = np.zeros((self.N, 2)) if want_psi else None
+        info = np.zeros(3, dtype=np.int64)
+        self._check(load().evr_oc_forward(self.h, C.byref(o), _p(field, _dp), _p(p0, _dp), _p(tg, _dp),
+                                          _p(out3, _dp), _p(psiT, _dp), _p(info, _lp)))
+        psi = psiT[:, 0] + 1j * psiT[:, 1] if want_psi else None
+        return out3[0], complex(out3[1], out3[2]), psi, dict(order=int(info[0]), columns=int(info[1]),
+                                                              checkpoints=int(info[2]))
+
+    def oc_backward(self, nsteps, want_ref=True):
+        """dJ/dE_n of the last oc_forward, and the continuous-time gradient at t_n = n dt."""
+        grad = np.zeros(nsteps)
+        ref = np.zeros(nsteps + 1) if want_ref else None
+        info = np.zeros(3, dtype=np.int64)
+        self._check(load().evr_oc_backward(self.h, _p(grad, _dp), _p(ref, _dp), _p(info, _lp)))
+        return grad, ref, dict(columns=int(info[0]), checkpoints=int(info[1]), segment=int(info[2]))
+
+    def set_kernel_path(self, path):
+        """1 or True (default): stage kernels for single-term problems, else the slab kernel
+        for the terms that fit and the general kernel for the rest; 2: the same without the
+        stage kernels; 0 or False: general kernel only.  Names "auto", "slab", "general" work too."""
+        names = {"auto": 1, "stages": 1, "slab": 2, "general": 0}
+        v = names[path] if isinstance(path, str) else (1 if path is True else 0 if path is False else int(path))
+        self._check(load().evr_set_kernel_path(self.h, v))
 
     def set_operator(self, form):
         """'H' (the reference's OpPsi), 'HT' (its transpose) or 'HSYM' ((H+H^T)/2)."""

@@ -72,6 +72,9 @@ class ProblemSpec:
     keo_type: int = 10
     G0: np.ndarray = None          # (D,D)
     g: np.ndarray = None           # (D,D,D), g[i,j,k] multiplies Q_k
+    dip_coef: np.ndarray = None    # optional dipole mu(Q), monomials like the potential
+    dip_idx: np.ndarray = None
+    dip_elec: np.ndarray = None
     name: str = ""
     extra: dict = field(default_factory=dict)
 
@@ -87,6 +90,8 @@ class ProblemSpec:
             self.g = np.zeros((D, D, D))
         if self.mono_elec is None and self.mono_coef is not None:
             self.mono_elec = np.zeros((len(self.mono_coef), 2), dtype=np.int32)
+        if self.dip_elec is None and self.dip_coef is not None:
+            self.dip_elec = np.zeros((len(self.dip_coef), 2), dtype=np.int32)
         for k in ("Aq", "Bq", "Ab", "Bb", "nq_dp", "nb_dp"):
             v = getattr(self, k)
             if v is not None:
@@ -232,6 +237,43 @@ def config_sg4_12d_l6(seed: int = 3) -> ProblemSpec:
     cubic couplings only between modes within a window of three neighbours, G = 1."""
     return config_sg4(12, 6, seed, wlo=0.002, whi=0.02, nq_A=1, cubic_sigma=5e-6, quartic_sigma=0.0,
                       g_amp=0.0, cubic_window=2)
+
+
+def dipole_poly(D, omega, rng, mu0=0.1, a_sigma=0.1, b_sigma=0.01):
+    """mu = mu0 + sum_i a_i q_i + sum_{i<=j} b_ij q_i q_j, a ~ N(0, a_sigma), b ~ N(0, b_sigma),
+    on the dimensionless q = sqrt(w) Q of ``anharmonic_poly``."""
+    s = np.sqrt(np.asarray(omega, dtype=np.float64))
+    p = Poly()
+    p.add(mu0, [])
+    for i in range(D):
+        p.add(rng.normal(0.0, a_sigma) * s[i], [i])
+    for (i, j) in combinations_with_replacement(range(D), 2):
+        p.add(rng.normal(0.0, b_sigma) * s[i] * s[j], [i, j])
+    return p.arrays()
+
+
+def config_oc(seed: int = 0, nb: int = 20, nq: int = 24, D: int = 3, omega=(0.010, 0.0092, 0.0035)) -> ProblemSpec:
+    """The optimal-control system: the direct-product system of ``config_dp3`` (D=3, nb=20,
+    nq=24) with a dipole mu(Q) = mu0 + sum a_i q_i + sum b_ij q_i q_j, a ~ N(0, 0.1),
+    b ~ N(0, 0.01).  Smaller nb/nq/D give the test-size versions."""
+    omega = np.asarray(omega[:D], dtype=np.float64)
+    rng = np.random.default_rng(seed)
+    c, idx, el, g = anharmonic_poly(D, omega, rng, 1e-5, 1e-6, 0.01)
+    dc, di, de = dipole_poly(D, omega, rng)
+    return ProblemSpec(kind="dp", D=D, nq_dp=[nq] * D, nb_dp=[nb] * D, scaleQ=np.sqrt(omega),
+                       mono_coef=c, mono_idx=idx, mono_elec=el, keo_type=10, g=g, dip_coef=dc, dip_idx=di,
+                       dip_elec=de, name=f"OC_DP{D}_nb{nb}_nq{nq}", extra=dict(omega=omega))
+
+
+def oc_field(nsteps: int = 4000, dt: float = 5.0, seed: int = 0, n_sin: int = 8, amp: float = 0.005,
+             wlo: float = 0.002, whi: float = 0.03) -> np.ndarray:
+    """Control field E_n = sum_k amp sin(w_k t_n + phi_k) at the step midpoints
+    t_n = (n + 1/2) dt, w_k ~ U(wlo, whi), phi_k ~ U(0, 2 pi)."""
+    rng = np.random.default_rng(seed)
+    w = rng.uniform(wlo, whi, size=n_sin)
+    ph = rng.uniform(0.0, 2.0 * np.pi, size=n_sin)
+    t = (np.arange(nsteps) + 0.5) * dt
+    return (amp * np.sin(np.outer(t, w) + ph[None, :])).sum(axis=1)
 
 
 def batched_systems(n: int = 256, seed: int = 2):

@@ -134,10 +134,12 @@ int evr_hpsi_device(evr_ctx *ctx, const double *psi, int64_t ld_psi, double *hps
 #define EVR_OP_HSYM 2
 int evr_set_operator(evr_ctx *ctx, int form);
 
-/* Kernel path of evr_hpsi_*: 1 (default) runs every term whose slab pipeline fits one
- * CTA's shared memory in the slab-streaming kernel and the rest in the general kernel;
- * 0 runs every term in the general kernel.  Both compute the same operator. */
-int evr_set_kernel_path(evr_ctx *ctx, int slab);
+/* Kernel path of evr_hpsi_*: 1 (default) runs a problem of a single term (a direct
+ * product basis) on the grid-wide stage kernels, and otherwise every term whose slab
+ * pipeline fits one CTA's shared memory in the slab-streaming kernel and the rest in the
+ * general kernel; 2 is path 1 without the stage kernels; 0 runs every term in the general
+ * kernel.  All compute the same operator. */
+int evr_set_kernel_path(evr_ctx *ctx, int path);
 
 /* H.psi that allocates nothing (no counterpart in the reference).
  * For callers that cannot let the library allocate device memory on the H.psi path --
@@ -205,6 +207,52 @@ int evr_cheby_propagate(evr_ctx *ctx, const double *psi0, int npsi, double dt, i
  * traffic): the peak of the CUDA-core pipe the contractions run on, in TFLOP/s.
  * Utility for roofline reporting; no counterpart in the reference. */
 int evr_fma_peak(int device, int prec, double *tflops);
+
+/*
+ * Field coupling H(t) = H0 - E(t) mu (one polarisation).
+ * evr_set_dipole: the dipole operator mu(Q), given like the potential (n_mono monomials
+ * coef * Q_i Q_j Q_k Q_l, idx[4m..4m+3] 0-based modes or -1, on the electronic block
+ * (elec[2m], elec[2m+1])), evaluated on every grid like V.  Replaces the dipole
+ * operators para_Dip(3) of sub_Opt_control (Source_ElVibRot/sub_propagation/sub_control.f90:290).
+ * evr_set_field: the grid operator of later evr_hpsi_*, evr_davidson and
+ * evr_cheby_propagate calls becomes vw*V + mw*mu, with the kinetic part when keo != 0
+ * (H0 - E mu: vw = 1, mw = -E, keo = 1; mu alone: vw = 0, mw = 1, keo = 0;
+ * (1, 0, 1) restores H0).  fcn_field's dWP = -i (H - E(t) Dip) WP
+ * (sub_module_propa_march.f90:1494-1503) with a static field.
+ */
+int evr_set_dipole(evr_ctx *ctx, int n_mono, const double *coef, const int *idx, const int *elec);
+int evr_set_field(evr_ctx *ctx, double vw, double mw, int keo);
+
+/*
+ * Optimal control: objective J = |<target|psi(T)>|^2 (calc_fidelity,
+ * sub_control.f90:1007-1050) under H(t) = H0 - E_n mu on step n (piecewise-constant field,
+ * field[n] for t in [n dt, (n+1) dt)); each step is the Chebyshev expansion of
+ * exp(-i (H0 - E_n mu) dt) on [emin - max|E| max|mu|, emax + max|E| max|mu|].
+ * evr_oc_forward propagates psi0 (HOST, N complex as re/im pairs), returns
+ * out3 = {J, Re c, Im c}, c = <target|psi(T)>, psi(T) in psiT (HOST, optional), and keeps
+ * the state every `checkpoint` steps on the device (0: ceil(sqrt(nsteps))).
+ * info: [Chebyshev order, H.psi columns applied, checkpoints kept].
+ * evr_oc_backward returns dJ/dE_n (grad, nsteps values) for the field and states of the
+ * last evr_oc_forward: the exact gradient of the discrete propagator, from the target
+ * propagated backwards through the adjoint of every step's Chebyshev recurrence (the
+ * transposed H, so also for the non-symmetric type-10 operator), the states recomputed
+ * segment by segment from the checkpoints.  ref (HOST, nsteps+1 values, optional): the
+ * continuous-time field gradient of build_field (sub_control.f90:955-975),
+ * -2 Im(<psi(t_n)|chi(t_n)><chi(t_n)|mu|psi(t_n)>) at t_n = n dt, where the reference's
+ * field update is E_new = ref / (2 alpha).  info: [H.psi columns applied, checkpoints,
+ * steps per segment].  The reference has no discrete adjoint and no checkpointing.
+ */
+typedef struct {
+  int nsteps;          /* steps of the control interval                              */
+  double dt;           /* time step (au)                                             */
+  double emin, emax;   /* spectral bounds of H0 (au)                                 */
+  double poly_tol;     /* Chebyshev truncation, e.g. 1e-14                           */
+  int checkpoint;      /* steps between stored states, 0 = ceil(sqrt(nsteps))        */
+  int prec;            /* EVR_PREC_FP64 (EVR_PREC_FP32: FP32 contractions)           */
+} evr_oc_opts;
+int evr_oc_forward(evr_ctx *ctx, const evr_oc_opts *opts, const double *field, const double *psi0,
+                   const double *target, double *out3, double *psiT, int64_t *info);
+int evr_oc_backward(evr_ctx *ctx, double *grad, double *ref, int64_t *info);
 
 #ifdef __cplusplus
 }

@@ -272,6 +272,12 @@ struct Problem {
   std::vector<double> G0, g;               // D*D, D*D*D
   std::vector<double> vgrid;               // sum_nq * nb0 * nb0
   bool vgrid_done = false;
+  // field coupling (fcn_field, sub_module_propa_march.f90:1494-1503: (H - E Dip) WP):
+  // grid operator vw*V + mw*mu, kinetic part when keo != 0
+  std::vector<Monomial> dip;
+  std::vector<double> mugrid;
+  double vw = 1.0, mw = 0.0;
+  int keo = 1;
 };
 
 // Get_n_FROM_Basis_L_TO_n, L_TO_n_type 0, expo 1 (sub_module_Basis_LTO_n.f90:443-447)
@@ -427,23 +433,30 @@ static void term_point_Q(const Problem* P, int t, long long iq, double* Q) {
   }
 }
 
-static void fill_vgrid(Problem* P) {
+static void fill_grid(Problem* P, const std::vector<Monomial>& mono, std::vector<double>& grid) {
   int nterm = (int)P->weight.size(), D = P->D, nb0 = P->nb0;
-  P->vgrid.assign((size_t)P->sum_nq * nb0 * nb0, 0.0);
+  grid.assign((size_t)P->sum_nq * nb0 * nb0, 0.0);
 #pragma omp parallel for schedule(dynamic)
   for (int t = 0; t < nterm; ++t) {
     std::vector<double> Q(D);
     long long NQ = P->nq_t[t];
-    double* Vt = &P->vgrid[(size_t)P->off_nq[t] * nb0 * nb0];
+    double* Vt = &grid[(size_t)P->off_nq[t] * nb0 * nb0];
     for (long long iq = 0; iq < NQ; ++iq) {
       term_point_Q(P, t, iq, Q.data());
-      for (const Monomial& m : P->mono) {
+      for (const Monomial& m : mono) {
         double v = m.coef;
         for (int k = 0; k < 4; ++k) if (m.idx[k] >= 0) v *= Q[m.idx[k]];
         Vt[iq + NQ * (m.ib0 + (long long)nb0 * m.jb0)] += v;
       }
     }
   }
+}
+
+// grid operator tables: V, and the dipole when the field term is on
+static void fill_vgrid(Problem* P) {
+  fill_grid(P, P->mono, P->vgrid);
+  if (!P->dip.empty()) fill_grid(P, P->dip, P->mugrid);
+  else P->mugrid.clear();
   P->vgrid_done = true;
 }
 
@@ -530,8 +543,20 @@ static void term_oppsi(const Problem* P, int t, std::vector<double>& psi_t) {
     bdp_to_gdp(P, t, G[a]);
   }
   const double* V = &P->vgrid[(size_t)P->off_nq[t] * nb0 * nb0];
+  std::vector<double> Vf;  // vw*V + mw*mu with a field term
+  if (P->vw != 1.0 || P->mw != 0.0) {
+    const size_t n = (size_t)NQ * nb0 * nb0;
+    Vf.assign(V, V + n);
+    const double* M = P->mugrid.empty() ? nullptr : &P->mugrid[(size_t)P->off_nq[t] * nb0 * nb0];
+    for (size_t i = 0; i < n; ++i) Vf[i] = P->vw * Vf[i] + (M ? P->mw * M[i] : 0.0);
+    V = Vf.data();
+  }
   std::vector<std::vector<double>> H(nb0, std::vector<double>(NQ, 0.0));
-  if (P->keo_type == 10) {
+  if (!P->keo) {
+    for (int a = 0; a < nb0; ++a)
+      for (int b = 0; b < nb0; ++b)
+        for (long long iq = 0; iq < NQ; ++iq) H[a][iq] += V[iq + NQ * (a + (long long)nb0 * b)] * G[b][iq];
+  } else if (P->keo_type == 10) {
     std::vector<double> Q(D);
     std::vector<double> PsiRj((size_t)NQ * D), PsiRi(NQ), OpPsiR(NQ);
     std::vector<double> Gq((size_t)NQ * D * D);
@@ -664,6 +689,29 @@ int or_set_keo(void* h, int type, const double* G0, const double* g) {
   int D = P->D;
   if (G0) P->G0.assign(G0, G0 + (size_t)D * D);
   if (g) P->g.assign(g, g + (size_t)D * D * D); else P->g.assign((size_t)D * D * D, 0.0);
+  return 0;
+}
+
+// Dipole operator mu(Q) (the para_Dip of sub_Opt_control, sub_control.f90:290), monomials
+// like the potential, and the field term of later or_hpsi calls: vw*V + mw*mu, kinetic
+// part when keo != 0 (H - E mu: vw = 1, mw = -E, keo = 1).
+int or_set_dipole(void* h, int n_mono, const double* coef, const int* idx, const int* elec) {
+  Problem* P = (Problem*)h;
+  P->dip.resize(n_mono);
+  for (int m = 0; m < n_mono; ++m) {
+    P->dip[m].coef = coef[m];
+    for (int k = 0; k < 4; ++k) P->dip[m].idx[k] = idx[4 * m + k];
+    P->dip[m].ib0 = elec ? elec[2 * m] : 0; P->dip[m].jb0 = elec ? elec[2 * m + 1] : 0;
+    for (int k = 0; k < 4; ++k) if (P->dip[m].idx[k] >= P->D) return -1;
+    if (P->dip[m].ib0 >= P->nb0 || P->dip[m].jb0 >= P->nb0) return -1;
+  }
+  P->vgrid_done = false;
+  return 0;
+}
+
+int or_set_field(void* h, double vw, double mw, int keo) {
+  Problem* P = (Problem*)h;
+  P->vw = vw; P->mw = mw; P->keo = keo ? 1 : 0;
   return 0;
 }
 

@@ -50,6 +50,8 @@ def lib():
         L.or_set_potential.argtypes = [vp, C.c_int, dp, ip, ip]
         L.or_set_keo.argtypes = [vp, C.c_int, dp, dp]
         L.or_vgrid.argtypes = [vp, dp]
+        L.or_set_dipole.argtypes = [vp, C.c_int, dp, ip, ip]
+        L.or_set_field.argtypes = [vp, C.c_double, C.c_double, C.c_int]
         L.or_hpsi.argtypes = [vp, dp, C.c_longlong, dp, C.c_longlong, C.c_int, C.c_int]
         _lib = L
     return _lib
@@ -106,6 +108,16 @@ class OracleProblem:
         g, pg = _d(np.asfortranarray(spec.g).ravel(order="F"))
         if L.or_set_keo(self.h, spec.keo_type, pG0, pg) != 0:
             raise ValueError("oracle: bad KEO")
+        if getattr(spec, "dip_coef", None) is not None:
+            dc, pdc = _d(spec.dip_coef)
+            di, pdi = _i(spec.dip_idx)
+            de, pde = _i(spec.dip_elec)
+            if L.or_set_dipole(self.h, len(dc), pdc, pdi, pde) != 0:
+                raise ValueError("oracle: bad dipole")
+
+    def set_field(self, vw: float = 1.0, mw: float = 0.0, keo: bool = True):
+        """Grid operator vw*V + mw*mu (+ kinetic part) of later hpsi calls (H - E mu: vw=1, mw=-E)."""
+        lib().or_set_field(self.h, float(vw), float(mw), 1 if keo else 0)
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -15,10 +15,31 @@ pytestmark = pytest.mark.gpu
 FP64_TOL = 1e-12
 FP32_TOL = 2e-5
 
+def dp_type1_two_states():
+    """Direct product, two coupled electronic states, type-1 KEO with off-diagonal G0,
+    uneven nq > nb per mode (the stage kernels' type-1 and multi-state branches)."""
+    omega = np.array([0.010, 0.008, 0.005])
+    s = np.sqrt(omega)
+    p = S.Poly()
+    for e in (0, 1):
+        for i in range(3):
+            p.add(0.5 * omega[i] ** 2, [i, i], e, e)
+    p.add(0.002, [], 1, 1)
+    p.add(0.001 * s[0], [0], 0, 1)
+    p.add(0.001 * s[0], [0], 1, 0)
+    p.add(2e-5 * s[0] * s[1] * s[2], [0, 1, 2], 1, 1)
+    c, idx, el = p.arrays()
+    G0 = np.eye(3) + 0.05 * (np.ones((3, 3)) - np.eye(3))
+    return S.ProblemSpec(kind="dp", D=3, nb0=2, nq_dp=[8, 7, 6], nb_dp=[6, 5, 5], scaleQ=s, mono_coef=c,
+                         mono_idx=idx, mono_elec=el, keo_type=1, G0=G0, name="DP3_type1_2states")
+
+
 CASES = {
     "hh6d_l3_type1": lambda: S.henon_heiles(6, 3),
     "pyrazine12d_nb0_2": lambda: S.pyrazine_12d(1),
     "dp3_type10_g": lambda: S.config_dp3(),
+    "dp3_type1_2states": dp_type1_two_states,
+    "dp4_nq_gt_nb": lambda: S.config_oc(seed=2, nb=5, nq=7, D=4, omega=(0.01, 0.009, 0.006, 0.004)),
     "sg4_d4_l5_type10_g": lambda: S.config_sg4(4, 5, seed=5),
     "sg4_d6_l4_type10_g": lambda: S.config_sg4(6, 4, seed=6),
     "sg4_d3_l8_nq_eq_nb": lambda: S.config_sg4(3, 8, seed=7, nq_A=1),
@@ -39,12 +60,15 @@ def rel(a, b):
     return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
 
 
-@pytest.mark.parametrize("slab", [True, False], ids=["slab", "general"])
+PATHS = dict(argvalues=[1, 2, 0], ids=["auto", "slab", "general"])
+
+
+@pytest.mark.parametrize("path", **PATHS)
 @pytest.mark.parametrize("name", list(CASES))
 @pytest.mark.parametrize("nvec", [1, 5, 64])
-def test_hpsi_fp64_matches_oracle(name, nvec, slab):
+def test_hpsi_fp64_matches_oracle(name, nvec, path):
     spec, pg, po = problems(name)
-    pg.set_kernel_path(slab)
+    pg.set_kernel_path(path)
     rng = np.random.default_rng(123 + nvec)
     psi = rng.standard_normal((pg.N, nvec))
     ref = po.hpsi(psi)
@@ -52,12 +76,12 @@ def test_hpsi_fp64_matches_oracle(name, nvec, slab):
     assert rel(out, ref) <= FP64_TOL
 
 
-@pytest.mark.parametrize("slab", [True, False], ids=["slab", "general"])
-@pytest.mark.parametrize("name", ["hh6d_l3_type1", "dp3_type10_g", "sg4_d6_l4_type10_g", "pyrazine12d_nb0_2",
-                                  "sg4_d12_l2"])
-def test_hpsi_fp32_matches_oracle(name, slab):
+@pytest.mark.parametrize("path", **PATHS)
+@pytest.mark.parametrize("name", ["hh6d_l3_type1", "dp3_type10_g", "dp3_type1_2states", "sg4_d6_l4_type10_g",
+                                  "pyrazine12d_nb0_2", "sg4_d12_l2"])
+def test_hpsi_fp32_matches_oracle(name, path):
     spec, pg, po = problems(name)
-    pg.set_kernel_path(slab)
+    pg.set_kernel_path(path)
     rng = np.random.default_rng(7)
     psi = rng.standard_normal((pg.N, 16))
     ref = po.hpsi(psi)
@@ -127,3 +151,19 @@ def test_errors_are_reported_not_fatal():
     assert ei.value.code == E.EVR_EINVAL
     out = pg.hpsi(np.ones((pg.N, 1)))  # context still usable
     assert np.isfinite(out).all()
+
+
+@pytest.mark.parametrize("path", **PATHS)
+def test_operator_forms_direct_product(path):
+    # H^T and (H + H^T)/2 of the non-symmetric type-10 direct-product operator (nq > nb)
+    spec, pg, po = problems("dp4_nq_gt_nb")
+    pg.set_kernel_path(path)
+    H = po.dense()
+    rng = np.random.default_rng(5)
+    psi = rng.standard_normal((pg.N, 6))
+    try:
+        for form, ref in (("HT", H.T @ psi), ("HSYM", 0.5 * (H + H.T) @ psi), ("H", H @ psi)):
+            pg.set_operator(form)
+            assert rel(pg.hpsi(psi), ref) <= FP64_TOL
+    finally:
+        pg.set_operator("H")
