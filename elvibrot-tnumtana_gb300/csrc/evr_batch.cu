@@ -1,0 +1,874 @@
+// evr_batch.cu -- many independent problems in one context: stacked H.psi and a lock-step
+// batched Davidson.
+//
+// evr_create_batch stacks n problems (any D and level, the same number of electronic
+// states and KEO form) into one term table: the terms of problem s keep their own 1-D
+// matrices, grids, G0 and g (at the offsets g0off/goff of each term), and their packed
+// functions occupy rows offsets[s] .. offsets[s+1]-1 of a stacked vector.  H is then block
+// diagonal, and one H.psi launch of the term kernels (one persistent item queue) applies
+// H_s to the rows of every problem in every column at once.  G(Q) is evaluated per point
+// from the linear model instead of a table (a table for 256 problems up to D=6, L=8 would
+// take 160 GB).
+//
+// evr_batch_davidson runs sub_propagation_Davidson (sub_module_Davidson.f90:54-748, as in
+// evr_davidson.cu) for every problem at once: all problems share the subspace size, so the
+// per-problem projections and Ritz combinations are grouped cuBLAS GEMMs (one group per
+// problem), the small projected eigenproblems are solved by a batched Jacobi kernel (one
+// CTA per problem), and the H.psi of the new directions of all problems is one call.
+// Mixed precision follows evr_davidson (FP32 phase, then FP64 H.psi of the kept Ritz
+// vectors and FP32 H.psi for new directions with the FP64 side of every mixed product).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <numeric>
+#include <vector>
+
+#include <cublas_v2.h>
+
+#include "evr_internal.h"
+
+using namespace evr;
+
+namespace {
+
+constexpr int kBT = 256;
+
+// ---------------------------------------------------------------------------------------
+// device kernels
+// ---------------------------------------------------------------------------------------
+
+// V table of the terms [t0, t1) from one problem's monomials (positions -> reference modes)
+__global__ void batch_vgrid_kernel(const TermDesc* __restrict__ terms, int t0, int t1, const double* __restrict__ mats,
+                                   int64_t q0, int64_t q1, int nb0, int n_mono, const double* __restrict__ coef,
+                                   const int* __restrict__ midx, const int* __restrict__ melec,
+                                   double* __restrict__ vgrid) {
+  for (int64_t gq = q0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; gq < q1;
+       gq += (int64_t)gridDim.x * blockDim.x) {
+    int lo = t0, hi = t1 - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (terms[mid].off_nq <= gq) lo = mid; else hi = mid - 1;
+    }
+    const TermDesc& T = terms[lo];
+    const int64_t q = gq - T.off_nq;
+    const int NQ = T.NQ, D = T.D;
+    double Q[kMaxD];
+    int64_t r = q;
+    for (int d = 0; d < D; ++d) {
+      Q[T.perm[d]] = mats[T.m_x[d] + (int)(r % T.nq[d])];
+      r /= T.nq[d];
+    }
+    double* V = vgrid + T.off_nq * nb0 * nb0;
+    for (int ab = 0; ab < nb0 * nb0; ++ab) V[(int64_t)ab * NQ + q] = 0.0;
+    for (int m = 0; m < n_mono; ++m) {
+      double v = coef[m];
+      for (int k = 0; k < 4; ++k) {
+        const int i = midx[4 * m + k];
+        if (i >= 0) v *= Q[i];
+      }
+      V[(int64_t)(melec[2 * m] + nb0 * melec[2 * m + 1]) * NQ + q] += v;
+    }
+  }
+}
+
+__global__ void batch_to_float(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+// Eigen-decomposition of one symmetric n x n matrix per CTA (n <= 64) by cyclic Jacobi
+// with the round-robin ordering: each round rotates n/2 disjoint pairs at once (angles
+// from the matrix before the round, so the round is A <- R^T A R with R a product of
+// commuting plane rotations).  At most max_sweeps sweeps; stops when the off-diagonal
+// norm is below tol times the norm of A.  Eigenvalues ascending into W, eigenvectors as
+// the columns of V (column-major, ld ldv).
+__global__ void batched_jacobi_kernel(const double* __restrict__ A, int lda, int64_t sa, int n,
+                                      double* __restrict__ W, int64_t sw, double* __restrict__ V, int ldv, int64_t sv,
+                                      int max_sweeps, double tol) {
+  extern __shared__ double sm[];
+  const int np = (n + 1) & ~1;
+  double* a = sm;             // np x np, a[i + np*j]
+  double* v = sm + np * np;   // np x np
+  __shared__ double c_[32], s_[32];
+  __shared__ int p_[32], q_[32];
+  __shared__ double red[kBT / 32];
+  __shared__ double s_off, s_tot;
+  const double* Ab = A + blockIdx.x * sa;
+  for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
+    const int i = e % np, j = e / np;
+    a[e] = (i < n && j < n) ? 0.5 * (Ab[i + (int64_t)lda * j] + Ab[j + (int64_t)lda * i]) : 0.0;
+    v[e] = i == j ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  const int npair = np / 2;
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    // off-diagonal and total Frobenius norms
+    double off = 0.0, tot = 0.0;
+    for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
+      const double x = a[e] * a[e];
+      tot += x;
+      if (e % np != e / np) off += x;
+    }
+    for (int pass = 0; pass < 2; ++pass) {
+      double val = pass == 0 ? off : tot;
+      for (int o = 16; o > 0; o >>= 1) val += __shfl_down_sync(0xffffffffu, val, o);
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = val;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        if (pass == 0) s_off = t; else s_tot = t;
+      }
+      __syncthreads();
+    }
+    if (!(s_off > tol * tol * s_tot)) break;
+    for (int r = 0; r < np - 1; ++r) {
+      if (threadIdx.x < npair) {
+        const int k = threadIdx.x;
+        auto player = [&](int pos) { return pos == 0 ? 0 : ((pos - 1 + r) % (np - 1)) + 1; };
+        int p = player(k), q = player(np - 1 - k);
+        if (p > q) { const int t = p; p = q; q = t; }
+        const double apq = a[p + np * q];
+        double c = 1.0, s = 0.0;
+        if (fabs(apq) > 1e-300) {
+          const double tau = (a[q + np * q] - a[p + np * p]) / (2.0 * apq);
+          const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+          c = 1.0 / sqrt(1.0 + t * t);
+          s = t * c;
+        }
+        c_[k] = c; s_[k] = s; p_[k] = p; q_[k] = q;
+      }
+      __syncthreads();
+      // rows p, q: a_pj <- c a_pj - s a_qj, a_qj <- s a_pj + c a_qj
+      for (int e = threadIdx.x; e < npair * np; e += blockDim.x) {
+        const int k = e / np, j = e % np;
+        const int p = p_[k], q = q_[k];
+        const double c = c_[k], s = s_[k];
+        const double x = a[p + np * j], y = a[q + np * j];
+        a[p + np * j] = c * x - s * y;
+        a[q + np * j] = s * x + c * y;
+      }
+      __syncthreads();
+      // columns p, q of A and V
+      for (int e = threadIdx.x; e < npair * np; e += blockDim.x) {
+        const int k = e / np, i = e % np;
+        const int p = p_[k], q = q_[k];
+        const double c = c_[k], s = s_[k];
+        const double x = a[i + np * p], y = a[i + np * q];
+        a[i + np * p] = c * x - s * y;
+        a[i + np * q] = s * x + c * y;
+        const double vx = v[i + np * p], vy = v[i + np * q];
+        v[i + np * p] = c * vx - s * vy;
+        v[i + np * q] = s * vx + c * vy;
+      }
+      __syncthreads();
+    }
+  }
+  // ascending order of the n real eigenvalues (the padding index, if any, is np - 1 = n
+  // and stays decoupled)
+  __shared__ int ord[64];
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < n; ++i) ord[i] = i;
+    for (int i = 1; i < n; ++i) {
+      const int t = ord[i];
+      const double x = a[t + np * t];
+      int j = i - 1;
+      while (j >= 0 && a[ord[j] + np * ord[j]] > x) { ord[j + 1] = ord[j]; --j; }
+      ord[j + 1] = t;
+    }
+  }
+  __syncthreads();
+  double* Wb = W + blockIdx.x * sw;
+  double* Vb = V + blockIdx.x * sv;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e % n, j = e / n;
+    Vb[i + (int64_t)ldv * j] = v[i + np * ord[j]];
+  }
+  for (int j = threadIdx.x; j < n; j += blockDim.x) Wb[j] = a[ord[j] + np * ord[j]];
+}
+
+// mirror the new columns of every projected matrix into its rows and, for dropped
+// (zero) columns, put a large diagonal so that they never enter the lowest Ritz pairs
+__global__ void batch_mirror_kernel(double* __restrict__ Hs, int ldh, int64_t sh, int n0, int n1,
+                                    const unsigned char* __restrict__ dead, int mcols) {
+  double* H = Hs + blockIdx.x * sh;
+  const unsigned char* dd = dead + (int64_t)blockIdx.x * mcols;
+  for (int e = threadIdx.x; e < n1 * (n1 - n0); e += blockDim.x) {
+    const int i = e % n1, j = n0 + e / n1;
+    if (i < n0) H[j + (int64_t)ldh * i] = H[i + (int64_t)ldh * j];
+  }
+  __syncthreads();
+  for (int j = n0 + threadIdx.x; j < n1; j += blockDim.x)
+    if (dd[j]) {
+      for (int i = 0; i < n1; ++i) {
+        H[i + (int64_t)ldh * j] = 0.0;
+        H[j + (int64_t)ldh * i] = 0.0;
+      }
+    }
+  __syncthreads();
+  for (int j = n0 + threadIdx.x; j < n1; j += blockDim.x)
+    if (dd[j]) H[j + (int64_t)ldh * j] = 1e30;
+}
+
+// R[r, j] = HX[r, j] - E[sys(r), j] X[r, j], j < k; and |R_j|^2 per problem (atomics: the
+// norms only steer the iteration)
+__global__ void batch_residual_kernel(const double* __restrict__ X, const double* __restrict__ HX, int ldx,
+                                      const double* __restrict__ E, int lde, const int* __restrict__ sys, int k,
+                                      int64_t N, double* __restrict__ R, double* __restrict__ nrm) {
+  const int64_t total = N * k;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / k;
+    const int j = (int)(e - r * k);
+    const int s = __ldg(sys + r);
+    const double val = HX[r * ldx + j] - __ldg(E + (int64_t)s * lde + j) * X[r * ldx + j];
+    R[r * ldx + j] = val;
+    atomicAdd(nrm + (int64_t)s * k + j, val * val);
+  }
+}
+
+// T[r, j] = R[r, sel[sys, j]] / (E[sys, sel] - e0[r]) (diagonal preconditioner, floored)
+__global__ void batch_precondition_kernel(const double* __restrict__ R, int ldr, const int* __restrict__ sel, int ns,
+                                          const double* __restrict__ E, int lde, const double* __restrict__ e0,
+                                          const int* __restrict__ sys, int64_t N, double* __restrict__ T, int ldt,
+                                          double floor_) {
+  const int64_t total = N * ns;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / ns;
+    const int j = (int)(e - r * ns);
+    const int s = __ldg(sys + r);
+    const int l = __ldg(sel + s * ns + j);
+    double den = __ldg(E + (int64_t)s * lde + l) - __ldg(e0 + r);
+    if (fabs(den) < floor_) den = den < 0 ? -floor_ : floor_;
+    T[r * ldt + j] = R[r * ldr + l] / den;
+  }
+}
+
+// transform of the symmetric orthonormalisation: M[:, j] = U[:, j]/sqrt(lambda_j) for
+// lambda_j > thr * lambda_max, else 0 (column j dropped)
+__global__ void batch_lowdin_kernel(const double* __restrict__ U, const double* __restrict__ lam, int ns,
+                                    double* __restrict__ Mt, int ldm, int64_t smt, unsigned char* __restrict__ dead,
+                                    int mcols, int col0, double thr) {
+  const double* Ub = U + blockIdx.x * (int64_t)ns * ns;
+  const double* lb = lam + blockIdx.x * (int64_t)ns;
+  double* Mb = Mt + blockIdx.x * smt;
+  const double lmax = fmax(lb[ns - 1], 1e-300);
+  for (int e = threadIdx.x; e < ns * ns; e += blockDim.x) {
+    const int i = e % ns, j = e / ns;
+    const bool ok = lb[j] > thr * lmax && lb[j] > 1e-280;
+    Mb[i + (int64_t)ldm * j] = ok ? Ub[i + (int64_t)ns * j] / sqrt(lb[j]) : 0.0;
+  }
+  for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+    const bool ok = lb[j] > thr * lmax && lb[j] > 1e-280;
+    dead[(int64_t)blockIdx.x * mcols + col0 + j] = ok ? 0 : 1;
+  }
+}
+
+// a projected matrix of Ritz pairs: diag(E_s) in the leading k x k block
+__global__ void batch_diag_kernel(double* __restrict__ Hs, int ldh, int64_t sh, const double* __restrict__ E,
+                                  int lde, int k) {
+  double* H = Hs + blockIdx.x * sh;
+  for (int e = threadIdx.x; e < ldh * ldh; e += blockDim.x) H[e] = 0.0;
+  __syncthreads();
+  for (int j = threadIdx.x; j < k; j += blockDim.x) H[j + (int64_t)ldh * j] = E[(int64_t)blockIdx.x * lde + j];
+}
+
+struct DBuf {
+  void* p = nullptr;
+  ~DBuf() {
+    if (p) cudaFree(p);
+  }
+  bool alloc(size_t bytes) { return cudaMalloc(&p, std::max<size_t>(bytes, 8)) != cudaSuccess; }
+  double* d() const { return (double*)p; }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// batch context
+// ---------------------------------------------------------------------------------------
+namespace evr {
+struct BatchInfo {
+  std::vector<int64_t> off;  // n_sys + 1 packed offsets
+  std::vector<HostProblem> sub;
+  int* sys_d = nullptr;      // row -> problem (nb0 == 1)
+};
+}  // namespace evr
+
+static void free_batch(evr_ctx* c) {
+  BatchInfo* b = (BatchInfo*)c->batch;
+  if (!b) return;
+  if (b->sys_d) cudaFree(b->sys_d);
+  delete b;
+  c->batch = nullptr;
+}
+
+namespace evr {
+void free_batch_info(evr_ctx* c) { free_batch(c); }
+}  // namespace evr
+
+#define EVR_CU(call, what)                 \
+  do {                                     \
+    int _rc = cuda_check(c, (call), what); \
+    if (_rc != EVR_OK) return _rc;         \
+  } while (0)
+
+static int merge_problems(evr_ctx* c, std::vector<HostProblem>& sub, std::string& err) {
+  HostProblem& P = c->hp;
+  P = HostProblem();
+  const HostProblem& P0 = sub[0];
+  P.kind = P0.kind;
+  P.nb0 = P0.nb0;
+  P.keo_type = P0.keo_type;
+  P.symmetric = true;
+  int Dmax = 0;
+  for (const HostProblem& Q : sub) {
+    if (Q.nb0 != P.nb0) { err = "batched problems need the same number of electronic states"; return EVR_EINVAL; }
+    if (Q.keo_type != P.keo_type) { err = "batched problems need the same KEO type"; return EVR_EINVAL; }
+    Dmax = std::max(Dmax, Q.D);
+    P.symmetric = P.symmetric && Q.symmetric;
+  }
+  P.D = Dmax;
+  int64_t np_off = 0, nb_off = 0, nq_off = 0;
+  size_t pool_off = 0, g0_off = 0, g_off = 0;
+  std::vector<int64_t> np_of(sub.size());
+  for (size_t s = 0; s < sub.size(); ++s) {
+    const HostProblem& Q = sub[s];
+    np_of[s] = np_off;
+    if (pool_off + Q.mat_pool.size() > (size_t)INT32_MAX || g_off + Q.g.size() > (size_t)INT32_MAX) {
+      err = "batch too large for 32-bit table offsets";
+      return EVR_EINVAL;
+    }
+    P.mat_pool.insert(P.mat_pool.end(), Q.mat_pool.begin(), Q.mat_pool.end());
+    P.G0.insert(P.G0.end(), Q.G0.begin(), Q.G0.end());
+    P.g.insert(P.g.end(), Q.g.begin(), Q.g.end());
+    auto shift = [&](TermDesc T) {
+      T.off_nb += nb_off;
+      T.off_nq += nq_off;
+      for (int p = 0; p < Q.D; ++p) {
+        T.m_d0b[p] += (int)pool_off;
+        T.m_bgw[p] += (int)pool_off;
+        T.m_d1[p] += (int)pool_off;
+        T.m_d2[p] += (int)pool_off;
+        T.m_x[p] += (int)pool_off;
+      }
+      T.m_x1L += (int)pool_off;
+      T.m_x2L += (int)pool_off;
+      T.m_e1L += (int)pool_off;
+      T.m_e2L += (int)pool_off;
+      T.g0off = (int)g0_off;
+      T.goff = (int)g_off;
+      return T;
+    };
+    for (size_t t = 0; t < Q.terms.size(); ++t) {
+      P.terms.push_back(shift(Q.terms[t]));
+      P.termsT.push_back(shift(Q.termsT[t]));
+      P.weight.push_back(Q.weight[t]);
+    }
+    for (int v : Q.map_perm) P.map_perm.push_back(v >= 0 ? (int)(v + np_off) : -1);
+    for (int v : Q.map) P.map.push_back(v >= 0 ? (int)(v + np_off) : -1);
+    np_off += Q.Np;
+    nb_off += Q.sum_nb;
+    nq_off += Q.sum_nq;
+    pool_off += Q.mat_pool.size();
+    g0_off += Q.G0.size();
+    g_off += Q.g.size();
+    P.max_nq = std::max(P.max_nq, Q.max_nq);
+    P.max_nb = std::max(P.max_nb, Q.max_nb);
+    P.flop_per_hpsi += Q.flop_per_hpsi;
+  }
+  if (np_off * P.nb0 >= INT32_MAX) { err = "batch too large (packed index beyond 32 bits)"; return EVR_EINVAL; }
+  P.Np = np_off;
+  P.sum_nb = nb_off;
+  P.sum_nq = nq_off;
+  const int nb0 = P.nb0;
+  const int64_t N = P.Np * nb0;
+  // CSR over the stacked rows (a * Np + packed), sources shifted with the term offsets
+  P.csr_ptr.assign((size_t)N + 1, 0);
+  for (int a = 0; a < nb0; ++a)
+    for (size_t s = 0; s < sub.size(); ++s) {
+      const HostProblem& Q = sub[s];
+      for (int64_t k = 0; k < Q.Np; ++k) {
+        const int64_t lr = a * Q.Np + k, gr = a * P.Np + np_of[s] + k;
+        P.csr_ptr[(size_t)gr + 1] = Q.csr_ptr[(size_t)lr + 1] - Q.csr_ptr[(size_t)lr];
+      }
+    }
+  for (int64_t r = 0; r < N; ++r) P.csr_ptr[(size_t)r + 1] += P.csr_ptr[(size_t)r];
+  P.csr_src.resize((size_t)P.csr_ptr[(size_t)N]);
+  P.csr_w.resize((size_t)P.csr_ptr[(size_t)N]);
+  P.e0diag.assign((size_t)N, 0.0);
+  int64_t nbo = 0;
+  for (size_t s = 0; s < sub.size(); ++s) {
+    const HostProblem& Q = sub[s];
+    for (int a = 0; a < nb0; ++a)
+      for (int64_t k = 0; k < Q.Np; ++k) {
+        const int64_t lr = a * Q.Np + k, gr = a * P.Np + np_of[s] + k;
+        int64_t o = P.csr_ptr[(size_t)gr];
+        for (int64_t e = Q.csr_ptr[(size_t)lr]; e < Q.csr_ptr[(size_t)lr + 1]; ++e, ++o) {
+          // local source off_nb*nb0 + a*NB + iB -> shift off_nb by the problem's offset
+          P.csr_src[(size_t)o] = Q.csr_src[(size_t)e] + nbo * nb0;
+          P.csr_w[(size_t)o] = Q.csr_w[(size_t)e];
+        }
+        P.e0diag[(size_t)gr] = Q.e0diag[(size_t)lr];
+      }
+    nbo += Q.sum_nb;
+  }
+  return EVR_OK;
+}
+
+static int upload_batch(evr_ctx* c) {
+  HostProblem& P = c->hp;
+  DeviceProblem& d = c->dp;
+  BatchInfo* b = (BatchInfo*)c->batch;
+  auto up = [&](void** dst, const void* src, size_t bytes) -> int {
+    EVR_CU(cudaMalloc(dst, std::max<size_t>(bytes, 8)), "cudaMalloc");
+    if (bytes) EVR_CU(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice), "cudaMemcpy");
+    return EVR_OK;
+  };
+  int rc;
+  if ((rc = up((void**)&d.terms, P.terms.data(), P.terms.size() * sizeof(TermDesc)))) return rc;
+  if ((rc = up((void**)&d.termsT, P.termsT.data(), P.termsT.size() * sizeof(TermDesc)))) return rc;
+  if ((rc = up((void**)&d.mats, P.mat_pool.data(), P.mat_pool.size() * sizeof(double)))) return rc;
+  if ((rc = up((void**)&d.map, P.map_perm.data(), P.map_perm.size() * sizeof(int)))) return rc;
+  if ((rc = up((void**)&d.csr_ptr, P.csr_ptr.data(), P.csr_ptr.size() * sizeof(int64_t)))) return rc;
+  if ((rc = up((void**)&d.csr_src, P.csr_src.data(), P.csr_src.size() * sizeof(int64_t)))) return rc;
+  if ((rc = up((void**)&d.csr_w, P.csr_w.data(), P.csr_w.size() * sizeof(double)))) return rc;
+  if ((rc = up((void**)&d.G0, P.G0.data(), P.G0.size() * sizeof(double)))) return rc;
+  if ((rc = up((void**)&d.g, P.g.data(), P.g.size() * sizeof(double)))) return rc;
+  if ((rc = up((void**)&d.e0diag, P.e0diag.data(), P.e0diag.size() * sizeof(double)))) return rc;
+  const int nb0 = P.nb0;
+  const int64_t nv = P.sum_nq * nb0 * nb0;
+  EVR_CU(cudaMalloc((void**)&d.vgrid, nv * sizeof(double)), "cudaMalloc vgrid");
+  // V per problem from its own monomials
+  int64_t t0 = 0, q0 = 0;
+  for (const HostProblem& Q : b->sub) {
+    const int nm = (int)Q.mono_coef.size();
+    double* dc = nullptr;
+    int *di = nullptr, *de = nullptr;
+    if ((rc = up((void**)&dc, Q.mono_coef.data(), nm * sizeof(double))) ||
+        (rc = up((void**)&di, Q.mono_idx.data(), Q.mono_idx.size() * sizeof(int))) ||
+        (rc = up((void**)&de, Q.mono_elec.data(), Q.mono_elec.size() * sizeof(int))))
+      return rc;
+    const int64_t t1 = t0 + (int64_t)Q.terms.size(), q1 = q0 + Q.sum_nq;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((Q.sum_nq + 255) / 256, c->num_sms * 8));
+    batch_vgrid_kernel<<<blocks, 256, 0, c->stream>>>(d.terms, (int)t0, (int)t1, d.mats, q0, q1, nb0, nm, dc, di, de,
+                                                       d.vgrid);
+    EVR_CU(cudaGetLastError(), "batch_vgrid_kernel");
+    EVR_CU(cudaStreamSynchronize(c->stream), "batch V");
+    cudaFree(dc);
+    cudaFree(di);
+    cudaFree(de);
+    t0 = t1;
+    q0 = q1;
+  }
+  EVR_CU(cudaMalloc((void**)&d.mats32, P.mat_pool.size() * sizeof(float) + 16), "cudaMalloc mats32");
+  EVR_CU(cudaMalloc((void**)&d.vgrid32, nv * sizeof(float)), "cudaMalloc vgrid32");
+  batch_to_float<<<c->num_sms * 4, 256, 0, c->stream>>>(d.mats, d.mats32, (int64_t)P.mat_pool.size());
+  batch_to_float<<<c->num_sms * 8, 256, 0, c->stream>>>(d.vgrid, d.vgrid32, nv);
+  EVR_CU(cudaGetLastError(), "batch_to_float");
+  // row -> problem
+  if (nb0 == 1) {
+    std::vector<int> sys((size_t)P.Np);
+    for (size_t s = 0; s + 1 < b->off.size(); ++s)
+      for (int64_t k = b->off[s]; k < b->off[s + 1]; ++k) sys[(size_t)k] = (int)s;
+    if ((rc = up((void**)&b->sys_d, sys.data(), sys.size() * sizeof(int)))) return rc;
+  }
+  EVR_CU(cudaStreamSynchronize(c->stream), "batch set-up");
+  return EVR_OK;
+}
+
+extern "C" {
+
+int evr_create_batch(evr_ctx** out, const evr_problem_desc* descs, int n_sys, int device) {
+  if (!out) return EVR_EINVAL;
+  *out = nullptr;
+  evr_ctx* c = new (std::nothrow) evr_ctx();
+  if (!c) return EVR_ENOMEM;
+  *out = c;
+  if (!descs || n_sys < 1) return set_error(c, EVR_EINVAL, "evr_create_batch: no problems");
+  c->device = device;
+  BatchInfo* b = new BatchInfo();
+  c->batch = b;
+  b->sub.resize(n_sys);
+  b->off.assign(n_sys + 1, 0);
+  for (int s = 0; s < n_sys; ++s) {
+    std::string err;
+    int rc = build_host_problem(&descs[s], b->sub[s], err);
+    if (rc) return set_error(c, rc, "evr_create_batch: problem " + std::to_string(s) + ": " + err);
+    b->off[s + 1] = b->off[s] + b->sub[s].Np;
+  }
+  std::string err;
+  int rc = merge_problems(c, b->sub, err);
+  if (rc) return set_error(c, rc, "evr_create_batch: " + err);
+  c->n_sys = n_sys;
+  c->gfly = false;
+  for (const HostProblem& Q : b->sub)
+    if (Q.keo_type == 10)
+      for (double v : Q.g) c->gfly |= (v != 0.0);
+  c->use_stages = false;
+  if (device < 0) {
+    c->host_only = true;
+    return EVR_OK;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device >= ndev) {
+    (void)cudaGetLastError();
+    return set_error(c, EVR_EDEVICE, "no CUDA device " + std::to_string(device));
+  }
+  EVR_CU(cudaSetDevice(device), "cudaSetDevice");
+  EVR_CU(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device), "attr");
+  EVR_CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  for (auto& e : c->ev) EVR_CU(cudaEventCreate(&e), "cudaEventCreate");
+  return upload_batch(c);
+}
+
+int evr_batch_offsets(const evr_ctx* c, int64_t* offsets) {
+  if (!c || !offsets) return EVR_EINVAL;
+  const BatchInfo* b = (const BatchInfo*)c->batch;
+  if (!b) {
+    offsets[0] = 0;
+    offsets[1] = c->hp.Np;
+    return EVR_OK;
+  }
+  std::copy(b->off.begin(), b->off.end(), offsets);
+  return EVR_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// batched Davidson
+// ---------------------------------------------------------------------------------------
+namespace {
+
+struct Grouped {
+  // one GEMM per problem: C_s = op(A_s) op(B_s), sizes and pointers per problem
+  std::vector<cublasOperation_t> ta, tb;
+  std::vector<int> m, n, k, lda, ldb, ldc, gsz;
+  std::vector<double> alpha, beta;
+  std::vector<const double*> A, B;
+  std::vector<double*> C;
+  DBuf dptr;  // device copies of the pointer arrays
+  size_t cap = 0;
+};
+
+struct BatchDavidson {
+  evr_ctx* c;
+  cudaStream_t s;
+  cublasHandle_t blas = nullptr;
+  int nsys = 0, M = 0, nkeep = 0, bmax = 0, op = OP_H;
+  int64_t N = 0;
+  std::vector<int64_t> off;
+  const int* sys_d = nullptr;
+  DBuf Pt, HPt, X, HX, R, T, Tt, Hs, Wv, Ev, Cm, Gm, Um, Lm, Mt, nrm, sel, dead, ptrs;
+  int64_t sh = 0;  // stride of one projected matrix (M*M)
+  Grouped g;
+
+  ~BatchDavidson() {
+    if (blas) cublasDestroy(blas);
+  }
+  int fail(int code, const std::string& m) { return set_error(c, code, "evr_batch_davidson: " + m); }
+
+  int init() {
+    if (cublasCreate(&blas) != CUBLAS_STATUS_SUCCESS) return fail(EVR_EDEVICE, "cublasCreate");
+    cublasSetStream(blas, s);
+    cublasSetPointerMode(blas, CUBLAS_POINTER_MODE_HOST);
+    sh = (int64_t)M * M;
+    const size_t nm = (size_t)N * M;
+    if (Pt.alloc(nm * 8) || HPt.alloc(nm * 8) || X.alloc((size_t)N * nkeep * 8) || HX.alloc((size_t)N * nkeep * 8) ||
+        R.alloc((size_t)N * nkeep * 8) || T.alloc((size_t)N * bmax * 8) || Tt.alloc((size_t)N * bmax * 8) ||
+        Hs.alloc((size_t)nsys * sh * 8) || Wv.alloc((size_t)nsys * sh * 8) || Ev.alloc((size_t)nsys * M * 8) ||
+        Cm.alloc((size_t)nsys * M * bmax * 8) || Gm.alloc((size_t)nsys * bmax * bmax * 8) ||
+        Um.alloc((size_t)nsys * bmax * bmax * 8) || Lm.alloc((size_t)nsys * bmax * 8) ||
+        Mt.alloc((size_t)nsys * bmax * bmax * 8) || nrm.alloc((size_t)nsys * nkeep * 8) ||
+        sel.alloc((size_t)nsys * bmax * sizeof(int)) || dead.alloc((size_t)nsys * M) ||
+        ptrs.alloc((size_t)3 * nsys * sizeof(double*)))
+      return fail(EVR_ENOMEM, "device allocation");
+    if (cudaMemsetAsync(dead.p, 0, (size_t)nsys * M, s)) return fail(EVR_EDEVICE, "memset");
+    const int np = ((std::max(M, bmax) + 1) & ~1);
+    if (cudaFuncSetAttribute(batched_jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(2 * np * np * sizeof(double))) != cudaSuccess)
+      return fail(EVR_EDEVICE, "jacobi attribute");
+    return EVR_OK;
+  }
+
+  // per problem q: C_q (m_q x n_q, ld ldc) = alpha op(A_q) op(B_q) + beta C_q, inner size k_q
+  using IntF = std::function<int(int)>;
+  using PtrF = std::function<const double*(int)>;
+  using OutF = std::function<double*(int)>;
+  int grouped(cublasOperation_t ta, cublasOperation_t tb, IntF mfun, IntF nfun, IntF kfun, PtrF afun, int lda,
+              PtrF bfun, int ldb, OutF cfun, int ldc, double alpha, double beta) {
+    g.ta.assign(nsys, ta);
+    g.tb.assign(nsys, tb);
+    g.m.resize(nsys);
+    g.n.resize(nsys);
+    g.k.resize(nsys);
+    g.lda.assign(nsys, lda);
+    g.ldb.assign(nsys, ldb);
+    g.ldc.assign(nsys, ldc);
+    g.gsz.assign(nsys, 1);
+    g.alpha.assign(nsys, alpha);
+    g.beta.assign(nsys, beta);
+    g.A.resize(nsys);
+    g.B.resize(nsys);
+    g.C.resize(nsys);
+    for (int q = 0; q < nsys; ++q) {
+      g.m[q] = mfun(q);
+      g.n[q] = nfun(q);
+      g.k[q] = kfun(q);
+      g.A[q] = afun(q);
+      g.B[q] = bfun(q);
+      g.C[q] = cfun(q);
+    }
+    const double** dA = (const double**)ptrs.p;
+    const double** dB = dA + nsys;
+    double** dC = (double**)(dB + nsys);
+    std::vector<const void*> hp(3 * (size_t)nsys);
+    for (int q = 0; q < nsys; ++q) {
+      hp[q] = g.A[q];
+      hp[nsys + q] = g.B[q];
+      hp[2 * nsys + q] = g.C[q];
+    }
+    if (cudaMemcpyAsync(ptrs.p, hp.data(), hp.size() * sizeof(void*), cudaMemcpyHostToDevice, s) ||
+        cudaStreamSynchronize(s))
+      return fail(EVR_EDEVICE, "pointer upload");
+    if (cublasDgemmGroupedBatched(blas, g.ta.data(), g.tb.data(), g.m.data(), g.n.data(), g.k.data(), g.alpha.data(),
+                                  dA, g.lda.data(), dB, g.ldb.data(), g.beta.data(), dC, g.ldc.data(), nsys,
+                                  g.gsz.data()) != CUBLAS_STATUS_SUCCESS)
+      return fail(EVR_EDEVICE, "cublasDgemmGroupedBatched");
+    return EVR_OK;
+  }
+
+  int rows(int q) const { return (int)(off[q + 1] - off[q]); }
+
+  // C_s (na x nb, ld ldc) = A_s^T B_s over the problem's rows: A, B interleaved blocks
+  int gram(const double* A, int lda, const double* B, int ldb, int na, int nb, double* C, int ldc, int64_t cstride,
+           double beta = 0.0) {
+    return grouped(CUBLAS_OP_N, CUBLAS_OP_T, [=](int) { return na; }, [=](int) { return nb; },
+                   [this](int q) { return rows(q); }, [=](int q) { return A + off[q] * lda; }, lda,
+                   [=](int q) { return B + off[q] * ldb; }, ldb, [=](int q) { return C + q * cstride; }, ldc, 1.0,
+                   beta);
+  }
+  // Y_s (rows x k, interleaved ld ldy) = alpha X_s (rows x n, ld ldx) Mat_s (n x k, ld ldm) + beta Y_s
+  int combine(const double* Xb, int ldx, int n, const double* Mat, int ldm, int64_t mstride, int k, double* Y, int ldy,
+              double alpha, double beta) {
+    return grouped(CUBLAS_OP_T, CUBLAS_OP_N, [=](int) { return k; }, [this](int q) { return rows(q); },
+                   [=](int) { return n; }, [=](int q) { return Mat + q * mstride; }, ldm,
+                   [=](int q) { return Xb + off[q] * ldx; }, ldx, [=](int q) { return Y + off[q] * ldy; }, ldy, alpha,
+                   beta);
+  }
+
+  int hop(const double* x, int ldx, double* y, int ldy, int n, int prec, int64_t& c64, int64_t& c32) {
+    int rc = hpsi_blocks(c, x, ldx, y, ldy, n, prec, s, op);
+    if (rc) return rc;
+    (prec == EVR_PREC_FP32 ? c32 : c64) += (int64_t)n * nsys * (op == OP_HSYM ? 2 : 1);
+    return EVR_OK;
+  }
+
+  int jacobi(const double* A, int lda, int64_t sa, int n, double* W, int64_t sw, double* V, int ldv, int64_t sv) {
+    const int np = (n + 1) & ~1;
+    batched_jacobi_kernel<<<nsys, kBT, 2 * np * np * sizeof(double), s>>>(A, lda, sa, n, W, sw, V, ldv, sv, 40, 1e-15);
+    return cudaGetLastError() == cudaSuccess ? EVR_OK : fail(EVR_EDEVICE, "jacobi launch");
+  }
+
+  // orthonormalise the ns columns of T against Pt(:, 0:n1) and among themselves, append
+  // them to Pt(:, n1:n1+ns); dropped directions become zero columns flagged in `dead`
+  int orthonormalize(int ns, int n1) {
+    for (int pass = 0; pass < 2; ++pass) {
+      if (n1 > 0) {
+        int rc = gram(Pt.d(), M, T.d(), bmax, n1, ns, Cm.d(), M, (int64_t)M * bmax);
+        if (rc) return rc;
+        rc = combine(Pt.d(), M, n1, Cm.d(), M, (int64_t)M * bmax, ns, T.d(), bmax, -1.0, 1.0);
+        if (rc) return rc;
+      }
+    }
+    int rc = gram(T.d(), bmax, T.d(), bmax, ns, ns, Gm.d(), ns, (int64_t)ns * ns);
+    if (rc) return rc;
+    if ((rc = jacobi(Gm.d(), ns, (int64_t)ns * ns, ns, Lm.d(), ns, Um.d(), ns, (int64_t)ns * ns))) return rc;
+    batch_lowdin_kernel<<<nsys, kBT, 0, s>>>(Um.d(), Lm.d(), ns, Mt.d(), bmax, (int64_t)bmax * bmax,
+                                             (unsigned char*)dead.p, M, n1, 1e-12);
+    if ((rc = combine(T.d(), bmax, ns, Mt.d(), bmax, (int64_t)bmax * bmax, ns, Tt.d(), bmax, 1.0, 0.0))) return rc;
+    if (cudaMemcpy2DAsync(Pt.d() + n1, sizeof(double) * M, Tt.d(), sizeof(double) * bmax, sizeof(double) * ns, N,
+                          cudaMemcpyDeviceToDevice, s))
+      return fail(EVR_EDEVICE, "append");
+    return EVR_OK;
+  }
+
+  // projected matrices, new columns n0..n1; columns 0..ke-1 carry an FP64 H.psi
+  int rayleigh_ritz(int n0, int n1, int ke) {
+    int rc = gram(Pt.d(), M, HPt.d() + n0, M, n1, n1 - n0, Hs.d() + (int64_t)M * n0, M, sh);
+    if (rc) return rc;
+    const int kx = std::min(ke, n0);
+    if (kx > 0 && (rc = gram(HPt.d(), M, Pt.d() + n0, M, kx, n1 - n0, Hs.d() + (int64_t)M * n0, M, sh))) return rc;
+    batch_mirror_kernel<<<nsys, kBT, 0, s>>>(Hs.d(), M, sh, n0, n1, (const unsigned char*)dead.p, M);
+    return jacobi(Hs.d(), M, sh, n1, Ev.d(), M, Wv.d(), M, sh);
+  }
+};
+
+}  // namespace
+
+extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double* eig, int64_t* info) {
+  if (!c || !o || !eig) return EVR_EINVAL;
+  if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
+  BatchInfo* bi = (BatchInfo*)c->batch;
+  if (!bi) return set_error(c, EVR_EINVAL, "evr_batch_davidson: not a batch context (evr_create_batch)");
+  if (c->hp.nb0 != 1) return set_error(c, EVR_EINVAL, "evr_batch_davidson: one electronic state per problem");
+  if (o->prec != EVR_PREC_FP64 && o->prec != EVR_PREC_FP32) return set_error(c, EVR_EINVAL, "unknown precision");
+  const int nsys = c->n_sys;
+  const int nlev = o->n_levels;
+  int64_t nmin = INT64_MAX;
+  for (int q = 0; q < nsys; ++q) nmin = std::min(nmin, bi->off[q + 1] - bi->off[q]);
+  const int b = std::min(std::max(o->block, 1), 32);
+  if (nlev < 1 || nlev > nmin) return set_error(c, EVR_EINVAL, "evr_batch_davidson: n_levels out of range");
+  if (cudaSetDevice(c->device) != cudaSuccess) return set_error(c, EVR_EDEVICE, "cudaSetDevice");
+  BatchDavidson d;
+  d.c = c;
+  d.s = c->stream;
+  d.nsys = nsys;
+  d.N = c->hp.Np;
+  d.off = bi->off;
+  d.sys_d = bi->sys_d;
+  d.bmax = b;
+  d.nkeep = (int)std::min<int64_t>(nmin, nlev + b);
+  d.M = (int)std::min<int64_t>(std::min<int64_t>(nmin, 64), std::max(o->max_dim, d.nkeep + b));
+  if (d.M < d.nkeep + 1) return set_error(c, EVR_EINVAL, "evr_batch_davidson: subspace too small for the smallest problem");
+  d.op = (o->sym > 0 || (o->sym < 0 && !c->hp.symmetric)) ? OP_HSYM : OP_H;
+  int rc = d.init();
+  if (rc) return rc;
+  const int M = d.M;
+  cudaStream_t s = d.s;
+  const int64_t N = d.N;
+
+  // initial space: unit vectors on the lowest zero-order energies of every problem
+  int n1 = 0, n0 = 0;
+  {
+    const int ninit = std::min(std::min(std::max(nlev, b), M - b), b);
+    std::vector<double> h((size_t)N * b, 0.0);
+    for (int q = 0; q < nsys; ++q) {
+      const int64_t r0 = bi->off[q], nr = bi->off[q + 1] - r0;
+      std::vector<int64_t> idx(nr);
+      std::iota(idx.begin(), idx.end(), 0);
+      const int m = (int)std::min<int64_t>(ninit, nr);
+      std::partial_sort(idx.begin(), idx.begin() + m, idx.end(),
+                        [&](int64_t a, int64_t bb) { return c->hp.e0diag[r0 + a] < c->hp.e0diag[r0 + bb]; });
+      for (int j = 0; j < m; ++j) h[(size_t)(r0 + idx[j]) * b + j] = 1.0;
+    }
+    if (cudaMemcpyAsync(d.T.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, s))
+      return set_error(c, EVR_EDEVICE, "init copy");
+    if ((rc = d.orthonormalize(ninit, 0))) return rc;
+    n1 = ninit;
+  }
+  int prec = o->prec;
+  bool refine = false;
+  int ke = 0;
+  int64_t c64 = 0, c32 = 0;
+  std::vector<double> Eh((size_t)nsys * M), Eold((size_t)nsys * nlev, 1e300), rn((size_t)nsys * d.nkeep);
+  double best_r = 1e300;
+  int stall = 0, it = 0;
+  bool converged = false;
+  for (it = 0; it < o->max_it; ++it) {
+    if (refine && n0 < ke) {
+      if ((rc = d.hop(d.Pt.d() + n0, M, d.HPt.d() + n0, M, ke - n0, EVR_PREC_FP64, c64, c32))) return rc;
+      if (n1 > ke && (rc = d.hop(d.Pt.d() + ke, M, d.HPt.d() + ke, M, n1 - ke, EVR_PREC_FP32, c64, c32))) return rc;
+    } else if ((rc = d.hop(d.Pt.d() + n0, M, d.HPt.d() + n0, M, n1 - n0, prec, c64, c32))) {
+      return rc;
+    }
+    if ((rc = d.rayleigh_ritz(n0, n1, refine ? ke : 0))) return rc;
+    n0 = n1;
+    const int k = std::min(d.nkeep, n1);
+    // Ritz vectors and their H.psi
+    if ((rc = d.combine(d.Pt.d(), M, n1, d.Wv.d(), M, d.sh, k, d.X.d(), d.nkeep, 1.0, 0.0))) return rc;
+    if ((rc = d.combine(d.HPt.d(), M, n1, d.Wv.d(), M, d.sh, k, d.HX.d(), d.nkeep, 1.0, 0.0))) return rc;
+    if (cudaMemsetAsync(d.nrm.p, 0, sizeof(double) * nsys * k, s)) return set_error(c, EVR_EDEVICE, "memset");
+    batch_residual_kernel<<<c->num_sms * 8, kBT, 0, s>>>(d.X.d(), d.HX.d(), d.nkeep, d.Ev.d(), M, d.sys_d, k, N,
+                                                         d.R.d(), d.nrm.d());
+    if (cudaMemcpyAsync(rn.data(), d.nrm.p, sizeof(double) * nsys * k, cudaMemcpyDeviceToHost, s) ||
+        cudaMemcpyAsync(Eh.data(), d.Ev.p, sizeof(double) * nsys * M, cudaMemcpyDeviceToHost, s) ||
+        cudaStreamSynchronize(s))
+      return set_error(c, EVR_EDEVICE, "evr_batch_davidson: residual norms");
+    const int nt = std::min(nlev, k);
+    double rmax = 0.0;
+    std::vector<std::vector<int>> todo(nsys);
+    size_t most = 0;
+    for (int q = 0; q < nsys; ++q) {
+      for (int j = 0; j < nt; ++j) {
+        const double r = std::sqrt(rn[(size_t)q * k + j]);
+        const double e = Eh[(size_t)q * M + j];
+        const double de = std::fabs(e - Eold[(size_t)q * nlev + j]);
+        Eold[(size_t)q * nlev + j] = e;
+        rmax = std::max(rmax, r);
+        if (!(r < o->conv_resi && de < o->conv_ene)) todo[q].push_back(j);
+      }
+      most = std::max(most, todo[q].size());
+    }
+    if (nt == nlev && most == 0 && (prec == EVR_PREC_FP64 || refine)) {
+      converged = true;
+      break;
+    }
+    if (prec == EVR_PREC_FP32) {
+      double hscale = 0.0;
+      for (int q = 0; q < nsys; ++q)
+        hscale = std::max(hscale, std::max(std::fabs(Eh[(size_t)q * M]), std::fabs(Eh[(size_t)q * M + nt - 1])));
+      const bool floor_hit = !refine && rmax < std::max(o->conv_resi, 1e-4 * hscale);
+      if (rmax < (refine ? 0.7 : 0.5) * best_r) { best_r = rmax; stall = 0; } else ++stall;
+      if (floor_hit || stall >= (refine ? 3 : 1) || (!refine && most == 0)) {
+        const int kr = std::min(k, nlev);
+        if (cudaMemcpy2DAsync(d.Pt.p, sizeof(double) * M, d.X.p, sizeof(double) * d.nkeep, sizeof(double) * kr, N,
+                              cudaMemcpyDeviceToDevice, s) ||
+            cudaMemsetAsync(d.dead.p, 0, (size_t)nsys * M, s))
+          return set_error(c, EVR_EDEVICE, "restart copy");
+        refine = true;
+        ke = kr;
+        n1 = kr;
+        n0 = 0;
+        std::fill(Eold.begin(), Eold.end(), 1e300);
+        best_r = 1e300;
+        stall = 0;
+        continue;
+      }
+    }
+    // new directions: per problem its lowest unconverged levels, filled up with its other
+    // levels so that every problem adds the same number of columns
+    int ns = (int)std::min<size_t>(std::max<size_t>(most, 1), (size_t)d.bmax);
+    if (nt < nlev) ns = std::min(d.bmax, nt);
+    std::vector<int> selh((size_t)nsys * ns);
+    for (int q = 0; q < nsys; ++q) {
+      std::vector<int> lst = todo[q];
+      if (nt < nlev) {
+        lst.clear();
+        for (int j = 0; j < nt; ++j) lst.push_back(j);
+      }
+      for (int j = 0; j < nt && (int)lst.size() < ns; ++j)
+        if (std::find(lst.begin(), lst.end(), j) == lst.end()) lst.push_back(j);
+      for (int j = 0; j < ns; ++j) selh[(size_t)q * ns + j] = lst[(size_t)j % lst.size()];
+    }
+    if (cudaMemcpyAsync(d.sel.p, selh.data(), selh.size() * sizeof(int), cudaMemcpyHostToDevice, s))
+      return set_error(c, EVR_EDEVICE, "copy");
+    batch_precondition_kernel<<<c->num_sms * 8, kBT, 0, s>>>(d.R.d(), d.nkeep, (const int*)d.sel.p, ns, d.Ev.d(), M,
+                                                             c->dp.e0diag, d.sys_d, N, d.T.d(), d.bmax, 1e-6);
+    if (n1 + ns > M) {
+      if (cudaMemcpy2DAsync(d.Pt.p, sizeof(double) * M, d.X.p, sizeof(double) * d.nkeep, sizeof(double) * k, N,
+                            cudaMemcpyDeviceToDevice, s) ||
+          cudaMemcpy2DAsync(d.HPt.p, sizeof(double) * M, d.HX.p, sizeof(double) * d.nkeep, sizeof(double) * k, N,
+                            cudaMemcpyDeviceToDevice, s) ||
+          cudaMemsetAsync(d.dead.p, 0, (size_t)nsys * M, s))
+        return set_error(c, EVR_EDEVICE, "restart copy");
+      batch_diag_kernel<<<nsys, kBT, 0, s>>>(d.Hs.d(), M, d.sh, d.Ev.d(), M, k);
+      n1 = n0 = k;
+      ke = k;
+    }
+    if ((rc = d.orthonormalize(ns, n1))) return rc;
+    n1 += ns;
+  }
+  const int k = std::min(d.nkeep, n1);
+  for (int q = 0; q < nsys; ++q)
+    for (int j = 0; j < nlev; ++j) eig[(size_t)q * nlev + j] = j < k ? Eh[(size_t)q * M + j] : NAN;
+  if (info) {
+    info[0] = it;
+    info[1] = c64;
+    info[2] = c32;
+    info[3] = converged ? 1 : 0;
+  }
+  if (cudaStreamSynchronize(s)) return set_error(c, EVR_EDEVICE, "sync");
+  return converged ? EVR_OK : set_error(c, EVR_ENOCONV, "evr_batch_davidson: not converged in max_it iterations");
+}

@@ -48,10 +48,15 @@ int evr_create(evr_ctx** out, const evr_problem_desc* desc, int device) {
 
 int evr_destroy(evr_ctx* c) {
   if (!c) return EVR_OK;
-  if (c->host_only) { delete c; return EVR_OK; }
+  if (c->host_only) {
+    free_batch_info(c);
+    delete c;
+    return EVR_OK;
+  }
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_control(c);
+  free_batch_info(c);
   free_workspace(c);
   free_problem(c);
   if (c->pinned) cudaFreeHost(c->pinned);

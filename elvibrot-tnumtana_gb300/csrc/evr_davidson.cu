@@ -13,10 +13,16 @@
 // interleaved layout (row k of the N x ld block holds component k of every vector), so
 // the projections are cuBLAS DGEMMs on the column-major transposes.
 //
-// Mixed precision (prec = EVR_PREC_FP32): the iteration runs with FP32 contractions in
-// H.psi; when the residuals reach the FP32 floor (or stop decreasing) the Ritz vectors
-// are kept, H.psi of the whole subspace is recomputed in FP64 and the iteration continues
-// in FP64 until the requested tolerances hold for the FP64 operator.
+// Mixed precision (prec = EVR_PREC_FP32): the iteration first runs with FP32 contractions
+// in H.psi.  When the residuals reach the FP32 floor (or stop decreasing) the subspace is
+// collapsed to the n_levels Ritz vectors and only those get an FP64 H.psi.  The iteration
+// then goes on with FP32 H.psi for the new directions, while every projected-matrix entry
+// that pairs a new direction with one of the FP64 columns is taken from the FP64 side,
+// <H psi_exact | t> (H, or (H + H^T)/2, is symmetric): the FP32 error then enters only
+// through the components of the Ritz vectors along the new directions, which are of the
+// size of the residual at the switch, so the residuals and eigenvalues converge below the
+// FP32 floor to the FP64 operator's.  A restart keeps the Ritz vectors and their H.psi as
+// FP64 columns; a stall of the refinement recomputes them in FP64.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -267,9 +273,12 @@ struct Davidson {
   }
 
   // Projected matrix rows/cols n0..n1, eigen-decomposition of the leading n1 x n1 block.
-  int rayleigh_ritz(int n0, int n1, std::vector<double>& Eh) {
+  // Columns 0..ke-1 carry an FP64 H.psi: their rows of the new block are <H psi_i|psi_j>.
+  int rayleigh_ritz(int n0, int n1, std::vector<double>& Eh, int ke = 0) {
     int rc = gram(Pt.p, M, HPt.p + n0, M, n1, n1 - n0, Hs.p + (size_t)M * n0, M);  // Hs(0:n1, n0:n1)
     if (rc) return rc;
+    const int kx = std::min(ke, n0);
+    if (kx > 0 && (rc = gram(HPt.p, M, Pt.p + n0, M, kx, n1 - n0, Hs.p + (size_t)M * n0, M))) return rc;
     // mirror the new columns into the new rows: Hs(n0:n1, 0:n0) = Hs(0:n0, n0:n1)^T
     const double one = 1.0, zero = 0.0;
     if (n0 > 0 && cublasDgeam(blas, CUBLAS_OP_T, CUBLAS_OP_N, n1 - n0, n0, &one, Hs.p + (size_t)M * n0, M, &zero,
@@ -360,10 +369,17 @@ extern "C" int evr_davidson(evr_ctx* c, const evr_davidson_opts* o, const double
   double best_r = 1e300;
   int stall = 0, it = 0;
   bool converged = false;
+  bool refine = false;  // mixed precision after the switch: FP64 columns 0..ke-1, FP32 H.psi for the others
+  int ke = 0;
   for (it = 0; it < o->max_it; ++it) {
-    // H.psi of the new vectors
-    if ((rc = d.hop(d.Pt.p + n0, M, d.HPt.p + n0, M, n1 - n0, prec, cnt64, cnt32))) return rc;
-    if ((rc = d.rayleigh_ritz(n0, n1, Eh))) return rc;
+    // H.psi of the new vectors (FP64 for the columns a switch or refresh marked exact)
+    if (refine && n0 < ke) {
+      if ((rc = d.hop(d.Pt.p + n0, M, d.HPt.p + n0, M, ke - n0, EVR_PREC_FP64, cnt64, cnt32))) return rc;
+      if (n1 > ke && (rc = d.hop(d.Pt.p + ke, M, d.HPt.p + ke, M, n1 - ke, EVR_PREC_FP32, cnt64, cnt32))) return rc;
+    } else if ((rc = d.hop(d.Pt.p + n0, M, d.HPt.p + n0, M, n1 - n0, prec, cnt64, cnt32))) {
+      return rc;
+    }
+    if ((rc = d.rayleigh_ritz(n0, n1, Eh, refine ? ke : 0))) return rc;
     n0 = n1;
     const int k = std::min(d.nkeep, n1);
     // Ritz vectors and H applied to them
@@ -390,23 +406,28 @@ extern "C" int evr_davidson(evr_ctx* c, const evr_davidson_opts* o, const double
     }
     for (int j = 0; j < nt; ++j) Eold[j] = Eh[j];
     if (nt == nlev && todo.empty()) {
-      if (prec == EVR_PREC_FP64) {
+      if (prec == EVR_PREC_FP64 || refine) {
         converged = true;
         break;
       }
     }
-    // FP32 -> FP64 switch: residual floor of the FP32 operator reached or stalled
+    // FP32 phase -> refinement: residual floor of the FP32 operator reached or stalled;
+    // in the refinement a stall recomputes the Ritz vectors' H.psi in FP64
     if (prec == EVR_PREC_FP32) {
+      // the refinement converges at the rate of the FP64 iteration, so the FP32 phase ends
+      // early: at a residual of 1e-4 of the level energies or when it stops halving
       const double hscale = std::max(std::fabs(Eh.front()), std::fabs(Eh.back()));
-      const bool floor_hit = rmax < std::max(o->conv_resi, 2e-6 * hscale);
-      if (rmax < 0.7 * best_r) { best_r = rmax; stall = 0; } else ++stall;
-      if (floor_hit || stall >= 4 || todo.empty()) {
-        // restart on the Ritz vectors with FP64 H.psi
-        if (cudaMemcpy2DAsync(d.Pt.p, sizeof(double) * M, d.X.p, sizeof(double) * d.nkeep, sizeof(double) * k, N,
+      const bool floor_hit = !refine && rmax < std::max(o->conv_resi, 1e-4 * hscale);
+      if (rmax < (refine ? 0.7 : 0.5) * best_r) { best_r = rmax; stall = 0; } else ++stall;
+      if (floor_hit || stall >= (refine ? 3 : 1) || (!refine && todo.empty())) {
+        // restart on the lowest n_levels Ritz vectors, H.psi of those in FP64
+        const int kr = std::min(k, nlev);
+        if (cudaMemcpy2DAsync(d.Pt.p, sizeof(double) * M, d.X.p, sizeof(double) * d.nkeep, sizeof(double) * kr, N,
                               cudaMemcpyDeviceToDevice, s))
           return set_error(c, EVR_EDEVICE, "restart copy");
-        prec = EVR_PREC_FP64;
-        n1 = k;
+        refine = true;
+        ke = kr;
+        n1 = kr;
         n0 = 0;
         std::fill(Eold.begin(), Eold.end(), 1e300);
         best_r = 1e300;
@@ -442,6 +463,7 @@ extern "C" int evr_davidson(evr_ctx* c, const evr_davidson_opts* o, const double
           return set_error(c, EVR_EDEVICE, "copy");
       if (cudaStreamSynchronize(s)) return set_error(c, EVR_EDEVICE, "sync");
       n1 = n0 = k;
+      ke = k;  // Ritz vectors and their H.psi: FP64 columns of the refinement
     }
     if ((rc = d.orthonormalize(d.T.p, ns, n1, added))) return rc;
     if (added == 0) break;  // no new direction: converged as far as the operator allows

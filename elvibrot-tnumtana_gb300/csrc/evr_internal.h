@@ -49,6 +49,8 @@ struct TermDesc {
   // (basis <- grid), padded like the others
   int32_t m_x1L, m_x2L, m_e1L, m_e2L;
   int32_t msz;           // elements of the term's 1-D matrices staged in shared memory
+  int32_t D;             // modes of the term's problem
+  int32_t g0off, goff;   // offsets of the problem's G0 (D*D) and g (D*D*D) in the coefficient arrays
   int32_t pad_;
   double weight;
 };
@@ -179,6 +181,8 @@ struct evr_ctx {
   bool capturing = false;           // inside a stream capture: no event records
   bool use_slab = true;             // slab kernel for the terms that fit (EVR_NO_SLAB=1 disables)
   bool use_stages = true;           // grid-wide stage path for single-term problems
+  bool gfly = false;                // G(Q) from the linear model per point instead of a table
+  int n_sys = 1;                    // problems stacked in this context (evr_create_batch)
   cudaStream_t stream = nullptr;
   evr::HostProblem hp;
   evr::DeviceProblem dp;
@@ -195,6 +199,7 @@ struct evr_ctx {
   evr::StageBuffers stg;
   evr::OpExtras field;             // grid-operator extras of evr_hpsi_* / Davidson / Chebyshev (evr_set_field)
   void* oc = nullptr;              // optimal-control state (evr_control.cu)
+  void* batch = nullptr;           // stacked problems (evr_batch.cu)
   // host staging for the host-pointer entry points
   double* pinned = nullptr;
   size_t pinned_bytes = 0;
@@ -223,6 +228,7 @@ int hpsi_stages(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy
                 cudaStream_t s, int op, const OpExtras& ex);
 void free_stages(evr_ctx* c);
 void free_control(evr_ctx* c);
+void free_batch_info(evr_ctx* c);
 // weighted CSR reduction of the term-basis output(s) into y (evr_kernels.cu)
 int reduce_terms(evr_ctx* c, int prec, const void* ht, const void* ht2, int nvec, double scale, double* y,
                  int64_t ldy, cudaStream_t s);

@@ -1,0 +1,36 @@
+// evr_kern_inst.cuh -- instantiation of one term kernel (EVR_KSLAB: slab-streaming or
+// general) for one (type, G source) pair; included by the evr_kern_*.cu units, which are
+// compiled in parallel.
+#include "evr_kernels_impl.cuh"
+
+namespace evr {
+namespace kern {
+
+#if EVR_KSLAB
+template <typename T, bool GFLY>
+cudaError_t launch_slab_kernel(int grid, size_t smem, cudaStream_t s, const ItemParams<T>& p) {
+  hpsi_slab_kernel<T, GFLY><<<grid, kSlabThreads, smem, s>>>(p);
+  return cudaGetLastError();
+}
+template <typename T, bool GFLY>
+cudaError_t set_slab_kernel_smem(int bytes) {
+  return cudaFuncSetAttribute(hpsi_slab_kernel<T, GFLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+template cudaError_t launch_slab_kernel<EVR_KT, EVR_KGFLY>(int, size_t, cudaStream_t, const ItemParams<EVR_KT>&);
+template cudaError_t set_slab_kernel_smem<EVR_KT, EVR_KGFLY>(int);
+#else
+template <typename T, bool GFLY>
+cudaError_t launch_items_kernel(int grid, size_t smem, cudaStream_t s, const ItemParams<T>& p) {
+  hpsi_items_kernel<T, GFLY><<<grid, kThreads, smem, s>>>(p);
+  return cudaGetLastError();
+}
+template <typename T, bool GFLY>
+cudaError_t set_items_kernel_smem(int bytes) {
+  return cudaFuncSetAttribute(hpsi_items_kernel<T, GFLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+template cudaError_t launch_items_kernel<EVR_KT, EVR_KGFLY>(int, size_t, cudaStream_t, const ItemParams<EVR_KT>&);
+template cudaError_t set_items_kernel_smem<EVR_KT, EVR_KGFLY>(int);
+#endif
+
+}  // namespace kern
+}  // namespace evr

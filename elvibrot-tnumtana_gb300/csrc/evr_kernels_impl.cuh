@@ -1,0 +1,919 @@
+// evr_kernels_impl.cuh -- device code of the term kernels (general and slab-streaming),
+// shared by the translation units that instantiate them (evr_kern_<type><gfly>.cu, one
+// per precision and G-source variant, compiled in parallel) and by the host code of
+// evr_kernels.cu, which only needs the parameter block and the launchers.
+#pragma once
+#include <algorithm>
+#include <cstdio>
+
+#include "evr_internal.h"
+
+namespace evr {
+namespace kern {
+
+constexpr int kThreads = 256;
+
+template <typename T>
+struct ItemParams {
+  const TermDesc* terms;
+  const T* mats;
+  const T* vgrid;
+  const T* ggrid;          // SoA symmetric G per term grid point, or nullptr (G constant)
+  const double* G0;        // D*D per problem, at the term's g0off (used when ggrid == nullptr)
+  const double* gco;       // g_ijk per problem at the term's goff: G(Q) = G0 + g.Q evaluated per point
+                           // (problems without a G table: gfly != 0)
+  int gfly;
+  const int* map;
+  const WorkItem* items;
+  int n_items;
+  int* counter;
+  T* slab;
+  int64_t slab_per_cta;
+  const double* x;         // interleaved input (FP64)
+  int64_t ldx;
+  T* ht;                   // term-basis output
+  int64_t ldh;
+  int64_t Np;
+  int D, nb0, keo_type;
+  int has_offdiag;         // type 1 with off-diagonal F2 terms
+  int vtrans;              // 1: V_ab read as V_ba (transposed operator)
+  int implicit_nvec;       // > 0: items are implicit, item = term * implicit_nvec + vector, one
+                           // vector each, buffers in the global slab (items == nullptr)
+  // grid operator extras: pot = vw*V + mw*mu when mugrid != nullptr (mw read from mu_dev
+  // when that is set); keo_on = 0 drops the kinetic part
+  const T* mugrid;
+  T vw, mw;
+  const double* mu_dev;
+  int keo_on;
+};
+
+// plain H: no dipole term, kinetic part on
+template <typename T>
+void set_plain(ItemParams<T>& p) {
+  p.mugrid = nullptr;
+  p.gco = nullptr;
+  p.gfly = 0;
+  p.vw = T(1);
+  p.mw = T(0);
+  p.mu_dev = nullptr;
+  p.keo_on = 1;
+}
+
+constexpr int kSlabThreads = 512;
+
+// out(a, m, b, v) = alpha * sum_k mat[m + M*k] * in(a, k, b, v)  (+ out if acc)
+// element (a, k, b, v) of a tensor with vector stride ld lives at ((a + A*(k + K*b))*ld + v).
+// four consecutive matrix coefficients (staged in shared memory) in one 16-byte load
+__device__ __forceinline__ void load4(const float* p, float& a, float& b, float& c, float& d) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  a = v.x; b = v.y; c = v.z; d = v.w;
+}
+__device__ __forceinline__ void load4(const double* p, double& a, double& b, double& c, double& d) {
+  const double2 u = reinterpret_cast<const double2*>(p)[0];
+  const double2 w = reinterpret_cast<const double2*>(p)[1];
+  a = u.x; b = u.y; c = w.x; d = w.y;
+}
+
+// acc[m] += mat[m + ldm*k] * xk for m < M; the matrix columns are padded to ldm = 4*ceil(M/4)
+template <typename T, int MAXM>
+__device__ __forceinline__ void fma_column(T (&accv)[MAXM], const T* __restrict__ mk, T xk, int M) {
+#pragma unroll
+  for (int m4 = 0; m4 < MAXM; m4 += 4)
+    if (m4 < M) {
+      T c0, c1, c2, c3;
+      load4(mk + m4, c0, c1, c2, c3);
+      accv[m4] = fma(c0, xk, accv[m4]);
+      accv[m4 + 1] = fma(c1, xk, accv[m4 + 1]);
+      accv[m4 + 2] = fma(c2, xk, accv[m4 + 2]);
+      accv[m4 + 3] = fma(c3, xk, accv[m4 + 3]);
+    }
+}
+
+// Division by a loop-invariant divisor d >= 1 for 0 <= n < 2^31 with one multiply-high:
+// q = (umulhi(m, n) + n) >> l, l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1.
+struct FastDiv {
+  uint32_t d, m, l;
+  __device__ __forceinline__ explicit FastDiv(uint32_t dd) : d(dd), l(0) {
+    while ((1u << l) < d) ++l;
+    m = (uint32_t)((((uint64_t)1 << 32) * (((uint64_t)1 << l) - d)) / d + 1);
+  }
+  __device__ __forceinline__ uint32_t div(uint32_t n) const { return (__umulhi(m, n) + n) >> l; }
+};
+
+// Matrix-stationary contraction: a thread owns MG consecutive output rows m0.. of the 1-D
+// matrix (held in registers) and one (a, v) lane, and walks the B dimension; each step
+// loads the K inputs of one fibre and issues MG*K FMAs.  Lanes are (a, v, row group);
+// when there are fewer lanes than threads the B dimension is split among them.
+template <typename T, int MAXK, int MG>
+__device__ __forceinline__ void contract_ms(const T* __restrict__ in, int64_t ldi, T* __restrict__ out, int64_t ldo,
+                                            int A, int K, int M, int B, int Vt, const T* __restrict__ mat, T alpha,
+                                            bool acc) {
+  const int ldm = (M + 3) & ~3;
+  const int nmg = (M + MG - 1) / MG;
+  const int AV = A * Vt;
+  const int lanes = AV * nmg;
+  const int nthr = blockDim.x;
+  int nbg = nthr / lanes;  // B groups when lanes < threads
+  if (nbg < 1) nbg = 1;
+  if (nbg > B) nbg = B;
+  const int tasks = lanes * nbg;
+  const FastDiv dvt((uint32_t)Vt), dlanes((uint32_t)lanes), dav((uint32_t)AV);
+  const int64_t istr = (int64_t)A * ldi, ostr = (int64_t)A * ldo;
+  for (int task = threadIdx.x; task < tasks; task += nthr) {
+    const int bg = (int)dlanes.div((uint32_t)task);
+    const int lane = task - bg * lanes;
+    const int mg = (int)dav.div((uint32_t)lane);
+    const int av = lane - mg * AV;
+    const int a = (int)dvt.div((uint32_t)av);
+    const int v = av - a * Vt;
+    const int m0 = mg * MG;
+    T strip[MG][MAXK];
+#pragma unroll
+    for (int mm = 0; mm < MG; ++mm)
+#pragma unroll
+      for (int k = 0; k < MAXK; ++k)
+        strip[mm][k] = (k < K && m0 + mm < M) ? mat[(m0 + mm) + ldm * k] : T(0);
+    const T* ip = in + (int64_t)a * ldi + v + (int64_t)bg * K * istr;
+    T* op = out + (int64_t)a * ldo + v + (int64_t)m0 * ostr + (int64_t)bg * M * ostr;
+    const int64_t istep = (int64_t)nbg * K * istr, ostep = (int64_t)nbg * M * ostr;
+    for (int b = bg; b < B; b += nbg, ip += istep, op += ostep) {
+      T x[MAXK];
+#pragma unroll
+      for (int k = 0; k < MAXK; ++k) x[k] = (k < K) ? ip[k * istr] : T(0);
+#pragma unroll
+      for (int mm = 0; mm < MG; ++mm) {
+        T s = T(0);
+#pragma unroll
+        for (int k = 0; k < MAXK; ++k)
+          if (k < K) s = fma(strip[mm][k], x[k], s);
+        if (m0 + mm < M) {
+          T val = alpha * s;
+          if (acc) val += op[mm * ostr];
+          op[mm * ostr] = val;
+        }
+      }
+    }
+  }
+}
+
+// Loads of a fibre are issued four at a time so that each thread keeps several memory
+// requests in flight before the FMAs that consume them; in FP32 a thread carries two
+// columns so that every matrix load feeds eight FMAs.
+template <typename T, int MAXM, int COLS>
+__device__ __forceinline__ void contract_m(const T* __restrict__ in, int64_t ldi, T* __restrict__ out, int64_t ldo,
+                                           int A, int K, int M, int B, int Vt, const T* __restrict__ mat, T alpha,
+                                           bool acc) {
+  const int ncol = A * B * Vt;
+  const int ldm = (M + 3) & ~3;
+  const FastDiv dv((uint32_t)Vt), da((uint32_t)A);
+  const int64_t istr = (int64_t)A * ldi, ostr = (int64_t)A * ldo;
+  for (int col0 = threadIdx.x; col0 < ncol; col0 += COLS * blockDim.x) {
+    const T* ip[COLS];
+    T* op[COLS];
+    bool on[COLS];
+#pragma unroll
+    for (int c = 0; c < COLS; ++c) {
+      const int col = col0 + c * blockDim.x;
+      on[c] = col < ncol;
+      const int cc = on[c] ? col : col0;
+      const int r = (int)dv.div((uint32_t)cc);
+      const int v = cc - r * Vt;
+      const int b = (int)da.div((uint32_t)r);
+      const int a = r - b * A;
+      ip[c] = in + (int64_t)(a + (int64_t)A * K * b) * ldi + v;
+      op[c] = out + (int64_t)(a + (int64_t)A * M * b) * ldo + v;
+    }
+    T accv[COLS][MAXM];
+#pragma unroll
+    for (int c = 0; c < COLS; ++c)
+#pragma unroll
+      for (int m = 0; m < MAXM; ++m) accv[c][m] = T(0);
+    for (int k0 = 0; k0 < K; k0 += 4) {
+      T x[COLS][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int c = 0; c < COLS; ++c) x[c][j] = (k0 + j < K) ? ip[c][(k0 + j) * istr] : T(0);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (k0 + j < K) {
+          const T* mk = mat + ldm * (k0 + j);
+#pragma unroll
+          for (int m4 = 0; m4 < MAXM; m4 += 4)
+            if (m4 < M) {
+              T c0, c1, c2, c3;
+              load4(mk + m4, c0, c1, c2, c3);
+#pragma unroll
+              for (int c = 0; c < COLS; ++c) {
+                accv[c][m4] = fma(c0, x[c][j], accv[c][m4]);
+                accv[c][m4 + 1] = fma(c1, x[c][j], accv[c][m4 + 1]);
+                accv[c][m4 + 2] = fma(c2, x[c][j], accv[c][m4 + 2]);
+                accv[c][m4 + 3] = fma(c3, x[c][j], accv[c][m4 + 3]);
+              }
+            }
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < COLS; ++c)
+      if (on[c])
+#pragma unroll
+        for (int m = 0; m < MAXM; ++m)
+          if (m < M) {
+            T val = alpha * accv[c][m];
+            if (acc) val += op[c][m * ostr];
+            op[c][m * ostr] = val;
+          }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64_t ldo, int A, int K, int M, int B,
+                                         int Vt, const T* mat, T alpha, bool acc) {
+  if constexpr (sizeof(T) == 4) {  // FP32: two columns per thread, matrix coefficients from shared memory
+    if (M <= 4) contract_m<T, 4, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (M <= 8) contract_m<T, 8, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (M <= 12) contract_m<T, 12, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (M <= 16) contract_m<T, 16, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (M <= 20) contract_m<T, 20, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else contract_m<T, 24, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  } else {  // FP64: matrix strip in registers (register budget MG*MAXK <= 24 doubles)
+    if (K <= 4) contract_ms<T, 4, 4>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (K <= 8) contract_ms<T, 8, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (K <= 12) contract_ms<T, 12, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (K <= 16) contract_ms<T, 16, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (K <= 20) contract_ms<T, 20, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else contract_ms<T, 24, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  }
+}
+
+// First B->G mode fused with the gather from the packed vector block:
+// in(k, b, v) = x[(map[off_nb + k + K*b] + Np*e) * ldx + v0 + v]  (0 when excluded)
+template <typename T, int MAXM>
+__device__ __forceinline__ void gather_contract_m(const double* __restrict__ x, int64_t ldx, const int* __restrict__ mp,
+                                                  int64_t eoff, T* __restrict__ out, int K, int M, int B, int Vt,
+                                                  const T* __restrict__ mat) {
+  const int ncol = B * Vt;
+  const int ldm = (M + 3) & ~3;
+  const FastDiv dv((uint32_t)Vt);
+  for (int col = threadIdx.x; col < ncol; col += blockDim.x) {
+    const int b = (int)dv.div((uint32_t)col);
+    const int v = col - b * Vt;
+    T accv[MAXM];
+#pragma unroll
+    for (int m = 0; m < MAXM; ++m) accv[m] = T(0);
+    for (int k0 = 0; k0 < K; k0 += 4) {
+      int pk[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) pk[j] = (k0 + j < K) ? __ldg(mp + k0 + j + K * b) : -1;
+      T xv[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) xv[j] = (pk[j] >= 0) ? (T)__ldg(x + (pk[j] + eoff) * ldx + v) : T(0);
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (k0 + j < K) fma_column<T, MAXM>(accv, mat + ldm * (k0 + j), xv[j], M);
+    }
+    T* op = out + (int64_t)M * b * Vt + v;
+#pragma unroll
+    for (int m = 0; m < MAXM; ++m)
+      if (m < M) op[(int64_t)m * Vt] = accv[m];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void gather_contract(const double* x, int64_t ldx, const int* mp, int64_t eoff, T* out,
+                                                int K, int M, int B, int Vt, const T* mat) {
+  if (M <= 4) gather_contract_m<T, 4>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+  else if (M <= 8) gather_contract_m<T, 8>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+  else if (M <= 12) gather_contract_m<T, 12>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+  else if (M <= 16) gather_contract_m<T, 16>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+  else if (M <= 20) gather_contract_m<T, 20>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+  else gather_contract_m<T, 24>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
+}
+
+// Copies the item's 1-D matrices from the global pool into shared memory (the layout of
+// term_matrix_elems) and points the shared TermDesc's offsets at the copies, so that every
+// contraction reads its coefficients from shared memory instead of a small, easily evicted
+// L1.
+struct StageBlocks {
+  int src[4 * kMaxD + 3], dst[4 * kMaxD + 3], n[4 * kMaxD + 3];
+  int count;
+};
+
+template <typename T>
+__device__ __forceinline__ void stage_matrices(TermDesc& Tm, int D, const T* __restrict__ pool, T* msm,
+                                               StageBlocks& sb) {
+  if (threadIdx.x == 0) {
+    int o = 0, c = 0;
+    auto add = [&](int32_t& off, int n) {
+      sb.src[c] = off;
+      sb.dst[c] = o;
+      sb.n[c] = n;
+      off = o;
+      o += n;
+      ++c;
+    };
+    for (int q = 0; q < D; ++q) {
+      add(Tm.m_d0b[q], mat_block(Tm.nq[q], Tm.nb[q]));
+      add(Tm.m_bgw[q], mat_block(Tm.nb[q], Tm.nq[q]));
+      add(Tm.m_d1[q], mat_block(Tm.nq[q], Tm.nq[q]));
+      add(Tm.m_d2[q], mat_block(Tm.nq[q], Tm.nq[q]));
+    }
+    const int L = D - 1;
+    add(Tm.m_x1L, mat_block(Tm.nq[L], Tm.nb[L]));
+    add(Tm.m_e1L, mat_block(Tm.nb[L], Tm.nq[L]));
+    add(Tm.m_e2L, mat_block(Tm.nb[L], Tm.nq[L]));
+    sb.count = c;
+  }
+  __syncthreads();
+  for (int b = 0; b < sb.count; ++b) {
+    const T* src = pool + sb.src[b];
+    T* dst = msm + sb.dst[b];
+    for (int i = threadIdx.x; i < sb.n[b]; i += blockDim.x) dst[i] = __ldg(src + i);
+  }
+  __syncthreads();
+}
+
+// Coordinates of a term grid point: positions 0..npos-1 from the index r (first position
+// fastest), the others left to the caller.
+template <typename T, int DM>
+__device__ __forceinline__ void point_coords(const ItemParams<T>& p, const TermDesc& Tm, int r, int npos,
+                                             double (&xq)[DM]) {
+#pragma unroll
+  for (int k = 0; k < DM; ++k)
+    if (k < npos) {
+      const int n = Tm.nq[k];
+      const int i = r % n;
+      r /= n;
+      xq[k] = (double)p.mats[Tm.m_x[k] + i];
+    } else {
+      xq[k] = 0.0;
+    }
+}
+
+// G_ij(Q) = G0_ij + sum_k g_ijk Q_k at a point with coordinates xq (positions i, j, k of the
+// term's mode order), for problems without a G table
+template <typename T, int DM>
+__device__ __forceinline__ T g_model(const ItemParams<T>& p, const TermDesc& Tm, const double (&xq)[DM], int i,
+                                     int j) {
+  const int D = Tm.D, oi = Tm.perm[i], oj = Tm.perm[j];
+  double s = __ldg(p.G0 + Tm.g0off + oi + D * oj);
+  const double* gp = p.gco + Tm.goff + oi + D * oj;
+#pragma unroll
+  for (int k = 0; k < DM; ++k)
+    if (k < D) s = fma(__ldg(gp + D * D * Tm.perm[k]), xq[k], s);
+  return (T)s;
+}
+
+// Y[i] <- sum_j G_ij(Q) Y[j] on the whole term grid (general kernel).  A thread owns a grid
+// point and a residue class of the tile's vectors (several classes per point when the
+// grid has fewer points than the CTA has threads); G(Q) is held in registers for D <= 6
+// (FP64) or 8 (FP32) and applied to the thread's vectors.
+template <typename T, int DM, bool GFLY>
+__device__ __forceinline__ void items_pointwise_G(const ItemParams<T>& p, const TermDesc& Tm, T* Y, int64_t stride,
+                                                  int Vt, int NQ) {
+  const int D = Tm.D;
+  const int nG = D * (D + 1) / 2;
+  constexpr bool kCache = DM <= (sizeof(T) == 4 ? 8 : 6);
+  constexpr int kG = kCache ? DM * (DM + 1) / 2 : 1;
+  const int nch = max(1, min(Vt, (int)blockDim.x / max(NQ, 1)));
+  auto slot = [D](int i, int j) { return i * D - i * (i - 1) / 2 + (j - i); };
+  for (int task = threadIdx.x; task < NQ * nch; task += blockDim.x) {
+    const int q = task / nch, ch = task - q * nch;
+    const T* Gp = p.ggrid ? p.ggrid + Tm.off_nq * nG + q : nullptr;
+    double xq[DM];
+    if constexpr (GFLY) point_coords<T, DM>(p, Tm, q, D, xq);
+    auto gget = [&](int i, int j) -> T {
+      if (i >= D || j >= D) return T(0);
+      if constexpr (GFLY) return g_model<T, DM>(p, Tm, xq, i, j);
+      return Gp ? __ldg(Gp + (int64_t)slot(i, j) * NQ) : (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[j]);
+    };
+    T G[kG];
+    if constexpr (kCache) {
+#pragma unroll
+      for (int i = 0; i < DM; ++i)
+#pragma unroll
+        for (int j = i; j < DM; ++j) G[i * DM - i * (i - 1) / 2 + (j - i)] = gget(i, j);
+    }
+    for (int v = ch; v < Vt; v += nch) {
+      const int64_t idx = (int64_t)q * Vt + v;
+      T y[DM], z[DM];
+#pragma unroll
+      for (int j = 0; j < DM; ++j) {
+        y[j] = (j < D) ? Y[j * stride + idx] : T(0);
+        z[j] = T(0);
+      }
+#pragma unroll
+      for (int i = 0; i < DM; ++i)
+#pragma unroll
+        for (int j = i; j < DM; ++j) {
+          T gij;
+          if constexpr (kCache) gij = G[i * DM - i * (i - 1) / 2 + (j - i)];
+          else gij = gget(i, j);
+          z[i] = fma(gij, y[j], z[i]);
+          if (j != i) z[j] = fma(gij, y[i], z[j]);
+        }
+#pragma unroll
+      for (int i = 0; i < DM; ++i)
+        if (i < D) Y[i * stride + idx] = z[i];
+    }
+  }
+}
+
+template <typename T, bool GFLY>
+__global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  __shared__ TermDesc s_term;
+  __shared__ StageBlocks s_blocks;
+  const int nb0 = p.nb0;
+  while (true) {
+    if (threadIdx.x == 0) s_item = atomicAdd(p.counter, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= p.n_items) break;
+    WorkItem w;
+    if (p.implicit_nvec > 0) {
+      w.term = it / p.implicit_nvec;
+      w.v0 = it - w.term * p.implicit_nvec;
+      w.vt = 1;
+      w.smem = 0;
+    } else {
+      w = p.items[it];
+    }
+    {
+      const int* src = reinterpret_cast<const int*>(p.terms + w.term);
+      int* dst = reinterpret_cast<int*>(&s_term);
+      for (int i = threadIdx.x; i < (int)(sizeof(TermDesc) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const int D = s_term.D;
+    T* const mb = reinterpret_cast<T*>(smem_raw);
+    stage_matrices<T>(s_term, D, p.mats, mb, s_blocks);
+    const TermDesc& Tm = s_term;
+    const int NQ = Tm.NQ, NB = Tm.NB, Vt = w.vt;
+    const int mpad = (Tm.msz + 3) & ~3;
+    T* buf = w.smem ? reinterpret_cast<T*>(smem_raw) + mpad : p.slab + (int64_t)blockIdx.x * p.slab_per_cta;
+    const int64_t stride = (int64_t)NQ * Vt;
+    T* X0 = buf;                     // psi on the grid, nb0 components
+    T* X1 = buf + nb0 * stride;      // H.psi accumulator, nb0 components
+    T* Y = buf + 2 * nb0 * stride;   // derivative arrays
+
+    // ---- gather + B->G (modes 0..D-1), ping-pong between X0[e] and X1[e]
+    for (int e = 0; e < nb0; ++e) {
+      T* A0 = X0 + e * stride;
+      T* A1 = X1 + e * stride;
+      T* cur = (D % 2) ? A0 : A1;   // so that the chain ends in A0
+      int nb_rest = NB / Tm.nb[0];
+      gather_contract<T>(p.x + w.v0, p.ldx, p.map + Tm.off_nb, p.Np * e, cur, Tm.nb[0], Tm.nq[0], nb_rest, Vt,
+                         mb + Tm.m_d0b[0]);
+      __syncthreads();
+      int A = Tm.nq[0];
+      for (int i = 1; i < D; ++i) {
+        nb_rest /= Tm.nb[i];
+        T* nxt = (cur == A0) ? A1 : A0;
+        contract<T>(cur, Vt, nxt, Vt, A, Tm.nb[i], Tm.nq[i], nb_rest, Vt, mb + Tm.m_d0b[i], T(1), false);
+        __syncthreads();
+        cur = nxt;
+        A *= Tm.nq[i];
+      }
+    }
+
+    // ---- V.psi: X1[a] = sum_b V_ab X0[b]   (V -> vw V + mw mu with a dipole term)
+    {
+      const T* Vt_ = p.vgrid + Tm.off_nq * nb0 * nb0;
+      const T* Mu_ = p.mugrid ? p.mugrid + Tm.off_nq * nb0 * nb0 : nullptr;
+      const T mw = p.mu_dev ? (T)__ldg(p.mu_dev) : p.mw;
+      const int64_t n = stride;
+      for (int64_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
+        const int q = (int)(idx / Vt);
+        for (int a = 0; a < nb0; ++a) {
+          T s = T(0);
+          for (int b = 0; b < nb0; ++b) {
+            const int ab = p.vtrans ? (b + nb0 * a) : (a + nb0 * b);
+            T vab = __ldg(Vt_ + (int64_t)ab * NQ + q);
+            if (Mu_) vab = fma(mw, __ldg(Mu_ + (int64_t)ab * NQ + q), p.vw * vab);
+            s = fma(vab, X0[b * stride + idx], s);
+          }
+          X1[a * stride + idx] = s;
+        }
+      }
+      __syncthreads();
+    }
+
+    // ---- KEO
+    if (!p.keo_on) {
+    } else if (p.keo_type == 10) {
+      for (int e = 0; e < nb0; ++e) {
+        const T* P0 = X0 + e * stride;
+        T* Acc = X1 + e * stride;
+        int A = 1, Bq = NQ;
+        for (int j = 0; j < D; ++j) {  // Y[j] = d1_j . psi_G
+          Bq /= Tm.nq[j];
+          contract<T>(P0, Vt, Y + j * stride, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, mb + Tm.m_d1[j], T(1), false);
+          A *= Tm.nq[j];
+        }
+        __syncthreads();
+        // Y[i] <- sum_j G_ij(q) Y[j]
+        if (D <= 4) items_pointwise_G<T, 4, GFLY>(p, Tm, Y, stride, Vt, NQ);
+        else if (D <= 6) items_pointwise_G<T, 6, GFLY>(p, Tm, Y, stride, Vt, NQ);
+        else if (D <= 8) items_pointwise_G<T, 8, GFLY>(p, Tm, Y, stride, Vt, NQ);
+        else items_pointwise_G<T, 16, GFLY>(p, Tm, Y, stride, Vt, NQ);
+        __syncthreads();
+        A = 1; Bq = NQ;
+        for (int i = 0; i < D; ++i) {  // Acc += -1/2 d1_i . Y[i]; same-fibre updates per mode
+          Bq /= Tm.nq[i];
+          contract<T>(Y + i * stride, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d1[i], T(-0.5), true);
+          __syncthreads();
+          A *= Tm.nq[i];
+        }
+      }
+    } else {
+      // type 1: Acc += F2_ii d2_i psi + sum_{i<j} F2_ij d1_i d1_j psi, F2 = -G0/2 (diag), -G0 (off)
+      for (int e = 0; e < nb0; ++e) {
+        const T* P0 = X0 + e * stride;
+        T* Acc = X1 + e * stride;
+        int A = 1, Bq = NQ;
+        for (int i = 0; i < D; ++i) {
+          Bq /= Tm.nq[i];
+          const T f = (T)(-0.5 * __ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[i]));
+          if (f != T(0))
+            contract<T>(P0, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d2[i], f, true);
+          __syncthreads();
+          A *= Tm.nq[i];
+        }
+        if (p.has_offdiag) {
+          int Ai = 1;
+          for (int i = 0; i < D; ++i) {
+            const int Bi = NQ / (Ai * Tm.nq[i]);
+            int Aj = Ai * Tm.nq[i];
+            for (int j = i + 1; j < D; ++j) {
+              const int Bj = NQ / (Aj * Tm.nq[j]);
+              const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[j]));
+              if (f != T(0)) {
+                contract<T>(P0, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, mb + Tm.m_d1[i], T(1), false);
+                __syncthreads();
+                contract<T>(Y, Vt, Acc, Vt, Aj, Tm.nq[j], Tm.nq[j], Bj, Vt, mb + Tm.m_d1[j], f, true);
+                __syncthreads();
+              }
+              Aj *= Tm.nq[j];
+            }
+            Ai *= Tm.nq[i];
+          }
+        }
+      }
+    }
+
+    // ---- G->B (modes 0..D-1) with d0b^T w; the last mode writes the term-basis output
+    for (int e = 0; e < nb0; ++e) {
+      T* A0 = X1 + e * stride;
+      T* A1 = X0 + e * stride;
+      T* cur = A0;
+      int A = 1, Bq = NQ;
+      for (int i = 0; i < D; ++i) {
+        Bq /= Tm.nq[i];
+        if (i == D - 1) {
+          T* dst = p.ht + (Tm.off_nb * nb0 + (int64_t)e * NB) * p.ldh + w.v0;
+          contract<T>(cur, Vt, dst, p.ldh, A, Tm.nq[i], Tm.nb[i], Bq, Vt, mb + Tm.m_bgw[i], T(1), false);
+        } else {
+          T* nxt = (cur == A0) ? A1 : A0;
+          contract<T>(cur, Vt, nxt, Vt, A, Tm.nq[i], Tm.nb[i], Bq, Vt, mb + Tm.m_bgw[i], T(1), false);
+          cur = nxt;
+        }
+        __syncthreads();
+        A *= Tm.nb[i];
+      }
+    }
+  }
+}
+
+// P[a] = sum_{k < nL} X[ldx*k] * Tg[a + ss*k]  for a < ss  (one grid slab of the streamed
+// position: row q of its grid<-basis matrix applied to the partially transformed tensor)
+template <typename T>
+__device__ __forceinline__ void slab_extract(const T* __restrict__ Tg, int64_t ss, int nL, const T* __restrict__ X,
+                                             int ldx, T* __restrict__ P) {
+  for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) {
+    T s = T(0);
+    for (int k0 = 0; k0 < nL; k0 += 8) {
+      T t[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) t[j] = (k0 + j < nL) ? Tg[a + ss * (k0 + j)] : T(0);
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (k0 + j < nL) s = fma(X[ldx * (k0 + j)], t[j], s);
+    }
+    P[a] = s;
+  }
+}
+
+// W[a + ss*k] += c1*O[k]*A1[a] + c2*E[k]*A2[a]  for k < nL (A2 may be null): the slab's
+// image under G->B of the streamed position
+template <typename T, int MAXL>
+__device__ __forceinline__ void slab_accumulate_m(T* __restrict__ W, int64_t ss, int nL, const T* __restrict__ O,
+                                                  const T* __restrict__ A1, T c1, const T* __restrict__ E,
+                                                  const T* __restrict__ A2, T c2) {
+  T o[MAXL], e[MAXL];  // the slab's column of both matrices, in registers
+#pragma unroll
+  for (int k = 0; k < MAXL; ++k) {
+    o[k] = k < nL ? c1 * O[k] : T(0);
+    e[k] = (A2 && k < nL) ? c2 * E[k] : T(0);
+  }
+  for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) {
+    const T u = A1[a];
+    const T z = A2 ? A2[a] : T(0);
+#pragma unroll
+    for (int k = 0; k < MAXL; ++k)
+      if (k < nL) W[a + ss * k] = fma(e[k], z, fma(o[k], u, W[a + ss * k]));
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void slab_accumulate(T* W, int64_t ss, int nL, const T* O, const T* A1, T c1, const T* E,
+                                                const T* A2, T c2) {
+  if (nL <= 8) slab_accumulate_m<T, 8>(W, ss, nL, O, A1, c1, E, A2, c2);
+  else if (nL <= 16) slab_accumulate_m<T, 16>(W, ss, nL, O, A1, c1, E, A2, c2);
+  else slab_accumulate_m<T, 24>(W, ss, nL, O, A1, c1, E, A2, c2);
+}
+
+// Phi_i = sum_j G_ij(Q) y_j on one slab, in place: y_j = Y[j] (j < L) and P (j = L).
+// One thread per grid point: G(Q) (symmetric pairs, from the grid table or the constant
+// G0) is read once and applied to the Vt vectors of the tile.
+template <typename T, int DM, bool GFLY>
+__device__ __forceinline__ void slab_pointwise_G(const ItemParams<T>& p, const TermDesc& Tm, T* Y, T* P, int64_t ss,
+                                                 int Vt, int q, int NQs, int nG) {
+  const int D = Tm.D, L = D - 1;
+  // registers hold the point's G for the vector loop when it is small (D <= 6 in FP64,
+  // D <= 8 in FP32)
+  constexpr bool kCache = DM <= (sizeof(T) == 4 ? 8 : 6);
+  constexpr int kG = kCache ? DM * (DM + 1) / 2 : 1;
+  for (int pt = threadIdx.x; pt < NQs; pt += blockDim.x) {
+    T G[kG];
+    const T* Gp = p.ggrid ? p.ggrid + Tm.off_nq * nG + (int64_t)q * NQs + pt : nullptr;
+    double xq[DM];
+    if constexpr (GFLY) {
+      point_coords<T, DM>(p, Tm, pt, L, xq);
+#pragma unroll
+      for (int k = 0; k < DM; ++k)
+        if (k == L) xq[k] = (double)p.mats[Tm.m_x[k] + q];
+    }
+    // packed slot of (i, j), i <= j < D, in the table's order
+    auto slot = [D](int i, int j) { return i * D - i * (i - 1) / 2 + (j - i); };
+    auto gload = [&](int i, int j) -> T {
+      if (i >= D || j >= D) return T(0);
+      if constexpr (GFLY) return g_model<T, DM>(p, Tm, xq, i, j);
+      return Gp ? __ldg(Gp + (int64_t)slot(i, j) * Tm.NQ) : (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[j]);
+    };
+    if constexpr (kCache) {
+#pragma unroll
+      for (int i = 0; i < DM; ++i)
+#pragma unroll
+        for (int j = i; j < DM; ++j) G[i * DM - i * (i - 1) / 2 + (j - i)] = gload(i, j);
+    }
+    for (int v = 0; v < Vt; ++v) {
+      const int64_t a = (int64_t)pt * Vt + v;
+      T y[DM], z[DM];
+#pragma unroll
+      for (int j = 0; j < DM; ++j) {
+        y[j] = (j < L) ? Y[j * ss + a] : ((j == L) ? P[a] : T(0));
+        z[j] = T(0);
+      }
+#pragma unroll
+      for (int i = 0; i < DM; ++i)
+#pragma unroll
+        for (int j = i; j < DM; ++j) {
+          T gij;
+          if constexpr (kCache) gij = G[i * DM - i * (i - 1) / 2 + (j - i)];
+          else gij = gload(i, j);
+          z[i] = fma(gij, y[j], z[i]);
+          if (j != i) z[j] = fma(gij, y[i], z[j]);
+        }
+#pragma unroll
+      for (int i = 0; i < DM; ++i) {
+        if (i < L) Y[i * ss + a] = z[i];
+        else if (i == L) P[a] = z[i];
+      }
+    }
+  }
+}
+
+// Slab-streaming pipeline for one (term, vector tile) item, one electronic state.  Positions
+// 0..L-1 of the term's mode order are transformed whole, position L = D-1 is streamed:
+//   A: gather + B->G over positions 0..L-1 (shared-memory ping-pong) -> Tg (global, L2)
+//   B: for each grid point q of position L: extract the grid slab P = d0b_L[q,:].Tg, apply V,
+//      the derivatives along positions < L and the G(Q) combination on the slab in shared
+//      memory (d_L psi comes from (d1.d0b)_L[q,:].Tg), and accumulate the slab's image under
+//      G->B of position L into W (shared memory):
+//      W[:,k] += bgw_L[k,q] Acc - 1/2 (bgw.d1)_L[k,q] Phi_L        (type 10)
+//      W[:,k] += bgw_L[k,q] Acc + F2_LL (bgw.d2)_L[k,q] P           (type 1)
+//   C: G->B over positions 0..L-1 of W (shared-memory ping-pong), the last one into the
+//      term-basis output.
+// The algebra is that of sub_TabOpPsi_OF_ONEDP_FOR_SGtype4 (sub_OpPsi_SG4.f90:1490-1650)
+// with the last mode's B->G, derivative and G->B matrices multiplied together.
+template <typename T, bool GFLY>
+__global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T> p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  __shared__ TermDesc s_term;
+  __shared__ StageBlocks s_blocks;
+  while (true) {
+    if (threadIdx.x == 0) s_item = atomicAdd(p.counter, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= p.n_items) break;
+    const WorkItem w = p.items[it];
+    {
+      const int* src = reinterpret_cast<const int*>(p.terms + w.term);
+      int* dst = reinterpret_cast<int*>(&s_term);
+      for (int i = threadIdx.x; i < (int)(sizeof(TermDesc) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const int D = s_term.D, L = D - 1;
+    T* const mb = reinterpret_cast<T*>(smem_raw);
+    stage_matrices<T>(s_term, D, p.mats, mb, s_blocks);
+    const TermDesc& Tm = s_term;
+    const int Vt = w.vt;
+    const int gL = Tm.nq[L], nL = Tm.nb[L];
+    const int NQs = Tm.NQ / gL;
+    const int64_t ss = (int64_t)NQs * Vt;  // one slab array
+    const int64_t tsz = ss * nL;           // T and W
+    T* sm = reinterpret_cast<T*>(smem_raw) + ((Tm.msz + 3) & ~3);
+    T* Tg = p.slab + (int64_t)blockIdx.x * p.slab_per_cta;
+
+    // ---- A: gather + B->G over positions 0..L-1
+    if (L == 0) {
+      for (int64_t i = threadIdx.x; i < (int64_t)nL * Vt; i += blockDim.x) {
+        const int v = (int)(i % Vt), k = (int)(i / Vt);
+        const int pk = __ldg(p.map + Tm.off_nb + k);
+        Tg[i] = pk >= 0 ? (T)__ldg(p.x + (int64_t)pk * p.ldx + w.v0 + v) : T(0);
+      }
+    } else {
+      T* b0 = sm;
+      T* b1 = sm + tsz;
+      int nb_rest = Tm.NB / Tm.nb[0];
+      T* cur = (L == 1) ? Tg : b0;
+      gather_contract<T>(p.x + w.v0, p.ldx, p.map + Tm.off_nb, 0, cur, Tm.nb[0], Tm.nq[0], nb_rest, Vt,
+                         mb + Tm.m_d0b[0]);
+      __syncthreads();
+      int A = Tm.nq[0];
+      for (int i = 1; i < L; ++i) {
+        nb_rest /= Tm.nb[i];
+        T* nxt = (i == L - 1) ? Tg : (cur == b0 ? b1 : b0);
+        contract<T>(cur, Vt, nxt, Vt, A, Tm.nb[i], Tm.nq[i], nb_rest, Vt, mb + Tm.m_d0b[i], T(1), false);
+        __syncthreads();
+        cur = nxt;
+        A *= Tm.nq[i];
+      }
+    }
+    __syncthreads();
+
+    // ---- B: stream the grid slabs of position L
+    T* W = sm;
+    T* Acc = sm + tsz;
+    T* P = Acc + ss;
+    T* Y = P + ss;
+    for (int64_t i = threadIdx.x; i < tsz; i += blockDim.x) W[i] = T(0);
+    const int ldx0 = (gL + 3) & ~3, ldo = (nL + 3) & ~3;
+    const T* X0 = mb + Tm.m_d0b[L];
+    const T* OUT = mb + Tm.m_bgw[L];
+    const int nG = D * (D + 1) / 2;
+    for (int q = 0; q < gL; ++q) {
+      __syncthreads();
+      slab_extract<T>(Tg, ss, nL, X0 + q, ldx0, P);
+      __syncthreads();
+      const T* Vq = p.vgrid + Tm.off_nq + (int64_t)q * NQs;
+      if (p.mugrid) {
+        const T* Mq = p.mugrid + Tm.off_nq + (int64_t)q * NQs;
+        const T mw = p.mu_dev ? (T)__ldg(p.mu_dev) : p.mw;
+        for (int64_t a = threadIdx.x; a < ss; a += blockDim.x)
+          Acc[a] = fma(mw, __ldg(Mq + a / Vt), p.vw * __ldg(Vq + a / Vt)) * P[a];
+      } else {
+        for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) Acc[a] = __ldg(Vq + a / Vt) * P[a];
+      }
+      if (!p.keo_on) {
+        __syncthreads();
+        slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), nullptr, nullptr, T(0));
+      } else if (p.keo_type == 10) {
+        int A = 1, Bq = NQs;
+        for (int j = 0; j < L; ++j) {  // Y[j] = d1_j P
+          Bq /= Tm.nq[j];
+          contract<T>(P, Vt, Y + j * ss, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, mb + Tm.m_d1[j], T(1), false);
+          A *= Tm.nq[j];
+        }
+        __syncthreads();
+        slab_extract<T>(Tg, ss, nL, mb + Tm.m_x1L + q, ldx0, P);  // P <- d_L psi on the slab
+        __syncthreads();
+        // Phi_i = sum_j G_ij(Q) y_j, in place (Y[i] for i < L, P for i = L)
+        if (D <= 4) slab_pointwise_G<T, 4, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
+        else if (D <= 6) slab_pointwise_G<T, 6, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
+        else if (D <= 8) slab_pointwise_G<T, 8, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
+        else if (D <= 12) slab_pointwise_G<T, 12, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
+        else slab_pointwise_G<T, 16, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
+        __syncthreads();
+        A = 1;
+        Bq = NQs;
+        for (int i = 0; i < L; ++i) {  // Acc += -1/2 d1_i Phi_i
+          Bq /= Tm.nq[i];
+          contract<T>(Y + i * ss, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d1[i], T(-0.5), true);
+          __syncthreads();
+          A *= Tm.nq[i];
+        }
+        slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), mb + Tm.m_e1L + (int64_t)ldo * q, P,
+                           T(-0.5));
+      } else {
+        __syncthreads();
+        int A = 1, Bq = NQs;
+        for (int i = 0; i < L; ++i) {  // Acc += F2_ii d2_i P
+          Bq /= Tm.nq[i];
+          const T f = (T)(-0.5 * __ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[i]));
+          if (f != T(0))
+            contract<T>(P, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d2[i], f, true);
+          __syncthreads();
+          A *= Tm.nq[i];
+        }
+        if (p.has_offdiag) {
+          int Ai = 1;
+          for (int i = 0; i < L; ++i) {
+            const int Bi = NQs / (Ai * Tm.nq[i]);
+            int Aj = Ai * Tm.nq[i];
+            for (int j = i + 1; j < L; ++j) {
+              const int Bj = NQs / (Aj * Tm.nq[j]);
+              const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[j]));
+              if (f != T(0)) {
+                contract<T>(P, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, mb + Tm.m_d1[i], T(1), false);
+                __syncthreads();
+                contract<T>(Y, Vt, Acc, Vt, Aj, Tm.nq[j], Tm.nq[j], Bj, Vt, mb + Tm.m_d1[j], f, true);
+                __syncthreads();
+              }
+              Aj *= Tm.nq[j];
+            }
+            Ai *= Tm.nq[i];
+          }
+        }
+        const T fLL = (T)(-0.5 * __ldg(p.G0 + Tm.g0off + Tm.perm[L] + D * Tm.perm[L]));
+        slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), mb + Tm.m_e2L + (int64_t)ldo * q, P,
+                           fLL);
+        if (p.has_offdiag) {  // F2_iL d1_i d_L: d_L through (bgw.d1)_L on the way back
+          int Ai = 1;
+          for (int i = 0; i < L; ++i) {
+            const int Bi = NQs / (Ai * Tm.nq[i]);
+            const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[L]));
+            if (f != T(0)) {
+              __syncthreads();
+              contract<T>(P, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, mb + Tm.m_d1[i], T(1), false);
+              __syncthreads();
+              slab_accumulate<T>(W, ss, nL, mb + Tm.m_e1L + (int64_t)ldo * q, Y, f, nullptr, nullptr, T(0));
+            }
+            Ai *= Tm.nq[i];
+          }
+        }
+      }
+    }
+    __syncthreads();
+
+    // ---- C: G->B over positions 0..L-1 of W, the last one into the term-basis output
+    T* dst = p.ht + Tm.off_nb * p.ldh + w.v0;
+    if (L == 0) {
+      for (int64_t i = threadIdx.x; i < (int64_t)nL * Vt; i += blockDim.x) {
+        const int v = (int)(i % Vt), k = (int)(i / Vt);
+        dst[(int64_t)k * p.ldh + v] = W[i];
+      }
+    } else {
+      T* b0 = W;
+      T* b1 = sm + tsz;
+      T* cur = b0;
+      int A = 1, Bq = NQs;
+      for (int i = 0; i < L; ++i) {
+        Bq /= Tm.nq[i];
+        const int Bt = Bq * nL;
+        if (i == L - 1) {
+          contract<T>(cur, Vt, dst, p.ldh, A, Tm.nq[i], Tm.nb[i], Bt, Vt, mb + Tm.m_bgw[i], T(1), false);
+        } else {
+          T* nxt = (cur == b0) ? b1 : b0;
+          contract<T>(cur, Vt, nxt, Vt, A, Tm.nq[i], Tm.nb[i], Bt, Vt, mb + Tm.m_bgw[i], T(1), false);
+          cur = nxt;
+        }
+        __syncthreads();
+        A *= Tm.nb[i];
+      }
+    }
+  }
+}
+
+
+// launchers, instantiated in evr_kern_*.cu
+template <typename T, bool GFLY>
+cudaError_t launch_items_kernel(int grid, size_t smem, cudaStream_t s, const ItemParams<T>& p);
+template <typename T, bool GFLY>
+cudaError_t launch_slab_kernel(int grid, size_t smem, cudaStream_t s, const ItemParams<T>& p);
+template <typename T, bool GFLY>
+cudaError_t set_items_kernel_smem(int bytes);
+template <typename T, bool GFLY>
+cudaError_t set_slab_kernel_smem(int bytes);
+template <typename T, bool GFLY>
+cudaError_t set_term_kernel_smem(int items_bytes, int slab_bytes) {
+  cudaError_t e = set_items_kernel_smem<T, GFLY>(items_bytes);
+  return e != cudaSuccess ? e : set_slab_kernel_smem<T, GFLY>(slab_bytes);
+}
+
+}  // namespace kern
+}  // namespace evr

@@ -363,6 +363,7 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
       const int L = P.term_l[(size_t)t * D + slab];
       T.m_x1L = off_x1[slab][L]; T.m_x2L = off_x2[slab][L]; T.m_e1L = off_e1[slab][L]; T.m_e2L = off_e2[slab][L];
       T.msz = term_matrix_elems(T, D);
+      T.D = D;
     }
     if (NB > (1 << 30) || NQ > (1 << 30)) { err = "term too large"; return EVR_EINVAL; }
     T.NB = (int32_t)NB; T.NQ = (int32_t)NQ; T.off_nb = onb; T.off_nq = onq;

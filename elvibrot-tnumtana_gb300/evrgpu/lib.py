@@ -63,7 +63,7 @@ EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_
            "evr_last_kernel_ms",
            "evr_davidson",
            "evr_cheby_propagate", "evr_fma_peak", "evr_hpsi_noalloc", "evr_set_dipole", "evr_set_field",
-           "evr_oc_forward", "evr_oc_backward"]
+           "evr_oc_forward", "evr_oc_backward", "evr_create_batch", "evr_batch_offsets", "evr_batch_davidson"]
 
 _lib = None
 
@@ -99,6 +99,9 @@ def load(build: bool = True):
     L.evr_set_kernel_path.argtypes = [vp, C.c_int]
     L.evr_fma_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.evr_hpsi_noalloc.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.c_int, vp]
+    L.evr_create_batch.argtypes = [C.POINTER(vp), C.POINTER(ProblemDesc), C.c_int, C.c_int]
+    L.evr_batch_offsets.argtypes = [vp, _lp]
+    L.evr_batch_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _dp, _lp]
     L.evr_set_dipole.argtypes = [vp, C.c_int, _dp, _ip, _ip]
     L.evr_set_field.argtypes = [vp, C.c_double, C.c_double, C.c_int]
     L.evr_oc_forward.argtypes = [vp, C.POINTER(OcOpts), _dp, _dp, _dp, _dp, _dp, _lp]
@@ -133,42 +136,52 @@ def _p(a, t):
     return None if a is None else a.ctypes.data_as(t)
 
 
+def _describe(spec, keep):
+    """ProblemDesc of a spec; the arrays it points to are appended to `keep`."""
+    def I(a):
+        if a is None:
+            return None
+        a = _iarr(a)
+        keep.append(a)
+        return _p(a, _ip)
+
+    def F(a):
+        if a is None:
+            return None
+        a = _darr(a)
+        keep.append(a)
+        return _p(a, _dp)
+
+    d = ProblemDesc()
+    d.kind = 0 if spec.kind == "sg4" else 1
+    d.D, d.nb0, d.LG, d.LB = spec.D, spec.nb0, spec.LG, spec.LB
+    d.Aq, d.Bq, d.Ab, d.Bb = I(spec.Aq), I(spec.Bq), I(spec.Ab), I(spec.Bb)
+    d.nq_dp, d.nb_dp = I(spec.nq_dp), I(spec.nb_dp)
+    d.scaleQ, d.Q0 = F(spec.scaleQ), F(spec.Q0)
+    d.n_mono = len(spec.mono_coef)
+    d.mono_coef, d.mono_idx, d.mono_elec = F(spec.mono_coef), I(spec.mono_idx), I(spec.mono_elec)
+    d.keo_type = spec.keo_type
+    d.G0 = F(np.asarray(spec.G0).ravel(order="F"))
+    d.g = F(np.asarray(spec.g).ravel(order="F"))
+    return d
+
+
 class Problem:
     """One H.psi problem on one GPU (device=-1: host tables only)."""
 
     def __init__(self, spec, device: int = 0):
         L = load()
         self.spec = spec
-        D = spec.D
-        keep = []
-
-        def I(a):
-            if a is None:
-                return None
-            a = _iarr(a)
-            keep.append(a)
-            return _p(a, _ip)
-
-        def F(a):
-            if a is None:
-                return None
-            a = _darr(a)
-            keep.append(a)
-            return _p(a, _dp)
-
-        d = ProblemDesc()
-        d.kind = 0 if spec.kind == "sg4" else 1
-        d.D, d.nb0, d.LG, d.LB = D, spec.nb0, spec.LG, spec.LB
-        d.Aq, d.Bq, d.Ab, d.Bb = I(spec.Aq), I(spec.Bq), I(spec.Ab), I(spec.Bb)
-        d.nq_dp, d.nb_dp = I(spec.nq_dp), I(spec.nb_dp)
-        d.scaleQ, d.Q0 = F(spec.scaleQ), F(spec.Q0)
-        d.n_mono = len(spec.mono_coef)
-        d.mono_coef, d.mono_idx, d.mono_elec = F(spec.mono_coef), I(spec.mono_idx), I(spec.mono_elec)
-        d.keo_type = spec.keo_type
-        d.G0 = F(np.asarray(spec.G0).ravel(order="F"))
-        d.g = F(np.asarray(spec.g).ravel(order="F"))
+        self._keep = []
+        d = _describe(spec, self._keep)
         h = C.c_void_p()
         rc = L.evr_create(C.byref(h), C.byref(d), device)
+        self._finish(h, rc, device)
+        if getattr(spec, "dip_coef", None) is not None and device >= 0:
+            self.set_dipole(spec.dip_coef, spec.dip_idx, spec.dip_elec)
+
+    def _finish(self, h, rc, device):
+        L = load()
         self.h = h
         if rc != 0:
             msg = L.evr_last_error(h).decode() if h else ""
@@ -180,8 +193,6 @@ class Problem:
         self.sum_nb, self.sum_nq, self.max_nq = s.sum_nb, s.sum_nq, s.max_nq_term
         self.flop_per_hpsi = s.flop_per_hpsi
         self.device = device
-        if getattr(spec, "dip_coef", None) is not None and device >= 0:
-            self.set_dipole(spec.dip_coef, spec.dip_idx, spec.dip_elec)
 
     def close(self):
         if getattr(self, "h", None):
@@ -357,3 +368,43 @@ class Problem:
         autocorr = ac.view(np.complex128).reshape(nsteps + 1, npsi)
         psi = out.view(np.complex128).reshape(npsi, N).T.copy() if want_psi else None
         return autocorr, psi, dict(max_order=int(info[0]), hpsi=int(info[1]), status=int(info[2]))
+
+
+class BatchProblem(Problem):
+    """Independent problems stacked in one context (evr_create_batch): vectors hold every
+    problem's packed functions (problem s in rows offsets[s]:offsets[s+1]); H.psi applies
+    the block-diagonal H in one launch; ``davidson`` runs all problems in lock-step."""
+
+    def __init__(self, specs, device: int = 0):
+        L = load()
+        self.specs = list(specs)
+        self.spec = self.specs[0]
+        self._keep = []
+        arr = (ProblemDesc * len(self.specs))(*[_describe(sp, self._keep) for sp in self.specs])
+        self._keep.append(arr)
+        h = C.c_void_p()
+        rc = L.evr_create_batch(C.byref(h), arr, len(self.specs), device)
+        self._finish(h, rc, device)
+        off = np.zeros(len(self.specs) + 1, dtype=np.int64)
+        self._check(L.evr_batch_offsets(self.h, _p(off, _lp)))
+        self.offsets = off
+
+    def davidson(self, n_levels, block=None, max_dim=None, max_it=200, conv_resi=1e-7, conv_ene=1e-10,
+                 prec="fp64", sym=-1):
+        L = load()
+        o = DavidsonOpts()
+        o.n_levels = n_levels
+        o.block = block or n_levels
+        o.max_dim = max_dim or 64
+        o.max_it = max_it
+        o.conv_resi, o.conv_ene = conv_resi, conv_ene
+        o.prec = PREC[prec]
+        o.sym = sym
+        eig = np.zeros((len(self.specs), n_levels))
+        info = np.zeros(4, dtype=np.int64)
+        rc = L.evr_batch_davidson(self.h, C.byref(o), _p(eig, _dp), _p(info, _lp))
+        stats = dict(iterations=int(info[0]), hpsi_fp64=int(info[1]), hpsi_fp32=int(info[2]),
+                     converged=bool(info[3]))
+        if rc not in (0, EVR_ENOCONV):
+            self._check(rc)
+        return eig, stats

@@ -254,6 +254,20 @@ int evr_oc_forward(evr_ctx *ctx, const evr_oc_opts *opts, const double *field, c
                    const double *target, double *out3, double *psiT, int64_t *info);
 int evr_oc_backward(evr_ctx *ctx, double *grad, double *ref, int64_t *info);
 
+/*
+ * Batches of independent problems (no counterpart in the reference, which runs one
+ * problem per process).  evr_create_batch stacks n_sys problems (any D and levels, the same
+ * nb0 and KEO type) into one context: a vector of the context holds every problem's
+ * packed functions, problem s in rows offsets[s] .. offsets[s+1]-1 (evr_batch_offsets,
+ * n_sys + 1 values), and evr_hpsi_* apply the block-diagonal H -- every problem, every
+ * column -- in one launch of the term kernels.  evr_batch_davidson: the lowest n_levels of
+ * every problem (eig: n_sys x n_levels, problem-major), one state per problem (nb0 = 1),
+ * subspace at most 64; info as evr_davidson (H.psi counts are per problem summed).
+ */
+int evr_create_batch(evr_ctx **ctx, const evr_problem_desc *descs, int n_sys, int device);
+int evr_batch_offsets(const evr_ctx *ctx, int64_t *offsets);
+int evr_batch_davidson(evr_ctx *ctx, const evr_davidson_opts *opts, double *eig, int64_t *info);
+
 #ifdef __cplusplus
 }
 #endif
