@@ -191,6 +191,82 @@ def davidson_legs(p, S):
     return out
 
 
+def run_suite(args):
+    """Timings of the other workloads, one JSON line each (device-resident data, wall clock
+    around the library call after a warm-up call)."""
+    from evrgpu import spec as S
+    from evrgpu.lib import Problem, BatchProblem
+
+    which = ["dp3", "batch", "prop12d", "control"] if args.suite == "all" else [args.suite]
+    for w in which:
+        out = {"suite": w}
+        if w == "dp3":
+            # D=3 direct product nb=20 nq=24 type-10 KEO: lowest 20 levels, 16 start vectors
+            p = Problem(S.config_dp3(), device=0)
+            p.davidson(20, block=16, conv_resi=1e-8, conv_ene=1e-11)
+            for prec in ("fp64", "fp32"):
+                t0 = time.perf_counter()
+                e, _, st = p.davidson(20, block=16, conv_resi=1e-8, conv_ene=1e-11, prec=prec)
+                out[prec] = {"s": time.perf_counter() - t0, **st}
+                out[prec + "_levels_cm"] = [float(x * S.AU_TO_CM) for x in e[:3]]
+            out["N"] = int(p.N)
+        elif w == "batch":
+            # D ~ U{3..6}, L ~ U{4..8}: lowest 10 levels of every problem, lock-step batched Davidson
+            t0 = time.perf_counter()
+            b = BatchProblem(S.batched_systems(args.batch_n, seed=2), device=0)
+            out.update({"problems": args.batch_n, "N": int(b.N), "terms": int(b.nterm),
+                        "create_s": time.perf_counter() - t0})
+            out["autotune"] = b.autotune(nvec=10, prec="fp32")
+            res = {}
+            for prec in ("fp64", "fp32"):
+                t0 = time.perf_counter()
+                e, st = b.davidson(10, block=10, conv_resi=1e-7, conv_ene=1e-10, prec=prec, max_it=100)
+                res[prec] = e
+                out[prec] = {"s": time.perf_counter() - t0, **st}
+            out["speedup"] = out["fp64"]["s"] / out["fp32"]["s"]
+            out["max_abs_diff_cm"] = float(np.abs(res["fp64"] - res["fp32"]).max() * S.AU_TO_CM)
+        elif w == "prop12d":
+            # D=12 SG4 L=6, Gaussian displaced by 1.0 in modes 1-3, Chebyshev dt = 10 au
+            sp = S.config_sg4_12d_l6()
+            p = Problem(sp, device=0)
+            psi0 = S.displaced_gaussian(sp, p, [0, 1, 2], 1.0)
+            emin, emax = S.spectral_bounds(sp)
+            out["N"] = int(p.N)
+            for prec in ("fp64", "fp32"):
+                p.chebyshev(psi0, 10.0, 2, emin, emax, prec=prec)
+                t0 = time.perf_counter()
+                ac, _, st = p.chebyshev(psi0, 10.0, args.prop_steps, emin, emax, prec=prec)
+                dt = time.perf_counter() - t0
+                out[prec] = {"steps": args.prop_steps, "s": dt, "s_per_step": dt / args.prop_steps,
+                             "order": st["max_order"], "autocorr_last": [float(ac[-1, 0].real), float(ac[-1, 0].imag)]}
+                out[prec]["s_2000_steps_extrapolated"] = 2000 * dt / args.prop_steps
+        elif w == "control":
+            # D=3 nb=20 nq=24 with the dipole; ground state -> level 5, 4000 steps of 5 au
+            sp = S.config_oc(seed=0)
+            p = Problem(sp, device=0)
+            e, vec, _ = p.davidson(8, block=16, conv_resi=1e-9, conv_ene=1e-12, want_vectors=True, sym=0)
+            rng = np.random.default_rng(0)
+            v = rng.standard_normal((p.N, 1))
+            for _ in range(200):
+                hv = p.hpsi(v)
+                lam = float(np.linalg.norm(hv))
+                v = hv / lam
+            psi0 = vec[:, 0] / np.linalg.norm(vec[:, 0]) + 0j
+            tgt = vec[:, 5] / np.linalg.norm(vec[:, 5]) + 0j
+            field = S.oc_field(4000, 5.0, seed=0)
+            t0 = time.perf_counter()
+            J, _, _, info = p.oc_forward(field, psi0, tgt, 5.0, e[0] - 0.01, 1.05 * lam)
+            tf = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            g, ref, binfo = p.oc_backward(len(field))
+            tb = time.perf_counter() - t0
+            out.update({"steps": 4000, "J": J, "forward_s": tf, "backward_s": tb, "order": info["order"],
+                        "checkpoints": info["checkpoints"],
+                        "ref_vs_grad": float(np.abs(0.5 * 5.0 * (ref[:-1] + ref[1:]) - g).max() / np.abs(g).max())})
+        print(json.dumps(out))
+    return 0
+
+
 def measure_dgemm_tflops(torch, dtype, n=4096, reps=5):
     a = torch.randn(n, n, dtype=dtype, device="cuda")
     b = torch.randn(n, n, dtype=dtype, device="cuda")
@@ -219,12 +295,19 @@ def main():
     ap.add_argument("--profile", default=None, choices=["sg4_6d_l6", "sg4_6d_l8"],
                     help="profiling mode: a few H.psi launches of the named workload, nothing else")
     ap.add_argument("--prec", default="both", choices=["both", "fp64", "fp32"], help="precision(s) in profiling mode")
+    ap.add_argument("--suite", default=None, choices=["dp3", "batch", "prop12d", "control", "all"],
+                    help="the other workloads (one JSON line each): direct-product Davidson, 256 batched "
+                         "problems, D=12 Chebyshev propagation, optimal-control gradient")
+    ap.add_argument("--batch-n", type=int, default=256, help="problems in the batch workload")
+    ap.add_argument("--prop-steps", type=int, default=200, help="time steps timed in the propagation workload")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
     if args.profile:
         return run_profile(args)
+    if args.suite:
+        return run_suite(args)
 
     import torch
 

@@ -80,9 +80,11 @@ __global__ void batch_to_float(const double* __restrict__ a, float* __restrict__
 // Eigen-decomposition of one symmetric n x n matrix per CTA (n <= 64) by cyclic Jacobi
 // with the round-robin ordering: each round rotates n/2 disjoint pairs at once (angles
 // from the matrix before the round, so the round is A <- R^T A R with R a product of
-// commuting plane rotations).  At most max_sweeps sweeps; stops when the off-diagonal
-// norm is below tol times the norm of A.  Eigenvalues ascending into W, eigenvectors as
-// the columns of V (column-major, ld ldv).
+// commuting plane rotations).  A pair is rotated unless |a_pq| <= tol sqrt(|a_pp a_qq|)
+// (relative to its own diagonal, so very large diagonal entries -- the flagged empty
+// directions -- do not hide the others); at most max_sweeps sweeps, stopping after a
+// sweep without rotations.  Eigenvalues ascending into W, eigenvectors as the columns of
+// V (column-major, ld ldv).
 __global__ void batched_jacobi_kernel(const double* __restrict__ A, int lda, int64_t sa, int n,
                                       double* __restrict__ W, int64_t sw, double* __restrict__ V, int ldv, int64_t sv,
                                       int max_sweeps, double tol) {
@@ -92,8 +94,7 @@ __global__ void batched_jacobi_kernel(const double* __restrict__ A, int lda, int
   double* v = sm + np * np;   // np x np
   __shared__ double c_[32], s_[32];
   __shared__ int p_[32], q_[32];
-  __shared__ double red[kBT / 32];
-  __shared__ double s_off, s_tot;
+  __shared__ int s_rot;
   const double* Ab = A + blockIdx.x * sa;
   for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
     const int i = e % np, j = e / np;
@@ -103,26 +104,8 @@ __global__ void batched_jacobi_kernel(const double* __restrict__ A, int lda, int
   __syncthreads();
   const int npair = np / 2;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
-    // off-diagonal and total Frobenius norms
-    double off = 0.0, tot = 0.0;
-    for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
-      const double x = a[e] * a[e];
-      tot += x;
-      if (e % np != e / np) off += x;
-    }
-    for (int pass = 0; pass < 2; ++pass) {
-      double val = pass == 0 ? off : tot;
-      for (int o = 16; o > 0; o >>= 1) val += __shfl_down_sync(0xffffffffu, val, o);
-      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = val;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
-        if (pass == 0) s_off = t; else s_tot = t;
-      }
-      __syncthreads();
-    }
-    if (!(s_off > tol * tol * s_tot)) break;
+    if (threadIdx.x == 0) s_rot = 0;
+    __syncthreads();
     for (int r = 0; r < np - 1; ++r) {
       if (threadIdx.x < npair) {
         const int k = threadIdx.x;
@@ -131,7 +114,8 @@ __global__ void batched_jacobi_kernel(const double* __restrict__ A, int lda, int
         if (p > q) { const int t = p; p = q; q = t; }
         const double apq = a[p + np * q];
         double c = 1.0, s = 0.0;
-        if (fabs(apq) > 1e-300) {
+        if (fabs(apq) > 1e-300 && fabs(apq) > tol * sqrt(fabs(a[p + np * p] * a[q + np * q]))) {
+          s_rot = 1;
           const double tau = (a[q + np * q] - a[p + np * p]) / (2.0 * apq);
           const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
           c = 1.0 / sqrt(1.0 + t * t);
@@ -164,6 +148,7 @@ __global__ void batched_jacobi_kernel(const double* __restrict__ A, int lda, int
       }
       __syncthreads();
     }
+    if (!s_rot) break;
   }
   // ascending order of the n real eigenvalues (the padding index, if any, is np - 1 = n
   // and stays decoupled)
@@ -244,6 +229,16 @@ __global__ void batch_precondition_kernel(const double* __restrict__ R, int ldr,
   }
 }
 
+// rows of the problems that are not active: zero (their new directions and H.psi columns)
+__global__ void batch_zero_rows_kernel(double* __restrict__ X, int ldx, int c0, int ncol, const int* __restrict__ sys,
+                                       const unsigned char* __restrict__ active, int64_t N) {
+  const int64_t total = N * ncol;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / ncol;
+    if (!active[__ldg(sys + r)]) X[r * ldx + c0 + (int)(e - r * ncol)] = 0.0;
+  }
+}
+
 // transform of the symmetric orthonormalisation: M[:, j] = U[:, j]/sqrt(lambda_j) for
 // lambda_j > thr * lambda_max, else 0 (column j dropped)
 __global__ void batch_lowdin_kernel(const double* __restrict__ U, const double* __restrict__ lam, int ns,
@@ -291,6 +286,7 @@ namespace evr {
 struct BatchInfo {
   std::vector<int64_t> off;  // n_sys + 1 packed offsets
   std::vector<HostProblem> sub;
+  std::vector<int> term_sys; // term -> problem
   int* sys_d = nullptr;      // row -> problem (nb0 == 1)
 };
 }  // namespace evr
@@ -496,6 +492,7 @@ int evr_create_batch(evr_ctx** out, const evr_problem_desc* descs, int n_sys, in
     int rc = build_host_problem(&descs[s], b->sub[s], err);
     if (rc) return set_error(c, rc, "evr_create_batch: problem " + std::to_string(s) + ": " + err);
     b->off[s + 1] = b->off[s] + b->sub[s].Np;
+    b->term_sys.insert(b->term_sys.end(), b->sub[s].terms.size(), s);
   }
   std::string err;
   int rc = merge_problems(c, b->sub, err);
@@ -560,7 +557,9 @@ struct BatchDavidson {
   int64_t N = 0;
   std::vector<int64_t> off;
   const int* sys_d = nullptr;
-  DBuf Pt, HPt, X, HX, R, T, Tt, Hs, Wv, Ev, Cm, Gm, Um, Lm, Mt, nrm, sel, dead, ptrs;
+  DBuf Pt, HPt, X, HX, R, T, Tt, Hs, Wv, Ev, Cm, Gm, Um, Lm, Mt, nrm, sel, dead, ptrs, actv;
+  std::vector<unsigned char> active;      // problems still iterating
+  const std::vector<int>* term_sys = nullptr;
   int64_t sh = 0;  // stride of one projected matrix (M*M)
   Grouped g;
 
@@ -582,7 +581,7 @@ struct BatchDavidson {
         Um.alloc((size_t)nsys * bmax * bmax * 8) || Lm.alloc((size_t)nsys * bmax * 8) ||
         Mt.alloc((size_t)nsys * bmax * bmax * 8) || nrm.alloc((size_t)nsys * nkeep * 8) ||
         sel.alloc((size_t)nsys * bmax * sizeof(int)) || dead.alloc((size_t)nsys * M) ||
-        ptrs.alloc((size_t)3 * nsys * sizeof(double*)))
+        ptrs.alloc((size_t)3 * nsys * sizeof(double*)) || actv.alloc((size_t)nsys))
       return fail(EVR_ENOMEM, "device allocation");
     if (cudaMemsetAsync(dead.p, 0, (size_t)nsys * M, s)) return fail(EVR_EDEVICE, "memset");
     const int np = ((std::max(M, bmax) + 1) & ~1);
@@ -658,10 +657,25 @@ struct BatchDavidson {
                    beta);
   }
 
-  int hop(const double* x, int ldx, double* y, int ldy, int n, int prec, int64_t& c64, int64_t& c32) {
+  // H.psi of n columns for the active problems only (the others' rows come out zero)
+  int hop(double* x, int ldx, double* y, int ldy, int n, int prec, int64_t& c64, int64_t& c32) {
+    int na = 0;
+    for (unsigned char a : active) na += a;
+    if (na == 0) return EVR_OK;
+    const bool all = na == nsys;
+    if (!all) {
+      c->term_active.resize(term_sys->size());
+      for (size_t t = 0; t < term_sys->size(); ++t) c->term_active[t] = active[(*term_sys)[t]];
+    }
     int rc = hpsi_blocks(c, x, ldx, y, ldy, n, prec, s, op);
+    c->term_active.clear();
     if (rc) return rc;
-    (prec == EVR_PREC_FP32 ? c32 : c64) += (int64_t)n * nsys * (op == OP_HSYM ? 2 : 1);
+    if (!all) {
+      if (cudaMemcpyAsync(actv.p, active.data(), nsys, cudaMemcpyHostToDevice, s)) return fail(EVR_EDEVICE, "copy");
+      batch_zero_rows_kernel<<<c->num_sms * 8, kBT, 0, s>>>(y, ldy, 0, n, sys_d, (const unsigned char*)actv.p, N);
+      if (cudaStreamSynchronize(s)) return fail(EVR_EDEVICE, "sync");
+    }
+    (prec == EVR_PREC_FP32 ? c32 : c64) += (int64_t)n * na * (op == OP_HSYM ? 2 : 1);
     return EVR_OK;
   }
 
@@ -728,6 +742,8 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
   d.N = c->hp.Np;
   d.off = bi->off;
   d.sys_d = bi->sys_d;
+  d.term_sys = &bi->term_sys;
+  d.active.assign(nsys, 1);
   d.bmax = b;
   d.nkeep = (int)std::min<int64_t>(nmin, nlev + b);
   d.M = (int)std::min<int64_t>(std::min<int64_t>(nmin, 64), std::max(o->max_dim, d.nkeep + b));
@@ -801,6 +817,8 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
       }
       most = std::max(most, todo[q].size());
     }
+    // problems with nothing left to do stop taking H.psi (their new columns are empty)
+    for (int q = 0; q < nsys; ++q) d.active[q] = (nt < nlev || !todo[q].empty()) ? 1 : 0;
     if (nt == nlev && most == 0 && (prec == EVR_PREC_FP64 || refine)) {
       converged = true;
       break;
@@ -822,6 +840,7 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
         n1 = kr;
         n0 = 0;
         std::fill(Eold.begin(), Eold.end(), 1e300);
+        std::fill(d.active.begin(), d.active.end(), 1);  // every problem refines its Ritz vectors
         best_r = 1e300;
         stall = 0;
         continue;
@@ -846,6 +865,11 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
       return set_error(c, EVR_EDEVICE, "copy");
     batch_precondition_kernel<<<c->num_sms * 8, kBT, 0, s>>>(d.R.d(), d.nkeep, (const int*)d.sel.p, ns, d.Ev.d(), M,
                                                              c->dp.e0diag, d.sys_d, N, d.T.d(), d.bmax, 1e-6);
+    // converged problems add empty directions (flagged and ignored by the projections)
+    if (cudaMemcpyAsync(d.actv.p, d.active.data(), nsys, cudaMemcpyHostToDevice, s))
+      return set_error(c, EVR_EDEVICE, "copy");
+    batch_zero_rows_kernel<<<c->num_sms * 8, kBT, 0, s>>>(d.T.d(), d.bmax, 0, ns, d.sys_d,
+                                                          (const unsigned char*)d.actv.p, N);
     if (n1 + ns > M) {
       if (cudaMemcpy2DAsync(d.Pt.p, sizeof(double) * M, d.X.p, sizeof(double) * d.nkeep, sizeof(double) * k, N,
                             cudaMemcpyDeviceToDevice, s) ||
@@ -870,5 +894,6 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
     info[3] = converged ? 1 : 0;
   }
   if (cudaStreamSynchronize(s)) return set_error(c, EVR_EDEVICE, "sync");
+  if ((rc = check_item_bounds(c))) return rc;
   return converged ? EVR_OK : set_error(c, EVR_ENOCONV, "evr_batch_davidson: not converged in max_it iterations");
 }

@@ -94,7 +94,8 @@ int evr_get_tables(const evr_ctx* c, int* term_l, double* weight, int* map, int*
 
 int evr_get_basis(const evr_ctx* c, int mode, int level, int* nb_nq, double* x, double* w, double* d0b, double* d1b,
                   double* d2b, double* bgw, double* d1gg, double* d2gg) {
-  if (!c || mode < 0 || mode >= c->hp.D || level < 0 || level >= (int)c->hp.bas[mode].size() || !nb_nq)
+  if (!c || mode < 0 || mode >= (int)c->hp.bas.size() || level < 0 || level >= (int)c->hp.bas[mode].size() ||
+      !nb_nq)
     return EVR_EINVAL;
   const Basis1D& b = c->hp.bas[mode][level];
   nb_nq[0] = b.nb;
@@ -111,6 +112,7 @@ int evr_get_vgrid(const evr_ctx* c0, double* v) {
   evr_ctx* c = const_cast<evr_ctx*>(c0);
   if (!c || !v) return EVR_EINVAL;
   if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
+  if (c->batch) return set_error(c, EVR_EINVAL, "evr_get_vgrid: not for batched contexts");
   EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
   const HostProblem& P = c->hp;
   const int nb2 = P.nb0 * P.nb0;
@@ -226,7 +228,7 @@ int evr_hpsi_host(evr_ctx* c, const double* psi, int64_t ld_psi, double* hpsi, i
   }
   c->last_kernels = kernels;
   EVR_CU(cudaStreamSynchronize(s), "evr_hpsi_host");
-  return EVR_OK;
+  return check_item_bounds(c);
 }
 
 

@@ -169,6 +169,19 @@ __global__ void oc_ref(const double* __restrict__ s1, const double* __restrict__
   if (threadIdx.x == 0 && blockIdx.x == 0) ref[0] = -2.0 * (s1[0] * s2[1] + s1[1] * s2[0]);
 }
 
+// mw = -field[*step], ++*step: the field of the next step, read from device memory so that
+// a captured step graph can be replayed for every step
+__global__ void oc_next_field(const double* __restrict__ field, int* __restrict__ step, double* __restrict__ mw) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    mw[0] = -field[step[0]];
+    step[0] += 1;
+  }
+}
+
+__global__ void oc_set_step(int* __restrict__ step, int v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) step[0] = v;
+}
+
 __global__ void to_float(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     b[i] = (float)a[i];
@@ -190,6 +203,13 @@ struct OCState {
   bool have_forward = false;
   // device
   std::vector<double*> bufs;
+  // field in device memory and the captured step graphs (forward step; backward step)
+  double* d_field = nullptr;
+  double* d_mw = nullptr;
+  int* d_step = nullptr;
+  double *pin = nullptr, *pn = nullptr;
+  cudaGraphExec_t exF = nullptr, exB = nullptr;
+  int64_t gen = -1;  // workspace generation the graphs were captured with
   double *target = nullptr, *cp = nullptr, *seg = nullptr, *Phi = nullptr, *MPhi = nullptr, *G = nullptr,
          *Hb = nullptr, *acc = nullptr, *ring = nullptr, *chi = nullptr, *chip = nullptr, *partial = nullptr,
          *dres = nullptr, *gc = nullptr, *ref = nullptr, *tmp = nullptr;
@@ -199,6 +219,9 @@ struct OCState {
 void oc_free(evr_ctx* c) {
   OCState* o = (OCState*)c->oc;
   if (!o) return;
+  if (o->exF) cudaGraphExecDestroy(o->exF);
+  if (o->exB) cudaGraphExecDestroy(o->exB);
+  if (o->d_step) cudaFree(o->d_step);
   for (double* p : o->bufs)
     if (p) cudaFree(p);
   delete o;
@@ -218,11 +241,12 @@ int oc_alloc(evr_ctx* c, OCState* o, double** p, size_t n) {
 // one propagation step: psi_out = U_n psi_in (may alias); with Phi != nullptr the phi_k
 // (k = 0..K) are kept at Phi + 2k (stride ldP); returns a status
 int fwd_step(evr_ctx* c, OCState* o, const double* psi_in, int64_t lpi, double* psi_out, int64_t lpo, double E,
-             double* Phi, int64_t ldP) {
+             double* Phi, int64_t ldP, const double* mu_dev = nullptr) {
   const int64_t N = o->N;
   cudaStream_t s = c->stream;
   OpExtras ex;
   ex.mw = -E;
+  ex.mu_dev = mu_dev;
   const int gb = grid_blocks(c, N);
   const int K = o->K;
   const double inv = 1.0 / o->Esc;
@@ -271,6 +295,44 @@ int dot1(evr_ctx* c, OCState* o, const double* a, int64_t la, const double* b, i
   return cuda_check(c, cudaGetLastError(), "optimal control: dot");
 }
 
+// Captures the launch sequence of body() on the context's stream into an executable graph.
+template <typename F>
+int capture(evr_ctx* c, F&& body, cudaGraphExec_t* exec) {
+  cudaStream_t s = c->stream;
+  c->capturing = true;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    c->capturing = false;
+    (void)cudaGetLastError();
+    return EVR_EDEVICE;
+  }
+  const int rc = body();
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(s, &g);
+  c->capturing = false;
+  if (rc || ce != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    (void)cudaGetLastError();
+    return rc ? rc : EVR_EDEVICE;
+  }
+  const cudaError_t ie = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) {
+    (void)cudaGetLastError();
+    *exec = nullptr;
+    return EVR_EDEVICE;
+  }
+  return EVR_OK;
+}
+
+// graphs hold the workspace's device pointers: drop them when the workspace changed
+void check_graphs(evr_ctx* c, OCState* o) {
+  if (o->gen == c->ws_gen) return;
+  if (o->exF) cudaGraphExecDestroy(o->exF);
+  if (o->exB) cudaGraphExecDestroy(o->exB);
+  o->exF = o->exB = nullptr;
+  o->gen = c->ws_gen;
+}
+
 }  // namespace
 
 namespace evr {
@@ -281,6 +343,7 @@ extern "C" {
 
 int evr_set_dipole(evr_ctx* c, int n_mono, const double* coef, const int* idx, const int* elec) {
   if (!c) return EVR_EINVAL;
+  if (c->batch) return set_error(c, EVR_EINVAL, "evr_set_dipole: not for batched contexts");
   const HostProblem& P = c->hp;
   if (n_mono < 0 || (n_mono > 0 && (!coef || !idx || !elec)))
     return set_error(c, EVR_EINVAL, "evr_set_dipole: n_mono < 0 or null arrays");
@@ -384,17 +447,33 @@ int evr_oc_forward(evr_ctx* c, const evr_oc_opts* opts, const double* field, con
   if ((rc = oc_alloc(c, o, &o->target, v2)) || (rc = oc_alloc(c, o, &o->cp, v2 * o->ncp)) ||
       (rc = oc_alloc(c, o, &o->Hb, v2)) || (rc = oc_alloc(c, o, &o->acc, v2)) ||
       (rc = oc_alloc(c, o, &o->ring, 3 * v2)) || (rc = oc_alloc(c, o, &o->partial, (size_t)2 * kDotBlocks * (K + 2))) ||
-      (rc = oc_alloc(c, o, &o->dres, (size_t)2 * (K + 4))) || (rc = oc_alloc(c, o, &o->tmp, v2))) {
+      (rc = oc_alloc(c, o, &o->dres, (size_t)2 * (K + 6))) || (rc = oc_alloc(c, o, &o->tmp, v2)) ||
+      (rc = oc_alloc(c, o, &o->d_field, (size_t)nst)) || (rc = oc_alloc(c, o, &o->d_mw, 1)) ||
+      (rc = oc_alloc(c, o, &o->pin, v2)) || (rc = oc_alloc(c, o, &o->pn, v2)) ||
+      (rc = cuda_check(c, cudaMalloc((void**)&o->d_step, sizeof(int)), "cudaMalloc"))) {
     oc_free(c);
     return rc;
   }
   cudaMemcpyAsync(o->cp, psi0, v2 * sizeof(double), cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(o->target, target, v2 * sizeof(double), cudaMemcpyHostToDevice, s);
   if ((rc = cuda_check(c, cudaGetLastError(), "evr_oc_forward: upload"))) return rc;
-  // psi lives in tmp; every S steps it is copied to the next checkpoint
+  cudaMemcpyAsync(o->d_field, o->field.data(), nst * sizeof(double), cudaMemcpyHostToDevice, s);
+  // psi lives in tmp; every S steps it is copied to the next checkpoint.  The first step
+  // runs eagerly (it also sets up every work decomposition), the others replay its graph.
+  o->gen = c->ws_gen;
+  oc_set_step<<<1, 1, 0, s>>>(o->d_step, 0);
   cudaMemcpyAsync(o->tmp, o->cp, v2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  auto stepF = [&]() -> int {
+    oc_next_field<<<1, 1, 0, s>>>(o->d_field, o->d_step, o->d_mw);
+    return fwd_step(c, o, o->tmp, 2, o->tmp, 2, 0.0, nullptr, 0, o->d_mw);
+  };
   for (int n = 1; n <= nst; ++n) {
-    if ((rc = fwd_step(c, o, o->tmp, 2, o->tmp, 2, o->field[n - 1], nullptr, 0))) return rc;
+    if (n == 2 && !o->exF && capture(c, stepF, &o->exF) != EVR_OK) o->exF = nullptr;
+    if (n >= 2 && o->exF) {
+      if ((rc = cuda_check(c, cudaGraphLaunch(o->exF, s), "evr_oc_forward: graph launch"))) return rc;
+    } else if ((rc = stepF())) {
+      return rc;
+    }
     if (n % o->S == 0)
       cudaMemcpyAsync(o->cp + v2 * (n / o->S), o->tmp, v2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
   }
@@ -465,51 +544,78 @@ int evr_oc_backward(evr_ctx* c, double* grad, double* ref, int64_t* info) {
   const int nseg = (nst + S - 1) / S;
   const int ndb = (int)std::min<int64_t>(kDotBlocks, (N + kT - 1) / kT);
   double* s12 = o->dres + 2 * (K + 1);  // two complex scalars for the boundary gradient (dres holds 2(K+4))
+  check_graphs(c, o);
+  OpExtras exT;  // H^T - E_n mu with E_n from device memory
+  exT.mu_dev = o->d_mw;
+  double* gslot = o->dres + 2 * (K + 3);   // df/dE of the step (2 doubles)
+  double* rslot = o->dres + 2 * (K + 3) + 2;  // boundary gradient of the step (dres holds 2(K+6))
+  // one backward step: psi_{n-1} in pin, psi_n in pn, the step's field index in d_step
+  auto stepB = [&]() -> int {
+    int r;
+    oc_next_field<<<1, 1, 0, s>>>(o->d_field, o->d_step, o->d_mw);
+    // phi_0..phi_K of the step (phi_K is produced but not needed) and psi_n beside them
+    if ((r = fwd_step(c, o, o->pin, 2, o->tmp, 2, 0.0, o->Phi, ldP, o->d_mw))) return r;
+    cudaMemcpy2DAsync(o->Phi + 2 * (K + 1), ldP * sizeof(double), o->pn, 2 * sizeof(double), 2 * sizeof(double), N,
+                      cudaMemcpyDeviceToDevice, s);
+    // mu phi_k (k < K) and mu psi_n: columns 0..2K-1 and 2K+2..2K+3; phi_K's columns ride along
+    if ((r = hpsi_blocks(c, o->Phi, ldP, o->MPhi, ldP, (int)ldP, o->prec, s, OP_H, &mu_only))) return r;
+    // boundary gradient at t_n: -2 Im(<psi_n|chi_n><chi_n|mu psi_n>)
+    if ((r = dot1(c, o, o->pn, 2, o->chi, 2, s12))) return r;
+    if ((r = dot1(c, o, o->chi, 2, o->MPhi + 2 * (K + 1), ldP, s12 + 2))) return r;
+    oc_ref<<<1, 32, 0, s>>>(s12, s12 + 2, rslot);
+    // adjoint recurrence with chi' = exp(+i Ebar dt) chi
+    oc_phase<<<gb, kT, 0, s>>>(o->chi, 2, o->chip, 2, o->cs, -o->sn, N);
+    oc_clenshaw<<<gb, kT, 0, s>>>(o->G + 2 * K, ldG, o->chip, nullptr, 0, nullptr, 0, nullptr, 0, o->coef[K], 0.0,
+                                  o->Eb, inv, N);
+    for (int k = K - 1; k >= 0; --k) {
+      const double* G1 = o->G + 2 * (k + 1);
+      if ((r = hpsi_interleaved(c, G1, ldG, o->Hb, 2, 2, o->prec, s, OP_HT, &exT))) return r;
+      oc_clenshaw<<<gb, kT, 0, s>>>(o->G + 2 * k, ldG, o->chip, o->Hb, 2, G1, ldG, o->G + 2 * (k + 2), ldG,
+                                    o->coef[k], k == 0 ? 1.0 : 2.0, o->Eb, inv, N);
+    }
+    // df/dE_n = (i/Esc) sum_k w_k <G_{k+1}|mu phi_k>
+    oc_dots<<<dim3(ndb, K), kT, 0, s>>>(o->G + 2, ldG, 2, o->MPhi, ldP, 2, N, o->partial);
+    oc_dots_final<<<1, 32, 0, s>>>(o->partial, ndb, K, nullptr, gslot, inv);
+    // chi_{n-1} = G_0
+    cudaMemcpy2DAsync(o->chi, 2 * sizeof(double), o->G, ldG * sizeof(double), 2 * sizeof(double), N,
+                      cudaMemcpyDeviceToDevice, s);
+    return cuda_check(c, cudaGetLastError(), "evr_oc_backward: step kernels");
+  };
+  auto stepF = [&]() -> int {
+    oc_next_field<<<1, 1, 0, s>>>(o->d_field, o->d_step, o->d_mw);
+    return fwd_step(c, o, o->tmp, 2, o->tmp, 2, 0.0, nullptr, 0, o->d_mw);
+  };
+  bool first = true;
   for (int sg = nseg - 1; sg >= 0; --sg) {
     const int n0 = sg * S, n1 = std::min(n0 + S, nst);
-    // states psi_{n0..n1} of the segment
+    // states psi_{n0..n1} of the segment, by the forward step (graph when available)
     cudaMemcpyAsync(o->seg, o->cp + v2 * sg, v2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(o->tmp, o->cp + v2 * sg, v2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    oc_set_step<<<1, 1, 0, s>>>(o->d_step, n0);
     for (int n = n0 + 1; n <= n1; ++n) {
-      if ((rc = fwd_step(c, o, o->seg + v2 * (n - 1 - n0), 2, o->seg + v2 * (n - n0), 2, o->field[n - 1], nullptr,
-                         0)))
+      if (o->exF) {
+        if ((rc = cuda_check(c, cudaGraphLaunch(o->exF, s), "evr_oc_backward: graph launch"))) return rc;
+      } else if ((rc = stepF())) {
         return rc;
+      }
+      cudaMemcpyAsync(o->seg + v2 * (n - n0), o->tmp, v2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
       cols += 2 * K;
     }
     for (int n = n1; n > n0; --n) {
-      const double E = o->field[n - 1];
-      OpExtras ex;
-      ex.mw = -E;
-      const double* psi_prev = o->seg + v2 * (n - 1 - n0);
-      const double* psi_n = o->seg + v2 * (n - n0);
-      // phi_0..phi_K of the step (phi_K is produced but not needed) and psi_n beside them
-      if ((rc = fwd_step(c, o, psi_prev, 2, o->tmp, 2, E, o->Phi, ldP))) return rc;
-      cudaMemcpy2DAsync(o->Phi + 2 * (K + 1), ldP * sizeof(double), psi_n, 2 * sizeof(double), 2 * sizeof(double), N,
-                        cudaMemcpyDeviceToDevice, s);
-      // mu phi_k (k < K) and mu psi_n: columns 0..2K-1 and 2K+2..2K+3; phi_K's columns ride along
-      if ((rc = hpsi_blocks(c, o->Phi, ldP, o->MPhi, ldP, (int)ldP, o->prec, s, OP_H, &mu_only))) return rc;
-      cols += 2 * K + ldP;
-      // boundary gradient at t_n: -2 Im(<psi_n|chi_n><chi_n|mu psi_n>)
-      if ((rc = dot1(c, o, psi_n, 2, o->chi, 2, s12))) return rc;
-      if ((rc = dot1(c, o, o->chi, 2, o->MPhi + 2 * (K + 1), ldP, s12 + 2))) return rc;
-      oc_ref<<<1, 32, 0, s>>>(s12, s12 + 2, o->ref + n);
-      // adjoint recurrence with chi' = exp(+i Ebar dt) chi
-      oc_phase<<<gb, kT, 0, s>>>(o->chi, 2, o->chip, 2, o->cs, -o->sn, N);
-      oc_clenshaw<<<gb, kT, 0, s>>>(o->G + 2 * K, ldG, o->chip, nullptr, 0, nullptr, 0, nullptr, 0, o->coef[K], 0.0,
-                                    o->Eb, inv, N);
-      for (int k = K - 1; k >= 0; --k) {
-        const double* G1 = o->G + 2 * (k + 1);
-        if ((rc = hpsi_interleaved(c, G1, ldG, o->Hb, 2, 2, o->prec, s, OP_HT, &ex))) return rc;
-        cols += 2;
-        oc_clenshaw<<<gb, kT, 0, s>>>(o->G + 2 * k, ldG, o->chip, o->Hb, 2, G1, ldG, o->G + 2 * (k + 2), ldG,
-                                      o->coef[k], k == 0 ? 1.0 : 2.0, o->Eb, inv, N);
+      cudaMemcpyAsync(o->pin, o->seg + v2 * (n - 1 - n0), v2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(o->pn, o->seg + v2 * (n - n0), v2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
+      oc_set_step<<<1, 1, 0, s>>>(o->d_step, n - 1);
+      if (!first && !o->exB && capture(c, stepB, &o->exB) != EVR_OK) o->exB = nullptr;
+      if (!first && o->exB) {
+        if ((rc = cuda_check(c, cudaGraphLaunch(o->exB, s), "evr_oc_backward: graph launch"))) return rc;
+      } else if ((rc = stepB())) {
+        return rc;
       }
-      // df/dE_n = (i/Esc) sum_k w_k <G_{k+1}|mu phi_k>
-      oc_dots<<<dim3(ndb, K), kT, 0, s>>>(o->G + 2, ldG, 2, o->MPhi, ldP, 2, N, o->partial);
-      oc_dots_final<<<1, 32, 0, s>>>(o->partial, ndb, K, nullptr, o->gc + 2 * n, inv);
-      // chi_{n-1} = G_0
-      cudaMemcpy2DAsync(o->chi, 2 * sizeof(double), o->G, ldG * sizeof(double), 2 * sizeof(double), N,
-                        cudaMemcpyDeviceToDevice, s);
-      if ((rc = cuda_check(c, cudaGetLastError(), "evr_oc_backward: step kernels"))) return rc;
+      first = false;
+      cudaMemcpyAsync(o->gc + 2 * n, gslot, 2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(o->ref + n, rslot, sizeof(double), cudaMemcpyDeviceToDevice, s);
+      cols += 4 * K + ldP;
+      if ((rc = cuda_check(c, cudaGetLastError(), "evr_oc_backward: step"))) return rc;
     }
   }
   // boundary gradient at t = 0

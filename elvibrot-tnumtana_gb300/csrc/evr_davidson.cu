@@ -487,5 +487,6 @@ extern "C" int evr_davidson(evr_ctx* c, const evr_davidson_opts* o, const double
     info[3] = converged ? 1 : 0;
   }
   if (cudaStreamSynchronize(s)) return set_error(c, EVR_EDEVICE, "sync");
+  if ((rc = check_item_bounds(c))) return rc;
   return converged ? EVR_OK : set_error(c, EVR_ENOCONV, "evr_davidson: not converged in max_it iterations");
 }

@@ -73,7 +73,8 @@ struct WorkItem {
   int32_t term;
   int32_t v0;
   int32_t vt;            // vectors in the tile
-  int32_t smem;          // 1: buffers in shared memory, 0: in the CTA's global slab
+  int32_t smem;          // general kernel: 1 buffers in shared memory, 0 in the CTA's global buffer;
+                         // slab kernel: 2 partially transformed tensor in shared memory too
 };
 
 struct HostProblem {
@@ -135,6 +136,7 @@ struct ItemSet {
   int n_items = 0;
   WorkItem* items_slab = nullptr;  // slab kernel
   int n_slab = 0;
+  std::vector<WorkItem> h_items, h_slab;  // host copies (filtered launches of batches)
 };
 
 struct Workspace {
@@ -150,6 +152,9 @@ struct Workspace {
   int grid = 0, smem_bytes = 0;             // general kernel
   int grid_slab = 0, smem_slab_bytes = 0;   // slab kernel
   size_t slab_slab_bytes = 0;               // slab kernel's global tensor per CTA
+  WorkItem* f_items = nullptr;              // filtered item lists (terms of active problems)
+  WorkItem* f_slab = nullptr;
+  size_t f_cap = 0;
 };
 
 // operator forms
@@ -182,6 +187,9 @@ struct evr_ctx {
   bool use_slab = true;             // slab kernel for the terms that fit (EVR_NO_SLAB=1 disables)
   bool use_stages = true;           // grid-wide stage path for single-term problems
   bool gfly = false;                // G(Q) from the linear model per point instead of a table
+  int vt_cap_slab = 32, vt_cap_items = 32;  // widest vector tile of an item (evr_autotune)
+  int64_t ws_gen = 0;               // bumped whenever workspace buffers are freed (captured graphs)
+  std::vector<unsigned char> term_active;  // batches: terms to run (empty = all)
   int n_sys = 1;                    // problems stacked in this context (evr_create_batch)
   cudaStream_t stream = nullptr;
   evr::HostProblem hp;
@@ -244,5 +252,8 @@ int transpose_to_interleaved(const double* in, int64_t ld_in, double* out, int64
 int transpose_from_interleaved(const double* in, int64_t ld_in, double* out, int64_t ld_out, int64_t N, int nvec,
                                cudaStream_t s);
 int set_error(evr_ctx* c, int code, const std::string& msg);
+// reads (and clears) the flag the term kernels raise when an item would exceed its buffers
+int check_item_bounds(evr_ctx* c);
+void clear_item_sets(evr_ctx* c);
 int cuda_check(evr_ctx* c, cudaError_t e, const char* what);
 }  // namespace evr

@@ -127,7 +127,7 @@ __global__ void transpose_kernel(const double* __restrict__ in, int64_t ld_in, d
 
 template <typename T>
 size_t footprint_elems(const HostProblem& P, const TermDesc& Tm, int vt) {
-  int ny = (P.keo_type == 10) ? P.D : 1;
+  int ny = (P.keo_type == 10) ? Tm.D : 1;
   return (size_t)(2 * P.nb0 + ny) * (size_t)Tm.NQ * (size_t)vt;
 }
 
@@ -233,19 +233,32 @@ void free_workspace(evr_ctx* c) {
     if (s.items) cudaFree(s.items);
     if (s.items_slab) cudaFree(s.items_slab);
   }
-  void* ptrs[] = {w.counter, w.slab, w.ht, w.ht2, w.xin, w.xout};
+  void* ptrs[] = {w.counter, w.slab, w.ht, w.ht2, w.xin, w.xout, w.f_items, w.f_slab};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   w = Workspace();
   free_stages(c);
+  ++c->ws_gen;
 }
 
 // elements of shared memory the slab kernel needs for a term and a vector tile
 static size_t slab_need_elems(const HostProblem& P, const TermDesc& Tm, int vt) {
-  const int L = P.D - 1;
+  const int L = Tm.D - 1;  // the term's own mode count (stacked problems differ)
   const size_t ss = (size_t)(Tm.NQ / Tm.nq[L]) * vt, tsz = ss * Tm.nb[L];
   const size_t ny = (P.keo_type == 10) ? (size_t)L : 1;
   return std::max(2 * tsz, tsz + (2 + ny) * ss);
+}
+
+// W-in-global mode of the slab kernel: shared memory holds only the slab arrays, the
+// global buffer Tg, W and one ping-pong tensor (3 tensors of NQs*nb_L*vt)
+static size_t slab_wg_smem_elems(const HostProblem& P, const TermDesc& Tm, int vt) {
+  const int L = Tm.D - 1;
+  const size_t ss = (size_t)(Tm.NQ / Tm.nq[L]) * vt;
+  return (2 + ((P.keo_type == 10) ? (size_t)L : 1)) * ss;
+}
+static size_t slab_wg_global_elems(const TermDesc& Tm, int vt) {
+  const int L = Tm.D - 1;
+  return 3 * (size_t)(Tm.NQ / Tm.nq[L]) * vt * Tm.nb[L];
 }
 
 // Work decomposition for a block of nvec vectors.  Terms whose slab pipeline fits the
@@ -272,11 +285,22 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
     }
     w.slab_per_cta_bytes = slab;
     // the slab kernel keeps its partially transformed tensor (at most half of its shared
-    // memory) in global memory
-    w.slab_slab_bytes = (size_t)(w.smem_slab_bytes / 2 + 256) & ~(size_t)255;
+    // memory) in global memory; terms in the W-in-global mode (FP64 terms whose slab
+    // pipeline does not fit shared memory) need three such tensors there
+    size_t sb = (size_t)(w.smem_slab_bytes / 2 + 256);
+    if (P.nb0 == 1)
+      for (const TermDesc& Tm : P.terms) {
+        if (Tm.weight == 0.0) continue;
+        const size_t mats = (size_t)((Tm.msz + 3) & ~3) * sizeof(double);
+        if (slab_need_elems(P, Tm, 1) * sizeof(double) + mats <= (size_t)w.smem_slab_bytes) continue;
+        if (slab_wg_smem_elems(P, Tm, 1) * sizeof(double) + mats > (size_t)w.smem_slab_bytes) continue;
+        sb = std::max(sb, slab_wg_global_elems(Tm, 1) * sizeof(double));
+      }
+    w.slab_slab_bytes = (sb + 255) & ~(size_t)255;
     const size_t total = std::max(slab * w.grid, w.slab_slab_bytes * w.grid_slab);
-    w.counter = (int*)dev_alloc<int>(2, rc);
+    w.counter = (int*)dev_alloc<int>(4, rc);  // item counters of both kernels, item-bounds flag
     if (rc) return set_error(c, rc, "workspace allocation (counter)");
+    EVR_CU(cudaMemset(w.counter, 0, 4 * sizeof(int)), "memset counter");
     w.slab = dev_alloc<unsigned char>(total, rc);
     if (rc) return set_error(c, rc, "workspace allocation (slab)");
     w.cap = kMaxBlock;
@@ -303,18 +327,38 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
     const size_t mats = (size_t)((Tm.msz + 3) & ~3) * esz;  // staged 1-D matrices
     if (mats > (size_t)w.smem_bytes) return set_error(c, EVR_EINVAL, "1-D matrices exceed shared memory");
     if (slab_ok && slab_need_elems(P, Tm, 1) * esz + mats <= (size_t)w.smem_slab_bytes) {
+      // FP32: the partially transformed tensor also in shared memory when a tile of
+      // min(4, nvec) vectors fits (its per-slab re-reads then stay on the SM); FP64 keeps it
+      // in the L2-resident global buffer, the FP64 pipe being the bound there
+      const int L = Tm.D - 1;
+      auto tg_elems = [&](int v) { return (size_t)(Tm.NQ / Tm.nq[L]) * v * Tm.nb[L]; };
+      auto fits = [&](int v, bool tg) {
+        return (slab_need_elems(P, Tm, v) + (tg ? tg_elems(v) : 0)) * esz + mats <= (size_t)w.smem_slab_bytes;
+      };
+      const bool tg = prec == EVR_PREC_FP32 && fits(std::min(4, nvec), true);
       int vt = 1;
-      while (vt * 2 <= nvec && vt * 2 <= 32 &&
-             slab_need_elems(P, Tm, vt * 2) * esz + mats <= (size_t)w.smem_slab_bytes)
-        vt *= 2;
-      for (int v0 = 0; v0 < nvec; v0 += vt) sitems.push_back(WorkItem{t, v0, std::min(vt, nvec - v0), 1});
+      while (vt * 2 <= nvec && vt * 2 <= c->vt_cap_slab && fits(vt * 2, tg)) vt *= 2;
+      for (int v0 = 0; v0 < nvec; v0 += vt) sitems.push_back(WorkItem{t, v0, std::min(vt, nvec - v0), tg ? 2 : 1});
+      continue;
+    }
+    // W in global memory: the slab pipeline with only the slab arrays in shared memory
+    if (slab_ok && slab_wg_smem_elems(P, Tm, 1) * esz + mats <= (size_t)w.smem_slab_bytes &&
+        slab_wg_global_elems(Tm, 1) * esz <= w.slab_slab_bytes) {
+      auto fits = [&](int v) {
+        return slab_wg_smem_elems(P, Tm, v) * esz + mats <= (size_t)w.smem_slab_bytes &&
+               slab_wg_global_elems(Tm, v) * esz <= w.slab_slab_bytes;
+      };
+      int vt = 1;
+      while (vt * 2 <= nvec && vt * 2 <= c->vt_cap_slab && fits(vt * 2)) vt *= 2;
+      for (int v0 = 0; v0 < nvec; v0 += vt) sitems.push_back(WorkItem{t, v0, std::min(vt, nvec - v0), 3});
       continue;
     }
     int vt = 1;
     const size_t fp1 = footprint_elems<double>(P, Tm, 1) * esz;
     const bool in_smem = fp1 + mats <= (size_t)w.smem_bytes;
     if (in_smem)
-      while (vt * 2 <= nvec && vt * 2 <= 32 && fp1 * (size_t)(vt * 2) + mats <= (size_t)w.smem_bytes) vt *= 2;
+      while (vt * 2 <= nvec && vt * 2 <= c->vt_cap_items && fp1 * (size_t)(vt * 2) + mats <= (size_t)w.smem_bytes)
+        vt *= 2;
     for (int v0 = 0; v0 < nvec; v0 += vt) items.push_back(WorkItem{t, v0, std::min(vt, nvec - v0), in_smem ? 1 : 0});
   }
   auto by_cost = [&](const WorkItem& a, const WorkItem& b) {
@@ -336,6 +380,8 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
   if (!sitems.empty())
     EVR_CU(cudaMemcpy(s.items_slab, sitems.data(), sitems.size() * sizeof(WorkItem), cudaMemcpyHostToDevice),
            "items");
+  s.h_items = items;
+  s.h_slab = sitems;
   w.sets.push_back(s);
   return EVR_OK;
 }
@@ -366,13 +412,19 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
   p.vtrans = vtrans;
   p.implicit_nvec = 0;
   p.has_offdiag = 0;
-  if (P.keo_type == 1)
-    for (int i = 0; i < P.D; ++i)
-      for (int j = i + 1; j < P.D; ++j) p.has_offdiag |= (P.G0[i + (size_t)P.D * j] != 0.0);
+  if (P.keo_type == 1) {
+    if (c->batch) {
+      p.has_offdiag = 1;  // stacked problems: the kernels skip the zero F2 pairs term by term
+    } else {
+      for (int i = 0; i < P.D; ++i)
+        for (int j = i + 1; j < P.D; ++j) p.has_offdiag |= (P.G0[i + (size_t)P.D * j] != 0.0);
+    }
+  }
   set_plain(p);
   p.keo_on = ex.keo;
   p.gco = c->dp.g;
   p.gfly = c->gfly ? 1 : 0;
+  p.err = w.counter + 2;
   if (ex.mw != 0.0 || ex.vw != 1.0 || ex.mu_dev) {
     if (!c->dp_mugrid) return set_error(c, EVR_EINVAL, "field term without a dipole (evr_set_dipole)");
     p.mugrid = f32 ? (const T*)c->dp_mugrid32 : (const T*)c->dp_mugrid;
@@ -387,6 +439,7 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
     ps.n_items = set.n_slab;
     ps.counter = w.counter + 1;
     ps.slab_per_cta = (int64_t)(w.slab_slab_bytes / sizeof(T));
+    ps.smem_elems = (int64_t)(w.smem_slab_bytes / sizeof(T));
     EVR_CU((p.gfly ? launch_slab_kernel<T, true>(w.grid_slab, w.smem_slab_bytes, s, ps)
                    : launch_slab_kernel<T, false>(w.grid_slab, w.smem_slab_bytes, s, ps)),
            "hpsi_slab_kernel launch");
@@ -395,6 +448,7 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
     p.items = set.items;
     p.n_items = set.n_items;
     p.slab_per_cta = (int64_t)(w.slab_per_cta_bytes / sizeof(T));
+    p.smem_elems = (int64_t)(w.smem_bytes / sizeof(T));
     EVR_CU((p.gfly ? launch_items_kernel<T, true>(w.grid, w.smem_bytes, s, p)
                    : launch_items_kernel<T, false>(w.grid, w.smem_bytes, s, p)),
            "hpsi_items_kernel launch");
@@ -443,7 +497,40 @@ int hpsi_interleaved(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_
   for (const ItemSet& it : c->ws.sets)
     if (it.nvec == nvec && it.prec == prec) set = &it;
   if (!set) return set_error(c, EVR_EINVAL, "no work decomposition");
-  const ItemSet cp = *set;
+  ItemSet cp;
+  cp.nvec = set->nvec;
+  cp.prec = set->prec;
+  cp.items = set->items;
+  cp.n_items = set->n_items;
+  cp.items_slab = set->items_slab;
+  cp.n_slab = set->n_slab;
+  if (!c->term_active.empty()) {
+    // batches: only the terms of the active problems (host-synchronous, not for capture)
+    if (c->capturing) return set_error(c, EVR_EINVAL, "filtered H.psi inside a stream capture");
+    Workspace& w = c->ws;
+    const size_t need = std::max(set->h_items.size(), set->h_slab.size());
+    if (w.f_cap < need) {
+      if (w.f_items) cudaFree(w.f_items);
+      if (w.f_slab) cudaFree(w.f_slab);
+      w.f_items = w.f_slab = nullptr;
+      w.f_cap = 0;
+      EVR_CU(cudaMalloc((void**)&w.f_items, need * sizeof(WorkItem)), "cudaMalloc items");
+      EVR_CU(cudaMalloc((void**)&w.f_slab, need * sizeof(WorkItem)), "cudaMalloc items");
+      w.f_cap = need;
+    }
+    std::vector<WorkItem> fi, fs;
+    for (const WorkItem& it : set->h_items)
+      if (c->term_active[it.term]) fi.push_back(it);
+    for (const WorkItem& it : set->h_slab)
+      if (c->term_active[it.term]) fs.push_back(it);
+    EVR_CU(cudaStreamSynchronize(s), "sync");  // the previous launch may still read the lists
+    if (!fi.empty()) EVR_CU(cudaMemcpy(w.f_items, fi.data(), fi.size() * sizeof(WorkItem), cudaMemcpyHostToDevice), "items");
+    if (!fs.empty()) EVR_CU(cudaMemcpy(w.f_slab, fs.data(), fs.size() * sizeof(WorkItem), cudaMemcpyHostToDevice), "items");
+    cp.items = w.f_items;
+    cp.n_items = (int)fi.size();
+    cp.items_slab = w.f_slab;
+    cp.n_slab = (int)fs.size();
+  }
   if (prec == EVR_PREC_FP32) return run_items<float>(c, cp, x, ldx, y, ldy, nvec, s, op, e);
   return run_items<double>(c, cp, x, ldx, y, ldy, nvec, s, op, e);
 }
@@ -476,6 +563,26 @@ int transpose_from_interleaved(const double* in, int64_t ld_in, double* out, int
   dim3 blk(32, 8), grd((unsigned)((nvec + 31) / 32), (unsigned)((N + 31) / 32));
   transpose_kernel<<<grd, blk, 0, s>>>(in, ld_in, out, ld_out, N, nvec);
   return cudaGetLastError() == cudaSuccess ? EVR_OK : EVR_EDEVICE;
+}
+
+// drops the cached work decompositions (they depend on the tile caps)
+void clear_item_sets(evr_ctx* c) {
+  for (ItemSet& st : c->ws.sets) {
+    if (st.items) cudaFree(st.items);
+    if (st.items_slab) cudaFree(st.items_slab);
+  }
+  c->ws.sets.clear();
+  ++c->ws_gen;
+}
+
+int check_item_bounds(evr_ctx* c) {
+  if (!c->ws.counter) return EVR_OK;
+  int flag = 0;
+  EVR_CU(cudaMemcpyAsync(&flag, c->ws.counter + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream), "flag");
+  EVR_CU(cudaStreamSynchronize(c->stream), "flag");
+  if (!flag) return EVR_OK;
+  EVR_CU(cudaMemsetAsync(c->ws.counter + 2, 0, sizeof(int), c->stream), "flag");
+  return set_error(c, EVR_EDEVICE, "a work item exceeded its buffers and was skipped (internal sizing error)");
 }
 
 int reduce_terms(evr_ctx* c, int prec, const void* ht, const void* ht2, int nvec, double scale, double* y,
@@ -557,7 +664,7 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
   int optin = 0;
   EVR_CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attr");
   if (smem > (size_t)optin / 2) return set_error(c, EVR_EINVAL, "evr_hpsi_noalloc: 1-D matrices too large");
-  if (c->gfly) return set_error(c, EVR_EINVAL, "evr_hpsi_noalloc: not for batched contexts");
+  if (c->gfly || c->batch) return set_error(c, EVR_EINVAL, "evr_hpsi_noalloc: not for batched contexts");
   EVR_CU((set_term_kernel_smem<double, false>(optin / 2, optin - 2048)), "attr");
   int* counter = reinterpret_cast<int*>(scratch);
   double* ht = reinterpret_cast<double*>(scratch + 256);
@@ -574,6 +681,8 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
   p.counter = counter;
   p.slab = slabp;
   p.slab_per_cta = (int64_t)slab;
+  p.smem_elems = (int64_t)((optin / 2) / sizeof(double));
+  p.err = counter + 2;
   p.x = x;
   p.ldx = ldx;
   p.ht = ht;
@@ -589,7 +698,7 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
   if (P.keo_type == 1)
     for (int i = 0; i < P.D; ++i)
       for (int j = i + 1; j < P.D; ++j) p.has_offdiag |= (P.G0[i + (size_t)P.D * j] != 0.0);
-  EVR_CU(cudaMemsetAsync(counter, 0, sizeof(int), s), "memset counter");  // the buffer keeps old contents
+  EVR_CU(cudaMemsetAsync(counter, 0, 4 * sizeof(int), s), "memset counter");  // the buffer keeps old contents
   EVR_CU((launch_items_kernel<double, false>(grid, optin / 2, s, p)), "hpsi_items_kernel launch");
   const int64_t N = P.Np * P.nb0;
   int rblocks = (int)std::min<int64_t>((N * nvec + 255) / 256, (int64_t)c->num_sms * 16);
@@ -600,3 +709,79 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
 }
 
 }  // namespace evr
+
+namespace {
+__global__ void autotune_fill(double* x, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = 1.0 / (1.0 + (double)((i * 2654435761u) % 1000));
+}
+}  // namespace
+
+// Autotuner of the work decomposition: the widest vector tile an item of the slab kernel
+// and of the general kernel may take (1..32).  Each candidate is timed with the events
+// around the term kernels (second of two H.psi calls on a fixed block); the slab cap is
+// chosen first with the general cap at its default, then the general cap.
+extern "C" int evr_autotune(evr_ctx* c, int nvec, int prec, int* caps, double* best_ms) {
+  using namespace evr;
+  if (!c) return EVR_EINVAL;
+  if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
+  if (nvec < 1 || nvec > kMaxBlock) return set_error(c, EVR_EINVAL, "evr_autotune: 1 <= nvec <= 64");
+  if (prec != EVR_PREC_FP64 && prec != EVR_PREC_FP32) return set_error(c, EVR_EINVAL, "unknown precision");
+  EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
+  const int64_t N = c->hp.Np * c->hp.nb0;
+  double* x = nullptr;
+  double* y = nullptr;
+  EVR_CU(cudaMalloc((void**)&x, sizeof(double) * N * nvec), "cudaMalloc");
+  if (cudaMalloc((void**)&y, sizeof(double) * N * nvec) != cudaSuccess) {
+    cudaFree(x);
+    (void)cudaGetLastError();
+    return set_error(c, EVR_ENOMEM, "evr_autotune: allocation");
+  }
+  autotune_fill<<<c->num_sms * 4, 256, 0, c->stream>>>(x, N * nvec);
+  auto time_it = [&](double& ms) -> int {
+    clear_item_sets(c);
+    float best = 1e30f;
+    for (int r = 0; r < 2; ++r) {
+      int rc = hpsi_interleaved(c, x, nvec, y, nvec, nvec, prec, c->stream, OP_H);
+      if (rc) return rc;
+      float a = 0.f;
+      EVR_CU(cudaEventSynchronize(c->ev[2]), "event sync");
+      EVR_CU(cudaEventElapsedTime(&a, c->ev[0], c->ev[1]), "event time");
+      if (r > 0) best = a;
+    }
+    ms = best;
+    return check_item_bounds(c);
+  };
+  const int cands[] = {32, 16, 8, 4, 2};
+  int rc = EVR_OK;
+  double best = 1e300;
+  int bs = c->vt_cap_slab, bi = c->vt_cap_items;
+  c->vt_cap_items = 32;
+  for (int cap : cands) {
+    c->vt_cap_slab = cap;
+    double ms;
+    if ((rc = time_it(ms))) break;
+    if (ms < best) { best = ms; bs = cap; }
+  }
+  if (!rc) {
+    c->vt_cap_slab = bs;
+    for (int cap : cands) {
+      c->vt_cap_items = cap;
+      double ms;
+      if ((rc = time_it(ms))) break;
+      if (ms < best) { best = ms; bi = cap; }
+    }
+  }
+  c->vt_cap_slab = bs;
+  c->vt_cap_items = bi;
+  clear_item_sets(c);
+  cudaFree(x);
+  cudaFree(y);
+  if (rc) return rc;
+  if (caps) {
+    caps[0] = bs;
+    caps[1] = bi;
+  }
+  if (best_ms) *best_ms = best;
+  return EVR_OK;
+}

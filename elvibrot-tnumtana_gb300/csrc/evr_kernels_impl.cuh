@@ -45,6 +45,11 @@ struct ItemParams {
   T vw, mw;
   const double* mu_dev;
   int keo_on;
+  // buffer bounds of an item, checked before it runs: elements of T in the dynamic shared
+  // memory and in the per-CTA global buffer; an item that would exceed them is skipped
+  // and flagged in *err (a host-side sizing error, reported by the host entry points)
+  int64_t smem_elems;
+  int* err;
 };
 
 // plain H: no dipole term, kinetic part on
@@ -448,6 +453,14 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
     }
     __syncthreads();
     const int D = s_term.D;
+    {
+      const int64_t need = (int64_t)(2 * nb0 + (p.keo_type == 10 ? D : 1)) * s_term.NQ * w.vt;
+      const int64_t mp = (s_term.msz + 3) & ~3;
+      if (mp > p.smem_elems || (w.smem ? mp + need > p.smem_elems : need > p.slab_per_cta)) {
+        if (threadIdx.x == 0) atomicExch(p.err, 1);
+        continue;
+      }
+    }
     T* const mb = reinterpret_cast<T*>(smem_raw);
     stage_matrices<T>(s_term, D, p.mats, mb, s_blocks);
     const TermDesc& Tm = s_term;
@@ -728,6 +741,18 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
     }
     __syncthreads();
     const int D = s_term.D, L = D - 1;
+    {
+      const int64_t ss0 = (int64_t)(s_term.NQ / s_term.nq[L]) * w.vt, tsz0 = ss0 * s_term.nb[L];
+      const int64_t ny = p.keo_type == 10 ? L : 1;
+      const int64_t need = max(2 * tsz0, tsz0 + (2 + ny) * ss0), mp = (s_term.msz + 3) & ~3;
+      const bool bad = w.smem == 3 ? (mp + (2 + ny) * ss0 > p.smem_elems || 3 * tsz0 > p.slab_per_cta)
+                                   : (mp + need + (w.smem == 2 ? tsz0 : 0) > p.smem_elems ||
+                                      (w.smem != 2 && tsz0 > p.slab_per_cta));
+      if (bad) {
+        if (threadIdx.x == 0) atomicExch(p.err, 1);
+        continue;
+      }
+    }
     T* const mb = reinterpret_cast<T*>(smem_raw);
     stage_matrices<T>(s_term, D, p.mats, mb, s_blocks);
     const TermDesc& Tm = s_term;
@@ -737,7 +762,17 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
     const int64_t ss = (int64_t)NQs * Vt;  // one slab array
     const int64_t tsz = ss * nL;           // T and W
     T* sm = reinterpret_cast<T*>(smem_raw) + ((Tm.msz + 3) & ~3);
-    T* Tg = p.slab + (int64_t)blockIdx.x * p.slab_per_cta;
+    // The partially transformed tensor Tg: after the phase buffers in shared memory
+    // (smem == 2) or in the CTA's global buffer.  smem == 3 (terms whose W does not fit):
+    // W and the ping-pong tensors of phases A and C also in the global buffer
+    // [Tg | W (= A ping) | A and C pong], only the slab arrays in shared memory.
+    const bool wg = w.smem == 3;
+    T* const gbuf = p.slab + (int64_t)blockIdx.x * p.slab_per_cta;
+    T* Tg = w.smem == 2 ? sm + max(2 * tsz, tsz + (2 + (p.keo_type == 10 ? L : 1)) * ss) : gbuf;
+    T* const wbuf = wg ? gbuf + tsz : sm;            // W, and the first ping-pong tensor
+    T* const pong = wg ? gbuf + 2 * tsz : sm + tsz;  // second ping-pong tensor of phases A and C
+    T* const slabs = wg ? sm : sm + tsz;             // Acc, P, Y
+    const FastDiv dvt((uint32_t)Vt);
 
     // ---- A: gather + B->G over positions 0..L-1
     if (L == 0) {
@@ -747,8 +782,8 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         Tg[i] = pk >= 0 ? (T)__ldg(p.x + (int64_t)pk * p.ldx + w.v0 + v) : T(0);
       }
     } else {
-      T* b0 = sm;
-      T* b1 = sm + tsz;
+      T* b0 = wbuf;
+      T* b1 = pong;
       int nb_rest = Tm.NB / Tm.nb[0];
       T* cur = (L == 1) ? Tg : b0;
       gather_contract<T>(p.x + w.v0, p.ldx, p.map + Tm.off_nb, 0, cur, Tm.nb[0], Tm.nq[0], nb_rest, Vt,
@@ -767,8 +802,8 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
     __syncthreads();
 
     // ---- B: stream the grid slabs of position L
-    T* W = sm;
-    T* Acc = sm + tsz;
+    T* W = wbuf;
+    T* Acc = slabs;
     T* P = Acc + ss;
     T* Y = P + ss;
     for (int64_t i = threadIdx.x; i < tsz; i += blockDim.x) W[i] = T(0);
@@ -784,10 +819,12 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
       if (p.mugrid) {
         const T* Mq = p.mugrid + Tm.off_nq + (int64_t)q * NQs;
         const T mw = p.mu_dev ? (T)__ldg(p.mu_dev) : p.mw;
-        for (int64_t a = threadIdx.x; a < ss; a += blockDim.x)
-          Acc[a] = fma(mw, __ldg(Mq + a / Vt), p.vw * __ldg(Vq + a / Vt)) * P[a];
+        for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) {
+          const int pt = (int)dvt.div((uint32_t)a);
+          Acc[a] = fma(mw, __ldg(Mq + pt), p.vw * __ldg(Vq + pt)) * P[a];
+        }
       } else {
-        for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) Acc[a] = __ldg(Vq + a / Vt) * P[a];
+        for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) Acc[a] = __ldg(Vq + dvt.div((uint32_t)a)) * P[a];
       }
       if (!p.keo_on) {
         __syncthreads();
@@ -879,7 +916,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
       }
     } else {
       T* b0 = W;
-      T* b1 = sm + tsz;
+      T* b1 = pong;
       T* cur = b0;
       int A = 1, Bq = NQs;
       for (int i = 0; i < L; ++i) {

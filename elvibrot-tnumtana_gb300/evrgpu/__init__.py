@@ -4,4 +4,4 @@
 operators and generates the seeded benchmark workloads.
 """
 from .spec import ProblemSpec, AU_TO_CM, AU_TO_EV, FS_TO_AU  # noqa: F401
-from .lib import Problem, EvrError, load, library_path, EXPORTS  # noqa: F401
+from .lib import Problem, BatchProblem, EvrError, load, library_path, EXPORTS  # noqa: F401

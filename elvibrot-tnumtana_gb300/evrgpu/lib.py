@@ -63,7 +63,7 @@ EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_
            "evr_last_kernel_ms",
            "evr_davidson",
            "evr_cheby_propagate", "evr_fma_peak", "evr_hpsi_noalloc", "evr_set_dipole", "evr_set_field",
-           "evr_oc_forward", "evr_oc_backward", "evr_create_batch", "evr_batch_offsets", "evr_batch_davidson"]
+           "evr_oc_forward", "evr_oc_backward", "evr_create_batch", "evr_batch_offsets", "evr_batch_davidson", "evr_autotune"]
 
 _lib = None
 
@@ -99,6 +99,7 @@ def load(build: bool = True):
     L.evr_set_kernel_path.argtypes = [vp, C.c_int]
     L.evr_fma_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.evr_hpsi_noalloc.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.c_int, vp]
+    L.evr_autotune.argtypes = [vp, C.c_int, C.c_int, _ip, _dp]
     L.evr_create_batch.argtypes = [C.POINTER(vp), C.POINTER(ProblemDesc), C.c_int, C.c_int]
     L.evr_batch_offsets.argtypes = [vp, _lp]
     L.evr_batch_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _dp, _lp]
@@ -339,6 +340,13 @@ class Problem:
         info = np.zeros(3, dtype=np.int64)
         self._check(load().evr_oc_backward(self.h, _p(grad, _dp), _p(ref, _dp), _p(info, _lp)))
         return grad, ref, dict(columns=int(info[0]), checkpoints=int(info[1]), segment=int(info[2]))
+
+    def autotune(self, nvec=64, prec="fp64"):
+        """Choose the vector-tile caps of the work items by timing; returns (slab cap, general cap, ms)."""
+        caps = np.zeros(2, dtype=np.int32)
+        ms = np.zeros(1)
+        self._check(load().evr_autotune(self.h, nvec, PREC[prec], _p(caps, _ip), _p(ms, _dp)))
+        return int(caps[0]), int(caps[1]), float(ms[0])
 
     def set_kernel_path(self, path):
         """1 or True (default): stage kernels for single-term problems, else the slab kernel

@@ -276,6 +276,34 @@ def oc_field(nsteps: int = 4000, dt: float = 5.0, seed: int = 0, n_sin: int = 8,
     return (amp * np.sin(np.outer(t, w) + ph[None, :])).sum(axis=1)
 
 
+def displaced_gaussian(spec: ProblemSpec, problem, modes, shift: float) -> np.ndarray:
+    """Harmonic ground state displaced by `shift` (dimensionless q) in `modes`, on the packed
+    basis of `problem`: product of coherent-state amplitudes e^{-a^2/2} a^k / sqrt(k!),
+    a = shift/sqrt(2), restricted to the packed functions and normalised (complex128)."""
+    packed = problem.tables()["packed"] - 1          # HO quantum numbers, Np x D
+    a = shift / math.sqrt(2.0)
+    kmax = int(packed.max()) + 1
+    lf = np.array([math.lgamma(k + 1.0) for k in range(kmax)])
+    amp = np.exp(-0.5 * a * a + np.arange(kmax) * math.log(a) - 0.5 * lf)
+    c = np.ones(len(packed))
+    for i in range(spec.D):
+        k = packed[:, i]
+        c *= amp[k] if i in modes else (k == 0).astype(float)
+    c = np.tile(c, spec.nb0) if spec.nb0 > 1 else c
+    return (c / np.linalg.norm(c)).astype(np.complex128)
+
+
+def spectral_bounds(spec: ProblemSpec, margin: float = 0.1):
+    """Bounds [emin, emax] of a harmonic-dominated SG4 Hamiltonian from its frequencies:
+    zero-point energy and the largest number of quanta of the packed basis (nb(l)-1 per
+    mode, sum of levels <= LB), widened by `margin` for the anharmonic couplings."""
+    w = np.asarray(spec.extra.get("omega", np.ones(spec.D)))
+    zpe = 0.5 * w.sum()
+    quanta = max(int(spec.Ab[i] + spec.Bb[i] * spec.LB) - 1 for i in range(spec.D))
+    top = zpe + quanta * w.max()
+    return zpe * (1.0 - margin), top * (1.0 + margin)
+
+
 def batched_systems(n: int = 256, seed: int = 2):
     """Uneven batch: D ~ U{3..6}, L ~ U{4..8}, each system seeded from ``seed``."""
     rng = np.random.default_rng(seed)
