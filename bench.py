@@ -167,9 +167,10 @@ def run_profile(args):
     return 0
 
 
-# DRAM bytes (read + write) of one FP64 64-vector launch of the term kernels, from the ncu
-# capture summarised in profiles/ (None until measured)
-TRAFFIC_PER_LAUNCH = None
+# DRAM bytes (read + write) of one FP64 64-vector launch of the term kernels: the D=6 L=6
+# capture of profiles/hpsi_slab_kernel_sg4_6d_l6.md (1.25 GB, dominated by the per-point
+# G table and V) scaled to the L=8 grid (37.77 M / 6.49 M points)
+TRAFFIC_PER_LAUNCH = 1.25e9 * 37.769167 / 6.487975
 DAV_LEVELS, DAV_BLOCK, DAV_RESI = 50, 64, 1e-7
 
 
@@ -230,8 +231,33 @@ def run_suite(args):
             sp = S.config_sg4_12d_l6()
             p = Problem(sp, device=0)
             psi0 = S.displaced_gaussian(sp, p, [0, 1, 2], 1.0)
-            emin, emax = S.spectral_bounds(sp)
-            out["N"] = int(p.N)
+            # spectral bounds of the Smolyak operator by power iterations on H and on
+            # (shift - H): the negative combination weights can put eigenvalues outside the
+            # harmonic estimate
+            rng = np.random.default_rng(0)
+            v = rng.standard_normal((p.N, 1))
+            for _ in range(150):
+                hv = p.hpsi(v)
+                top = float(np.vdot(v, hv).real / np.vdot(v, v).real)
+                v = hv / np.linalg.norm(hv)
+            shift = 1.02 * abs(top)
+            v = rng.standard_normal((p.N, 1))
+            for _ in range(150):
+                hv = shift * v - p.hpsi(v)
+                low = shift - float(np.vdot(v, hv).real / np.vdot(v, v).real)
+                v = hv / np.linalg.norm(hv)
+            span = top - low
+            emin, emax = low - 0.05 * span, top + 0.05 * span
+            out.update({"N": int(p.N), "emin": emin, "emax": emax})
+            for attempt in range(4):  # widen the bounds if the series meets a spectrum beyond them
+                try:
+                    p.chebyshev(psi0, 10.0, 2, emin, emax)
+                    break
+                except Exception:
+                    emin, emax = emin - 0.1 * (emax - emin), emax + 0.2 * (emax - emin)
+            out.update({"emin": emin, "emax": emax})
+            if args.autotune:
+                out["autotune"] = p.autotune(nvec=2, prec="fp64")
             for prec in ("fp64", "fp32"):
                 p.chebyshev(psi0, 10.0, 2, emin, emax, prec=prec)
                 t0 = time.perf_counter()
@@ -292,6 +318,7 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-davidson", action="store_true", help="skip the Davidson time-to-tolerance legs")
+    ap.add_argument("--autotune", action="store_true", help="tune the work decomposition before timing")
     ap.add_argument("--profile", default=None, choices=["sg4_6d_l6", "sg4_6d_l8"],
                     help="profiling mode: a few H.psi launches of the named workload, nothing else")
     ap.add_argument("--prec", default="both", choices=["both", "fp64", "fp32"], help="precision(s) in profiling mode")
@@ -336,6 +363,8 @@ def main():
     def step(prec, out):
         p.hpsi_device(x.data_ptr(), NVEC, out.data_ptr(), NVEC, NVEC, layout=E.LAYOUT_INTERLEAVED, prec=prec,
                       stream=stream)
+
+    tuned = p.autotune(nvec=NVEC, prec="fp64") if args.autotune else None
 
     for _ in range(args.warmup):
         step("fp64", y)
@@ -419,6 +448,7 @@ def main():
                          "peak_source": "FP64 FMA issue rate measured in this run (evr_fma_peak); no FP64 figure "
                                         "in the measured-peaks file"},
             "davidson": dav,
+            "autotune": tuned,
             "gpu_launches": launches,
             "clocks": clk.summary()}
     if rank == 0 and not args.no_cpu_baseline:

@@ -188,6 +188,7 @@ struct evr_ctx {
   bool use_stages = true;           // grid-wide stage path for single-term problems
   bool gfly = false;                // G(Q) from the linear model per point instead of a table
   int vt_cap_slab = 32, vt_cap_items = 32;  // widest vector tile of an item (evr_autotune)
+  int slab_min_points = 0;          // terms with fewer grid points x vectors run in the general kernel
   int64_t ws_gen = 0;               // bumped whenever workspace buffers are freed (captured graphs)
   std::vector<unsigned char> term_active;  // batches: terms to run (empty = all)
   int n_sys = 1;                    // problems stacked in this context (evr_create_batch)

@@ -326,7 +326,8 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
     if (Tm.weight == 0.0) continue;
     const size_t mats = (size_t)((Tm.msz + 3) & ~3) * esz;  // staged 1-D matrices
     if (mats > (size_t)w.smem_bytes) return set_error(c, EVR_EINVAL, "1-D matrices exceed shared memory");
-    if (slab_ok && slab_need_elems(P, Tm, 1) * esz + mats <= (size_t)w.smem_slab_bytes) {
+    const bool small = (int64_t)Tm.NQ * std::min(nvec, c->vt_cap_slab) < c->slab_min_points;
+    if (slab_ok && !small && slab_need_elems(P, Tm, 1) * esz + mats <= (size_t)w.smem_slab_bytes) {
       // FP32: the partially transformed tensor also in shared memory when a tile of
       // min(4, nvec) vectors fits (its per-slab re-reads then stay on the SM); FP64 keeps it
       // in the L2-resident global buffer, the FP64 pipe being the bound there
@@ -342,7 +343,7 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
       continue;
     }
     // W in global memory: the slab pipeline with only the slab arrays in shared memory
-    if (slab_ok && slab_wg_smem_elems(P, Tm, 1) * esz + mats <= (size_t)w.smem_slab_bytes &&
+    if (slab_ok && !small && slab_wg_smem_elems(P, Tm, 1) * esz + mats <= (size_t)w.smem_slab_bytes &&
         slab_wg_global_elems(Tm, 1) * esz <= w.slab_slab_bytes) {
       auto fits = [&](int v) {
         return slab_wg_smem_elems(P, Tm, v) * esz + mats <= (size_t)w.smem_slab_bytes &&
@@ -718,9 +719,10 @@ __global__ void autotune_fill(double* x, int64_t n) {
 }  // namespace
 
 // Autotuner of the work decomposition: the widest vector tile an item of the slab kernel
-// and of the general kernel may take (1..32).  Each candidate is timed with the events
-// around the term kernels (second of two H.psi calls on a fixed block); the slab cap is
-// chosen first with the general cap at its default, then the general cap.
+// and of the general kernel may take (2..32), and the size (grid points x tile) below which
+// a term runs in the general kernel's smaller CTAs.  Each candidate is timed with the
+// events around the term kernels (second of two H.psi calls on a fixed block), one
+// parameter at a time: slab cap, general cap, threshold.
 extern "C" int evr_autotune(evr_ctx* c, int nvec, int prec, int* caps, double* best_ms) {
   using namespace evr;
   if (!c) return EVR_EINVAL;
@@ -772,8 +774,21 @@ extern "C" int evr_autotune(evr_ctx* c, int nvec, int prec, int* caps, double* b
       if (ms < best) { best = ms; bi = cap; }
     }
   }
+  // small terms (grid points x tile below a threshold) in the general kernel's CTAs
+  int bm = c->slab_min_points;
+  if (!rc) {
+    c->vt_cap_items = bi;
+    const int thr[] = {0, 1024, 4096, 16384};
+    for (int t : thr) {
+      c->slab_min_points = t;
+      double ms;
+      if ((rc = time_it(ms))) break;
+      if (ms < best) { best = ms; bm = t; }
+    }
+  }
   c->vt_cap_slab = bs;
   c->vt_cap_items = bi;
+  c->slab_min_points = bm;
   clear_item_sets(c);
   cudaFree(x);
   cudaFree(y);
@@ -781,6 +796,7 @@ extern "C" int evr_autotune(evr_ctx* c, int nvec, int prec, int* caps, double* b
   if (caps) {
     caps[0] = bs;
     caps[1] = bi;
+    caps[2] = bm;
   }
   if (best_ms) *best_ms = best;
   return EVR_OK;

@@ -171,7 +171,9 @@ __device__ __forceinline__ void contract_m(const T* __restrict__ in, int64_t ldi
   const int ncol = A * B * Vt;
   const int ldm = (M + 3) & ~3;
   const FastDiv dv((uint32_t)Vt), da((uint32_t)A);
-  const int64_t istr = (int64_t)A * ldi, ostr = (int64_t)A * ldo;
+  // strides along the contracted and produced index: 32-bit (a tensor of one item holds
+  // fewer than 2^31 elements), so the per-load address arithmetic stays 32-bit
+  const int istr = (int)(A * ldi), ostr = (int)(A * ldo);
   for (int col0 = threadIdx.x; col0 < ncol; col0 += COLS * blockDim.x) {
     const T* ip[COLS];
     T* op[COLS];
@@ -605,12 +607,13 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
 template <typename T>
 __device__ __forceinline__ void slab_extract(const T* __restrict__ Tg, int64_t ss, int nL, const T* __restrict__ X,
                                              int ldx, T* __restrict__ P) {
-  for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) {
+  const int s32 = (int)ss;  // 32-bit index arithmetic (a slab tensor has < 2^31 elements)
+  for (int a = threadIdx.x; a < s32; a += blockDim.x) {
     T s = T(0);
     for (int k0 = 0; k0 < nL; k0 += 8) {
       T t[8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) t[j] = (k0 + j < nL) ? Tg[a + ss * (k0 + j)] : T(0);
+      for (int j = 0; j < 8; ++j) t[j] = (k0 + j < nL) ? Tg[a + s32 * (k0 + j)] : T(0);
 #pragma unroll
       for (int j = 0; j < 8; ++j)
         if (k0 + j < nL) s = fma(X[ldx * (k0 + j)], t[j], s);
@@ -631,12 +634,13 @@ __device__ __forceinline__ void slab_accumulate_m(T* __restrict__ W, int64_t ss,
     o[k] = k < nL ? c1 * O[k] : T(0);
     e[k] = (A2 && k < nL) ? c2 * E[k] : T(0);
   }
-  for (int64_t a = threadIdx.x; a < ss; a += blockDim.x) {
+  const int s32 = (int)ss;
+  for (int a = threadIdx.x; a < s32; a += blockDim.x) {
     const T u = A1[a];
     const T z = A2 ? A2[a] : T(0);
 #pragma unroll
     for (int k = 0; k < MAXL; ++k)
-      if (k < nL) W[a + ss * k] = fma(e[k], z, fma(o[k], u, W[a + ss * k]));
+      if (k < nL) W[a + s32 * k] = fma(e[k], z, fma(o[k], u, W[a + s32 * k]));
   }
 }
 

@@ -11,7 +11,8 @@
 // every later order; |phi_k| <= |psi| when the spectrum lies in [Emin, Emax]), so one
 // time step is a fixed launch sequence: it is captured once in a CUDA graph and replayed
 // for every step, with the autocorrelation <psi0|psi(t_n)> and |psi|^2 written to device
-// arrays and copied back at the end.  A norm growing beyond 1e-6 relative signals a
+// arrays and copied back at the end.  A norm moving by more than 1e-6 relative (1e-3 with
+// FP32 contractions) signals a
 // spectrum outside [Emin, Emax] (the reference retries with a larger Hmax, :4355-4362);
 // the call then returns EVR_ENOCONV with the step where it happened.
 #include <algorithm>
@@ -287,7 +288,9 @@ extern "C" int evr_cheby_propagate(evr_ctx* c, const double* psi0, int npsi, dou
   for (int st = 0; st <= nsteps && bad_step < 0; ++st)
     for (int p = 0; p < npsi; ++p) {
       const double n0 = ac[3 * p + 2], nn = ac[(size_t)3 * npsi * st + 3 * p + 2];
-      if (!(std::fabs(nn - n0) <= 1e-6 * n0 + 1e-300)) { bad_step = st; break; }
+      // FP32 contractions move the norm by ~1e-6 per step; divergence grows it without bound
+      const double ntol = prec == EVR_PREC_FP32 ? 1e-3 : 1e-6;
+      if (!(std::fabs(nn - n0) <= ntol * n0 + 1e-300)) { bad_step = st; break; }
     }
   if (autocorr)
     for (int st = 0; st <= nsteps; ++st)

@@ -342,11 +342,12 @@ class Problem:
         return grad, ref, dict(columns=int(info[0]), checkpoints=int(info[1]), segment=int(info[2]))
 
     def autotune(self, nvec=64, prec="fp64"):
-        """Choose the vector-tile caps of the work items by timing; returns (slab cap, general cap, ms)."""
-        caps = np.zeros(2, dtype=np.int32)
+        """Choose the work decomposition by timing; returns (slab cap, general cap,
+        small-term threshold, ms)."""
+        caps = np.zeros(3, dtype=np.int32)
         ms = np.zeros(1)
         self._check(load().evr_autotune(self.h, nvec, PREC[prec], _p(caps, _ip), _p(ms, _dp)))
-        return int(caps[0]), int(caps[1]), float(ms[0])
+        return int(caps[0]), int(caps[1]), int(caps[2]), float(ms[0])
 
     def set_kernel_path(self, path):
         """1 or True (default): stage kernels for single-term problems, else the slab kernel

@@ -158,8 +158,9 @@ int evr_hpsi_noalloc(evr_ctx *ctx, const double *psi, int64_t ld_psi, double *hp
 
 /* Autotuner (no counterpart in the reference; its Tune_SG4threads_HPsi, vib.f90:1598-1705,
  * tunes OpenMP thread counts): times the term kernels on an nvec-vector block for each
- * cap of the vector tile of a work item (1..32, slab kernel then general kernel) and keeps
- * the fastest for later calls.  caps[2] (optional): the chosen caps; best_ms: the time. */
+ * cap of the vector tile of a work item (2..32, slab kernel then general kernel) and for
+ * the size below which a term runs in the general kernel, and keeps the fastest for later
+ * calls.  caps[3] (optional): slab cap, general cap, size threshold; best_ms: the time. */
 int evr_autotune(evr_ctx *ctx, int nvec, int prec, int *caps, double *best_ms);
 
 /* Launch statistics of the last evr_hpsi_* call (kernels launched, work items). */

@@ -172,8 +172,8 @@ def test_operator_forms_direct_product(path):
 def test_autotune_keeps_results():
     spec, pg, po = problems("sg4_d4_l5_type10_g")
     pg.set_kernel_path(1)
-    cs, ci, ms = pg.autotune(nvec=16, prec="fp64")
-    assert cs in (2, 4, 8, 16, 32) and ci in (2, 4, 8, 16, 32) and ms > 0
+    cs, ci, thr, ms = pg.autotune(nvec=16, prec="fp64")
+    assert cs in (2, 4, 8, 16, 32) and ci in (2, 4, 8, 16, 32) and thr >= 0 and ms > 0
     rng = np.random.default_rng(21)
     psi = rng.standard_normal((pg.N, 16))
     assert rel(pg.hpsi(psi), po.hpsi(psi)) <= FP64_TOL
