@@ -142,22 +142,27 @@ def run_reference(args):
 
 
 def run_profile(args):
-    """A handful of H.psi launches (FP64 then FP32, 64 vectors) for ncu captures:
-    D=6 Smolyak level 6 (small case) or level 8 (the benchmark workload)."""
+    """A handful of H.psi launches (FP64 then FP32) for ncu captures: D=6 Smolyak level 6
+    (small case) or level 8 (the benchmark workload) on 64 vectors, or the D=3 direct
+    product (stage kernels) on 16 vectors."""
     import torch
     from evrgpu import Problem, spec as S
     import evrgpu.lib as E
 
-    spec = S.config_sg4(6, 6, seed=1) if args.profile == "sg4_6d_l6" else S.config_sg4_6d_l8()
+    nvec = NVEC
+    if args.profile == "dp3":  # direct product D=3 nb=20 nq=24: the stage kernels, 16 vectors
+        spec, nvec = S.config_dp3(), 16
+    else:
+        spec = S.config_sg4(6, 6, seed=1) if args.profile == "sg4_6d_l6" else S.config_sg4_6d_l8()
     p = Problem(spec, device=0)
-    x = torch.randn((p.N, NVEC), dtype=torch.float64, device="cuda")
+    x = torch.randn((p.N, nvec), dtype=torch.float64, device="cuda")
     y = torch.empty_like(x)
     st = torch.cuda.Stream()
     torch.cuda.set_stream(st)
     out, launches = {}, {}
     for prec in (("fp64", "fp32") if args.prec == "both" else (args.prec,)):
         for _ in range(args.steps):
-            p.hpsi_device(x.data_ptr(), NVEC, y.data_ptr(), NVEC, NVEC, layout=E.LAYOUT_INTERLEAVED, prec=prec,
+            p.hpsi_device(x.data_ptr(), nvec, y.data_ptr(), nvec, nvec, layout=E.LAYOUT_INTERLEAVED, prec=prec,
                           stream=st.cuda_stream)
         torch.cuda.synchronize()
         out[prec] = p.last_kernel_ms()[0]
@@ -319,7 +324,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-davidson", action="store_true", help="skip the Davidson time-to-tolerance legs")
     ap.add_argument("--autotune", action="store_true", help="tune the work decomposition before timing")
-    ap.add_argument("--profile", default=None, choices=["sg4_6d_l6", "sg4_6d_l8"],
+    ap.add_argument("--profile", default=None, choices=["sg4_6d_l6", "sg4_6d_l8", "dp3"],
                     help="profiling mode: a few H.psi launches of the named workload, nothing else")
     ap.add_argument("--prec", default="both", choices=["both", "fp64", "fp32"], help="precision(s) in profiling mode")
     ap.add_argument("--suite", default=None, choices=["dp3", "batch", "prop12d", "control", "all"],

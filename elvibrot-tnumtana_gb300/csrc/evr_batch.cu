@@ -53,14 +53,15 @@ __global__ void batch_vgrid_kernel(const TermDesc* __restrict__ terms, int t0, i
     const TermDesc& T = terms[lo];
     const int64_t q = gq - T.off_nq;
     const int NQ = T.NQ, D = T.D;
-    double Q[kMaxD];
+    double Q[kMaxD];  // dropped 1-point modes sit at Q = 0
+    for (int d = 0; d < kMaxD; ++d) Q[d] = 0.0;
     int64_t r = q;
     for (int d = 0; d < D; ++d) {
       Q[T.perm[d]] = mats[T.m_x[d] + (int)(r % T.nq[d])];
       r /= T.nq[d];
     }
     double* V = vgrid + T.off_nq * nb0 * nb0;
-    for (int ab = 0; ab < nb0 * nb0; ++ab) V[(int64_t)ab * NQ + q] = 0.0;
+    for (int ab = 0; ab < nb0 * nb0; ++ab) V[(int64_t)ab * NQ + q] = ab % (nb0 + 1) == 0 ? T.vshift : 0.0;
     for (int m = 0; m < n_mono; ++m) {
       double v = coef[m];
       for (int k = 0; k < 4; ++k) {

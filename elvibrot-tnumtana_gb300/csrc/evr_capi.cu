@@ -121,13 +121,16 @@ int evr_get_vgrid(const evr_ctx* c0, double* v) {
   EVR_CU(cudaMemcpyAsync(dev.data(), c->dp.vgrid, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
          "copy vgrid");
   EVR_CU(cudaStreamSynchronize(c->stream), "sync");
-  // device grid points follow each term's permuted mode order: back to the reference order
+  // device grid points follow each term's permuted mode order: back to the reference order;
+  // the device table holds V plus the constant of the term's dropped 1-point modes
   for (const TermDesc& T : P.terms)
-    for (int ab = 0; ab < nb2; ++ab)
+    for (int ab = 0; ab < nb2; ++ab) {
+      const double shift = ab % (P.nb0 + 1) == 0 ? T.vshift : 0.0;
       for (int64_t qp = 0; qp < T.NQ; ++qp) {
         const int64_t q = P.grid_perm[(size_t)T.off_nq + qp] - T.off_nq;
-        v[(size_t)T.off_nq * nb2 + (size_t)ab * T.NQ + q] = dev[(size_t)T.off_nq * nb2 + (size_t)ab * T.NQ + qp];
+        v[(size_t)T.off_nq * nb2 + (size_t)ab * T.NQ + q] = dev[(size_t)T.off_nq * nb2 + (size_t)ab * T.NQ + qp] - shift;
       }
+    }
   return EVR_OK;
 }
 

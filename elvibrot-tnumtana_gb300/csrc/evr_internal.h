@@ -49,10 +49,11 @@ struct TermDesc {
   // (basis <- grid), padded like the others
   int32_t m_x1L, m_x2L, m_e1L, m_e2L;
   int32_t msz;           // elements of the term's 1-D matrices staged in shared memory
-  int32_t D;             // modes of the term's problem
-  int32_t g0off, goff;   // offsets of the problem's G0 (D*D) and g (D*D*D) in the coefficient arrays
-  int32_t pad_;
-  double weight;
+  int32_t D;             // positions of the term (its modes minus the dropped 1-point ones)
+  int32_t g0off, goff;   // offsets of the problem's G0 (Dp*Dp) and g (Dp^3) in the coefficient arrays
+  int32_t Dp;            // modes of the term's problem (strides of G0, g; G-table slots per point)
+  double weight;         // Smolyak weight times the factors of the dropped 1-point modes
+  double vshift;         // constant added to V_aa: second derivatives of dropped modes (type 1)
 };
 
 // elements of one staged matrix block: rows padded to 4, times the columns

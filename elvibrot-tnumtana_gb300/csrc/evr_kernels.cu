@@ -56,11 +56,14 @@ __global__ void csr_reduce_kernel(const int64_t* __restrict__ ptr, const int64_t
   }
 }
 
-// grid tables: V_ab(Q) from monomials and the symmetric G(Q) = G0 + sum_k g_ijk Q_k
+// grid tables: V_ab(Q) from monomials (plus the term's constant of dropped 1-point modes on
+// the diagonal when with_shift) and the symmetric G(Q) = G0 + sum_k g_ijk Q_k over the
+// term's positions; the dropped modes sit at Q = 0
 __global__ void grid_eval_kernel(const TermDesc* __restrict__ terms, int n_terms, const double* __restrict__ mats,
                                  int64_t sum_nq, int D, int nb0, int n_mono, const double* __restrict__ coef,
                                  const int* __restrict__ midx, const int* __restrict__ melec, const double* __restrict__ G0,
-                                 const double* __restrict__ g, double* __restrict__ vgrid, double* __restrict__ ggrid) {
+                                 const double* __restrict__ g, double* __restrict__ vgrid, double* __restrict__ ggrid,
+                                 int with_shift) {
   for (int64_t gq = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; gq < sum_nq;
        gq += (int64_t)gridDim.x * blockDim.x) {
     int lo = 0, hi = n_terms - 1;  // last term with off_nq <= gq
@@ -72,13 +75,15 @@ __global__ void grid_eval_kernel(const TermDesc* __restrict__ terms, int n_terms
     int64_t q = gq - T.off_nq;
     const int NQ = T.NQ;
     double Q[kMaxD];  // coordinates in the reference's mode order
+    for (int d = 0; d < kMaxD; ++d) Q[d] = 0.0;
     int64_t r = q;
-    for (int d = 0; d < D; ++d) {
+    for (int d = 0; d < T.D; ++d) {
       Q[T.perm[d]] = mats[T.m_x[d] + (int)(r % T.nq[d])];
       r /= T.nq[d];
     }
     double* V = vgrid + T.off_nq * nb0 * nb0;
-    for (int ab = 0; ab < nb0 * nb0; ++ab) V[(int64_t)ab * NQ + q] = 0.0;
+    for (int ab = 0; ab < nb0 * nb0; ++ab)
+      V[(int64_t)ab * NQ + q] = (with_shift && ab % (nb0 + 1) == 0) ? T.vshift : 0.0;
     for (int m = 0; m < n_mono; ++m) {
       double v = coef[m];
       for (int k = 0; k < 4; ++k) {
@@ -91,8 +96,8 @@ __global__ void grid_eval_kernel(const TermDesc* __restrict__ terms, int n_terms
       const int nG = D * (D + 1) / 2;
       double* Gp = ggrid + T.off_nq * nG + q;
       int c = 0;
-      for (int i = 0; i < D; ++i)  // (i, j) positions of the term's mode order
-        for (int j = i; j < D; ++j) {
+      for (int i = 0; i < T.D; ++i)  // (i, j) positions of the term's mode order
+        for (int j = i; j < T.D; ++j) {
           const int oi = T.perm[i], oj = T.perm[j];
           double s = G0[oi + D * oj];
           for (int k = 0; k < D; ++k) s += g[oi + D * (oj + D * k)] * Q[k];
@@ -196,7 +201,7 @@ int upload_problem(evr_ctx* c) {
   c->dp_ggrid = gg;
   grid_eval_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(d.terms, (int)P.terms.size(), d.mats, P.sum_nq, D, nb0,
                                                           (int)P.mono_coef.size(), d.mono_coef, d.mono_idx,
-                                                          d.mono_elec, d.G0, d.g, d.vgrid, gg);
+                                                          d.mono_elec, d.G0, d.g, d.vgrid, gg, 1);
   EVR_CU(cudaGetLastError(), "grid_eval_kernel");
   // FP32 copies for the mixed-precision contractions
   EVR_CU(cudaMalloc((void**)&d.mats32, P.mat_pool.size() * sizeof(float) + 16), "cudaMalloc mats32");
@@ -619,7 +624,7 @@ int eval_grid_monomials(evr_ctx* c, int n_mono, const double* coef, const int* i
   const HostProblem& P = c->hp;
   grid_eval_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(c->dp.terms, (int)P.terms.size(), c->dp.mats, P.sum_nq,
                                                           P.D, P.nb0, n_mono, coef, idx, elec, c->dp.G0, c->dp.g,
-                                                          out, nullptr);
+                                                          out, nullptr, 0);
   EVR_CU(cudaGetLastError(), "grid_eval_kernel");
   if (maxnorm) {
     unsigned long long* d = nullptr;

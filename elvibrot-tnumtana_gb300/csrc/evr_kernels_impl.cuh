@@ -363,12 +363,12 @@ __device__ __forceinline__ void point_coords(const ItemParams<T>& p, const TermD
 template <typename T, int DM>
 __device__ __forceinline__ T g_model(const ItemParams<T>& p, const TermDesc& Tm, const double (&xq)[DM], int i,
                                      int j) {
-  const int D = Tm.D, oi = Tm.perm[i], oj = Tm.perm[j];
-  double s = __ldg(p.G0 + Tm.g0off + oi + D * oj);
-  const double* gp = p.gco + Tm.goff + oi + D * oj;
+  const int D = Tm.D, Dp = Tm.Dp, oi = Tm.perm[i], oj = Tm.perm[j];
+  double s = __ldg(p.G0 + Tm.g0off + oi + Dp * oj);
+  const double* gp = p.gco + Tm.goff + oi + Dp * oj;
 #pragma unroll
-  for (int k = 0; k < DM; ++k)
-    if (k < D) s = fma(__ldg(gp + D * D * Tm.perm[k]), xq[k], s);
+  for (int k = 0; k < DM; ++k)  // dropped 1-point modes sit at Q = 0
+    if (k < D) s = fma(__ldg(gp + Dp * Dp * Tm.perm[k]), xq[k], s);
   return (T)s;
 }
 
@@ -380,7 +380,7 @@ template <typename T, int DM, bool GFLY>
 __device__ __forceinline__ void items_pointwise_G(const ItemParams<T>& p, const TermDesc& Tm, T* Y, int64_t stride,
                                                   int Vt, int NQ) {
   const int D = Tm.D;
-  const int nG = D * (D + 1) / 2;
+  const int nG = Tm.Dp * (Tm.Dp + 1) / 2;  // the table reserves the problem's slots per point
   constexpr bool kCache = DM <= (sizeof(T) == 4 ? 8 : 6);
   constexpr int kG = kCache ? DM * (DM + 1) / 2 : 1;
   const int nch = max(1, min(Vt, (int)blockDim.x / max(NQ, 1)));
@@ -393,7 +393,7 @@ __device__ __forceinline__ void items_pointwise_G(const ItemParams<T>& p, const 
     auto gget = [&](int i, int j) -> T {
       if (i >= D || j >= D) return T(0);
       if constexpr (GFLY) return g_model<T, DM>(p, Tm, xq, i, j);
-      return Gp ? __ldg(Gp + (int64_t)slot(i, j) * NQ) : (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[j]);
+      return Gp ? __ldg(Gp + (int64_t)slot(i, j) * NQ) : (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]);
     };
     T G[kG];
     if constexpr (kCache) {
@@ -551,7 +551,7 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
         int A = 1, Bq = NQ;
         for (int i = 0; i < D; ++i) {
           Bq /= Tm.nq[i];
-          const T f = (T)(-0.5 * __ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[i]));
+          const T f = (T)(-0.5 * __ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[i]));
           if (f != T(0))
             contract<T>(P0, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d2[i], f, true);
           __syncthreads();
@@ -564,7 +564,7 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
             int Aj = Ai * Tm.nq[i];
             for (int j = i + 1; j < D; ++j) {
               const int Bj = NQ / (Aj * Tm.nq[j]);
-              const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[j]));
+              const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]));
               if (f != T(0)) {
                 contract<T>(P0, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, mb + Tm.m_d1[i], T(1), false);
                 __syncthreads();
@@ -678,7 +678,7 @@ __device__ __forceinline__ void slab_pointwise_G(const ItemParams<T>& p, const T
     auto gload = [&](int i, int j) -> T {
       if (i >= D || j >= D) return T(0);
       if constexpr (GFLY) return g_model<T, DM>(p, Tm, xq, i, j);
-      return Gp ? __ldg(Gp + (int64_t)slot(i, j) * Tm.NQ) : (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[j]);
+      return Gp ? __ldg(Gp + (int64_t)slot(i, j) * Tm.NQ) : (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]);
     };
     if constexpr (kCache) {
 #pragma unroll
@@ -814,7 +814,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
     const int ldx0 = (gL + 3) & ~3, ldo = (nL + 3) & ~3;
     const T* X0 = mb + Tm.m_d0b[L];
     const T* OUT = mb + Tm.m_bgw[L];
-    const int nG = D * (D + 1) / 2;
+    const int nG = Tm.Dp * (Tm.Dp + 1) / 2;  // G-table slots per point (term offset)
     for (int q = 0; q < gL; ++q) {
       __syncthreads();
       slab_extract<T>(Tg, ss, nL, X0 + q, ldx0, P);
@@ -865,7 +865,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         int A = 1, Bq = NQs;
         for (int i = 0; i < L; ++i) {  // Acc += F2_ii d2_i P
           Bq /= Tm.nq[i];
-          const T f = (T)(-0.5 * __ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[i]));
+          const T f = (T)(-0.5 * __ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[i]));
           if (f != T(0))
             contract<T>(P, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d2[i], f, true);
           __syncthreads();
@@ -878,7 +878,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
             int Aj = Ai * Tm.nq[i];
             for (int j = i + 1; j < L; ++j) {
               const int Bj = NQs / (Aj * Tm.nq[j]);
-              const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[j]));
+              const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]));
               if (f != T(0)) {
                 contract<T>(P, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, mb + Tm.m_d1[i], T(1), false);
                 __syncthreads();
@@ -890,14 +890,14 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
             Ai *= Tm.nq[i];
           }
         }
-        const T fLL = (T)(-0.5 * __ldg(p.G0 + Tm.g0off + Tm.perm[L] + D * Tm.perm[L]));
+        const T fLL = (T)(-0.5 * __ldg(p.G0 + Tm.g0off + Tm.perm[L] + Tm.Dp * Tm.perm[L]));
         slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), mb + Tm.m_e2L + (int64_t)ldo * q, P,
                            fLL);
         if (p.has_offdiag) {  // F2_iL d1_i d_L: d_L through (bgw.d1)_L on the way back
           int Ai = 1;
           for (int i = 0; i < L; ++i) {
             const int Bi = NQs / (Ai * Tm.nq[i]);
-            const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + D * Tm.perm[L]));
+            const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[L]));
             if (f != T(0)) {
               __syncthreads();
               contract<T>(P, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, mb + Tm.m_d1[i], T(1), false);

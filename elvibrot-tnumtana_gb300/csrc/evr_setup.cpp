@@ -212,6 +212,60 @@ void smolyak_terms(int D, int Lmax, std::vector<int>& out) {
 
 }  // namespace
 
+// Drops the positions of 1-point modes from every SG4 term: nq = nb = 1 with the grid node
+// at 0 and a zero first derivative (the level-0 modes of L_TO_nq_A = 1 rules).  Such a mode
+// multiplies the term's operator by d0b*bgw (folded into the term weight), its first
+// derivatives vanish (type 10 and the off-diagonal type-1 terms), and its second
+// derivative adds the constant -1/2 G0_ii d2gg to V_aa (type 1, `vshift`).  Term-local
+// indices do not change (the dropped factors have size 1), so the map and the grids stay.
+// The position with the most grid points stays last (a term of 1-point modes only keeps it).
+static void compact_trivial_modes(HostProblem& P) {
+  const int D = P.D;
+  for (size_t t = 0; t < P.terms.size(); ++t) {
+    TermDesc& T = P.terms[t];
+    TermDesc& TT = P.termsT[t];
+    T.Dp = TT.Dp = D;
+    T.vshift = TT.vshift = 0.0;
+    if (P.kind != EVR_BASIS_SG4) continue;
+    int keep[kMaxD], nk = 0;
+    double scale = 1.0, shift = 0.0;
+    for (int p = 0; p < D; ++p) {
+      const int i = T.perm[p];
+      const Basis1D& b = P.bas[i][P.term_l[t * D + i]];
+      const bool trivial = b.nq == 1 && b.nb == 1 && b.x[0] == 0.0 &&
+                           std::fabs(b.d1gg[0]) <= 1e-14 * std::max(1.0, std::fabs(b.d2gg[0]));
+      if (trivial && !(p == D - 1 && nk == 0)) {
+        scale *= b.d0b[0] * b.bgw[0];
+        if (P.keo_type == 1) shift += -0.5 * P.G0[i + (size_t)D * i] * b.d2gg[0];
+      } else {
+        keep[nk++] = p;
+      }
+    }
+    if (nk == D) continue;
+    auto squeeze = [&](TermDesc& X) {
+      const TermDesc Y = X;
+      for (int k = 0; k < kMaxD; ++k) {
+        const bool on = k < nk;
+        const int p = on ? keep[k] : 0;
+        X.nb[k] = on ? Y.nb[p] : 0;
+        X.nq[k] = on ? Y.nq[p] : 0;
+        X.perm[k] = on ? Y.perm[p] : 0;
+        X.m_d0b[k] = on ? Y.m_d0b[p] : 0;
+        X.m_bgw[k] = on ? Y.m_bgw[p] : 0;
+        X.m_d1[k] = on ? Y.m_d1[p] : 0;
+        X.m_d2[k] = on ? Y.m_d2[p] : 0;
+        X.m_x[k] = on ? Y.m_x[p] : 0;
+      }
+      X.D = nk;
+      X.msz = term_matrix_elems(X, nk);
+      X.weight = Y.weight * scale;
+      X.vshift = shift;
+    };
+    squeeze(T);
+    squeeze(TT);
+  }
+}
+
 int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& err) {
   if (!d) { err = "null problem description"; return EVR_EINVAL; }
   const int D = d->D;
@@ -470,8 +524,50 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
     }
   }
 
-  // CSR transpose over N = Np*nb0 rows, sources in the term-basis output buffer
   const int nb0 = P.nb0;
+  // operator
+  P.mono_coef.assign(d->mono_coef, d->mono_coef + d->n_mono);
+  P.mono_idx.assign(d->mono_idx, d->mono_idx + 4 * (size_t)d->n_mono);
+  if (d->mono_elec) P.mono_elec.assign(d->mono_elec, d->mono_elec + 2 * (size_t)d->n_mono);
+  else P.mono_elec.assign(2 * (size_t)d->n_mono, 0);
+  for (int m = 0; m < d->n_mono; ++m) {
+    for (int k = 0; k < 4; ++k)
+      if (P.mono_idx[4 * m + k] >= D || P.mono_idx[4 * m + k] < -1) { err = "monomial mode index out of range"; return EVR_EINVAL; }
+    if (P.mono_elec[2 * m] < 0 || P.mono_elec[2 * m] >= nb0 || P.mono_elec[2 * m + 1] < 0 || P.mono_elec[2 * m + 1] >= nb0) {
+      err = "monomial electronic index out of range"; return EVR_EINVAL;
+    }
+  }
+  P.G0.assign((size_t)D * D, 0.0);
+  if (d->G0) P.G0.assign(d->G0, d->G0 + (size_t)D * D);
+  else for (int i = 0; i < D; ++i) P.G0[i + (size_t)D * i] = 1.0;
+  P.g.assign((size_t)D * D * D, 0.0);
+  if (d->g) P.g.assign(d->g, d->g + (size_t)D * D * D);
+
+  // algorithmic FLOP of one H.psi on one real vector: contraction chain B->G and G->B,
+  // 2D first-derivative passes (type 10) or D second-derivative passes (type 1),
+  // pointwise G/V terms.
+  double fl = 0.0;
+  for (int t = 0; t < nterm; ++t) {
+    const TermDesc& T = P.terms[t];
+    double c = 0.0, a = 1.0;
+    for (int i = 0; i < D; ++i) {
+      double rest = 1.0;
+      for (int j = i + 1; j < D; ++j) rest *= T.nb[j];
+      c += a * T.nq[i] * T.nb[i] * rest;
+      a *= T.nq[i];
+    }
+    double bg = 2.0 * c * nb0;                      // B->G and G->B, FMA counted as 2 FLOP below
+    double der = 0.0;
+    for (int i = 0; i < D; ++i) der += (double)T.NQ * T.nq[i];
+    der *= (P.keo_type == 10 ? 2.0 : 1.0) * nb0;
+    double pw = (P.keo_type == 10 ? (double)D * D + D : 0.0) * T.NQ * nb0 + (double)nb0 * nb0 * T.NQ;
+    fl += 2.0 * (bg + der + pw);
+  }
+  P.flop_per_hpsi = fl;
+
+  compact_trivial_modes(P);
+
+  // CSR transpose over N = Np*nb0 rows, sources in the term-basis output buffer
   const int64_t N = P.Np * nb0;
   std::vector<int64_t> cnt(N + 1, 0);
   for (int t = 0; t < nterm; ++t) {
@@ -500,24 +596,6 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
       }
   }
 
-  // operator
-  P.mono_coef.assign(d->mono_coef, d->mono_coef + d->n_mono);
-  P.mono_idx.assign(d->mono_idx, d->mono_idx + 4 * (size_t)d->n_mono);
-  if (d->mono_elec) P.mono_elec.assign(d->mono_elec, d->mono_elec + 2 * (size_t)d->n_mono);
-  else P.mono_elec.assign(2 * (size_t)d->n_mono, 0);
-  for (int m = 0; m < d->n_mono; ++m) {
-    for (int k = 0; k < 4; ++k)
-      if (P.mono_idx[4 * m + k] >= D || P.mono_idx[4 * m + k] < -1) { err = "monomial mode index out of range"; return EVR_EINVAL; }
-    if (P.mono_elec[2 * m] < 0 || P.mono_elec[2 * m] >= nb0 || P.mono_elec[2 * m + 1] < 0 || P.mono_elec[2 * m + 1] >= nb0) {
-      err = "monomial electronic index out of range"; return EVR_EINVAL;
-    }
-  }
-  P.G0.assign((size_t)D * D, 0.0);
-  if (d->G0) P.G0.assign(d->G0, d->G0 + (size_t)D * D);
-  else for (int i = 0; i < D; ++i) P.G0[i + (size_t)D * i] = 1.0;
-  P.g.assign((size_t)D * D * D, 0.0);
-  if (d->g) P.g.assign(d->g, d->g + (size_t)D * D * D);
-
   // zero-order diagonal for the Davidson preconditioner: separable harmonic energies
   // E0(n) = sum_i G0_ii scaleQ_i^2 (n_i - 1/2) plus the constant part of V_aa.
   P.e0diag.assign((size_t)N, 0.0);
@@ -533,27 +611,6 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
     for (int a = 0; a < nb0; ++a) P.e0diag[k + P.Np * a] = e + vconst[a];
   }
 
-  // algorithmic FLOP of one H.psi on one real vector: contraction chain B->G and G->B,
-  // 2D first-derivative passes (type 10) or D second-derivative passes (type 1),
-  // pointwise G/V terms.
-  double fl = 0.0;
-  for (int t = 0; t < nterm; ++t) {
-    const TermDesc& T = P.terms[t];
-    double c = 0.0, a = 1.0;
-    for (int i = 0; i < D; ++i) {
-      double rest = 1.0;
-      for (int j = i + 1; j < D; ++j) rest *= T.nb[j];
-      c += a * T.nq[i] * T.nb[i] * rest;
-      a *= T.nq[i];
-    }
-    double bg = 2.0 * c * nb0;                      // B->G and G->B, FMA counted as 2 FLOP below
-    double der = 0.0;
-    for (int i = 0; i < D; ++i) der += (double)T.NQ * T.nq[i];
-    der *= (P.keo_type == 10 ? 2.0 : 1.0) * nb0;
-    double pw = (P.keo_type == 10 ? (double)D * D + D : 0.0) * T.NQ * nb0 + (double)nb0 * nb0 * T.NQ;
-    fl += 2.0 * (bg + der + pw);
-  }
-  P.flop_per_hpsi = fl;
   return EVR_OK;
 }
 
