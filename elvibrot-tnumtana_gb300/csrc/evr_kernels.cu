@@ -247,19 +247,20 @@ void free_workspace(evr_ctx* c) {
 }
 
 // elements of shared memory the slab kernel needs for a term and a vector tile
-static size_t slab_need_elems(const HostProblem& P, const TermDesc& Tm, int vt) {
+static size_t slab_need_elems(const HostProblem& P, const TermDesc& Tm, int vt, bool fp32) {
   const int L = Tm.D - 1;  // the term's own mode count (stacked problems differ)
   const size_t ss = (size_t)(Tm.NQ / Tm.nq[L]) * vt, tsz = ss * Tm.nb[L];
-  const size_t ny = (P.keo_type == 10) ? (size_t)L : 1;
+  // type 10: the first derivatives, and d_L psi in FP32 (fused extraction)
+  const size_t ny = (P.keo_type == 10) ? (size_t)L + (fp32 ? 1 : 0) : 1;
   return std::max(2 * tsz, tsz + (2 + ny) * ss);
 }
 
 // W-in-global mode of the slab kernel: shared memory holds only the slab arrays, the
 // global buffer Tg, W and one ping-pong tensor (3 tensors of NQs*nb_L*vt)
-static size_t slab_wg_smem_elems(const HostProblem& P, const TermDesc& Tm, int vt) {
+static size_t slab_wg_smem_elems(const HostProblem& P, const TermDesc& Tm, int vt, bool fp32) {
   const int L = Tm.D - 1;
   const size_t ss = (size_t)(Tm.NQ / Tm.nq[L]) * vt;
-  return (2 + ((P.keo_type == 10) ? (size_t)L : 1)) * ss;
+  return (2 + ((P.keo_type == 10) ? (size_t)L + (fp32 ? 1 : 0) : 1)) * ss;
 }
 static size_t slab_wg_global_elems(const TermDesc& Tm, int vt) {
   const int L = Tm.D - 1;
@@ -297,8 +298,8 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
       for (const TermDesc& Tm : P.terms) {
         if (Tm.weight == 0.0) continue;
         const size_t mats = (size_t)((Tm.msz + 3) & ~3) * sizeof(double);
-        if (slab_need_elems(P, Tm, 1) * sizeof(double) + mats <= (size_t)w.smem_slab_bytes) continue;
-        if (slab_wg_smem_elems(P, Tm, 1) * sizeof(double) + mats > (size_t)w.smem_slab_bytes) continue;
+        if (slab_need_elems(P, Tm, 1, false) * sizeof(double) + mats <= (size_t)w.smem_slab_bytes) continue;
+        if (slab_wg_smem_elems(P, Tm, 1, false) * sizeof(double) + mats > (size_t)w.smem_slab_bytes) continue;
         sb = std::max(sb, slab_wg_global_elems(Tm, 1) * sizeof(double));
       }
     w.slab_slab_bytes = (sb + 255) & ~(size_t)255;
@@ -324,6 +325,7 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
   for (const ItemSet& s : w.sets)
     if (s.nvec == nvec && s.prec == prec) return EVR_OK;
   const size_t esz = prec == EVR_PREC_FP32 ? sizeof(float) : sizeof(double);
+  const bool f32 = prec == EVR_PREC_FP32;
   const bool slab_ok = P.nb0 == 1 && c->use_slab;
   std::vector<WorkItem> items, sitems;
   for (int t = 0; t < (int)P.terms.size(); ++t) {
@@ -332,14 +334,14 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
     const size_t mats = (size_t)((Tm.msz + 3) & ~3) * esz;  // staged 1-D matrices
     if (mats > (size_t)w.smem_bytes) return set_error(c, EVR_EINVAL, "1-D matrices exceed shared memory");
     const bool small = (int64_t)Tm.NQ * std::min(nvec, c->vt_cap_slab) < c->slab_min_points;
-    if (slab_ok && !small && slab_need_elems(P, Tm, 1) * esz + mats <= (size_t)w.smem_slab_bytes) {
+    if (slab_ok && !small && slab_need_elems(P, Tm, 1, f32) * esz + mats <= (size_t)w.smem_slab_bytes) {
       // FP32: the partially transformed tensor also in shared memory when a tile of
       // min(4, nvec) vectors fits (its per-slab re-reads then stay on the SM); FP64 keeps it
       // in the L2-resident global buffer, the FP64 pipe being the bound there
       const int L = Tm.D - 1;
       auto tg_elems = [&](int v) { return (size_t)(Tm.NQ / Tm.nq[L]) * v * Tm.nb[L]; };
       auto fits = [&](int v, bool tg) {
-        return (slab_need_elems(P, Tm, v) + (tg ? tg_elems(v) : 0)) * esz + mats <= (size_t)w.smem_slab_bytes;
+        return (slab_need_elems(P, Tm, v, f32) + (tg ? tg_elems(v) : 0)) * esz + mats <= (size_t)w.smem_slab_bytes;
       };
       const bool tg = prec == EVR_PREC_FP32 && fits(std::min(4, nvec), true);
       int vt = 1;
@@ -348,10 +350,10 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
       continue;
     }
     // W in global memory: the slab pipeline with only the slab arrays in shared memory
-    if (slab_ok && !small && slab_wg_smem_elems(P, Tm, 1) * esz + mats <= (size_t)w.smem_slab_bytes &&
+    if (slab_ok && !small && slab_wg_smem_elems(P, Tm, 1, f32) * esz + mats <= (size_t)w.smem_slab_bytes &&
         slab_wg_global_elems(Tm, 1) * esz <= w.slab_slab_bytes) {
       auto fits = [&](int v) {
-        return slab_wg_smem_elems(P, Tm, v) * esz + mats <= (size_t)w.smem_slab_bytes &&
+        return slab_wg_smem_elems(P, Tm, v, f32) * esz + mats <= (size_t)w.smem_slab_bytes &&
                slab_wg_global_elems(Tm, v) * esz <= w.slab_slab_bytes;
       };
       int vt = 1;

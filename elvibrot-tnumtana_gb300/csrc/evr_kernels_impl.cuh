@@ -622,6 +622,38 @@ __device__ __forceinline__ void slab_extract(const T* __restrict__ Tg, int64_t s
   }
 }
 
+// One pass over the partially transformed tensor for the type-10 slab: psi (row X of the
+// grid<-basis matrix) and its derivative along the streamed position (row X1 of d1.d0b) on
+// the slab, and Acc = (vw V + mw mu) psi
+template <typename T>
+__device__ __forceinline__ void slab_extract_fused(const T* __restrict__ Tg, int64_t ss, int nL,
+                                                   const T* __restrict__ X, const T* __restrict__ X1, int ldx,
+                                                   T* __restrict__ P, T* __restrict__ P1, T* __restrict__ Acc,
+                                                   const T* __restrict__ Vq, const T* __restrict__ Mq, T vw, T mw,
+                                                   const FastDiv& dvt) {
+  const int s32 = (int)ss;
+  for (int a = threadIdx.x; a < s32; a += blockDim.x) {
+    T s = T(0), s1 = T(0);
+    for (int k0 = 0; k0 < nL; k0 += 8) {
+      T t[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) t[j] = (k0 + j < nL) ? Tg[a + s32 * (k0 + j)] : T(0);
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (k0 + j < nL) {
+          s = fma(X[ldx * (k0 + j)], t[j], s);
+          s1 = fma(X1[ldx * (k0 + j)], t[j], s1);
+        }
+    }
+    P[a] = s;
+    P1[a] = s1;
+    const int pt = (int)dvt.div((uint32_t)a);
+    T v = __ldg(Vq + pt);
+    if (Mq) v = fma(mw, __ldg(Mq + pt), vw * v);
+    Acc[a] = v * s;
+  }
+}
+
 // W[a + ss*k] += c1*O[k]*A1[a] + c2*E[k]*A2[a]  for k < nL (A2 may be null): the slab's
 // image under G->B of the streamed position
 template <typename T, int MAXL>
@@ -663,7 +695,11 @@ __device__ __forceinline__ void slab_pointwise_G(const ItemParams<T>& p, const T
   // D <= 8 in FP32)
   constexpr bool kCache = DM <= (sizeof(T) == 4 ? 8 : 6);
   constexpr int kG = kCache ? DM * (DM + 1) / 2 : 1;
-  for (int pt = threadIdx.x; pt < NQs; pt += blockDim.x) {
+  // a thread owns a point and a residue class of the tile's vectors: with fewer points in
+  // the slab than threads, several threads share a point (each loads its G)
+  const int nch = max(1, min(Vt, (int)blockDim.x / max(NQs, 1)));
+  for (int task = threadIdx.x; task < NQs * nch; task += blockDim.x) {
+    const int pt = task / nch, ch = task - pt * nch;
     T G[kG];
     const T* Gp = p.ggrid ? p.ggrid + Tm.off_nq * nG + (int64_t)q * NQs + pt : nullptr;
     double xq[DM];
@@ -686,7 +722,7 @@ __device__ __forceinline__ void slab_pointwise_G(const ItemParams<T>& p, const T
 #pragma unroll
         for (int j = i; j < DM; ++j) G[i * DM - i * (i - 1) / 2 + (j - i)] = gload(i, j);
     }
-    for (int v = 0; v < Vt; ++v) {
+    for (int v = ch; v < Vt; v += nch) {
       const int64_t a = (int64_t)pt * Vt + v;
       T y[DM], z[DM];
 #pragma unroll
@@ -747,7 +783,8 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
     const int D = s_term.D, L = D - 1;
     {
       const int64_t ss0 = (int64_t)(s_term.NQ / s_term.nq[L]) * w.vt, tsz0 = ss0 * s_term.nb[L];
-      const int64_t ny = p.keo_type == 10 ? L : 1;
+      // type 10: the first derivatives, and d_L psi in FP32 (fused extraction)
+      const int64_t ny = p.keo_type == 10 ? L + (sizeof(T) == 4 ? 1 : 0) : 1;
       const int64_t need = max(2 * tsz0, tsz0 + (2 + ny) * ss0), mp = (s_term.msz + 3) & ~3;
       const bool bad = w.smem == 3 ? (mp + (2 + ny) * ss0 > p.smem_elems || 3 * tsz0 > p.slab_per_cta)
                                    : (mp + need + (w.smem == 2 ? tsz0 : 0) > p.smem_elems ||
@@ -772,7 +809,8 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
     // [Tg | W (= A ping) | A and C pong], only the slab arrays in shared memory.
     const bool wg = w.smem == 3;
     T* const gbuf = p.slab + (int64_t)blockIdx.x * p.slab_per_cta;
-    T* Tg = w.smem == 2 ? sm + max(2 * tsz, tsz + (2 + (p.keo_type == 10 ? L : 1)) * ss) : gbuf;
+    T* Tg = w.smem == 2 ? sm + max(2 * tsz, tsz + (2 + (p.keo_type == 10 ? L + (sizeof(T) == 4 ? 1 : 0) : 1)) * ss)
+                        : gbuf;
     T* const wbuf = wg ? gbuf + tsz : sm;            // W, and the first ping-pong tensor
     T* const pong = wg ? gbuf + 2 * tsz : sm + tsz;  // second ping-pong tensor of phases A and C
     T* const slabs = wg ? sm : sm + tsz;             // Acc, P, Y
@@ -817,6 +855,41 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
     const int nG = Tm.Dp * (Tm.Dp + 1) / 2;  // G-table slots per point (term offset)
     for (int q = 0; q < gL; ++q) {
       __syncthreads();
+      if (sizeof(T) == 4 && p.keo_on && p.keo_type == 10) {
+        // FP32: psi, d_L psi (kept in Y[L], later Phi_L) and Acc = V psi in one pass (FP64
+        // keeps the two passes below, with fewer live registers)
+        T* P1 = Y + (int64_t)L * ss;
+        const T* Mq = p.mugrid ? p.mugrid + Tm.off_nq + (int64_t)q * NQs : nullptr;
+        const T mw = p.mu_dev ? (T)__ldg(p.mu_dev) : p.mw;
+        slab_extract_fused<T>(Tg, ss, nL, X0 + q, mb + Tm.m_x1L + q, ldx0, P, P1, Acc,
+                              p.vgrid + Tm.off_nq + (int64_t)q * NQs, Mq, p.mugrid ? p.vw : T(1), mw, dvt);
+        __syncthreads();
+        int A = 1, Bq = NQs;
+        for (int j = 0; j < L; ++j) {  // Y[j] = d1_j psi
+          Bq /= Tm.nq[j];
+          contract<T>(P, Vt, Y + j * ss, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, mb + Tm.m_d1[j], T(1), false);
+          A *= Tm.nq[j];
+        }
+        __syncthreads();
+        // Phi_i = sum_j G_ij(Q) y_j, in place (Y[i], i <= L)
+        if (D <= 4) slab_pointwise_G<T, 4, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
+        else if (D <= 6) slab_pointwise_G<T, 6, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
+        else if (D <= 8) slab_pointwise_G<T, 8, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
+        else if (D <= 12) slab_pointwise_G<T, 12, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
+        else slab_pointwise_G<T, 16, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
+        __syncthreads();
+        A = 1;
+        Bq = NQs;
+        for (int i = 0; i < L; ++i) {  // Acc += -1/2 d1_i Phi_i
+          Bq /= Tm.nq[i];
+          contract<T>(Y + i * ss, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d1[i], T(-0.5), true);
+          __syncthreads();
+          A *= Tm.nq[i];
+        }
+        slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), mb + Tm.m_e1L + (int64_t)ldo * q, P1,
+                           T(-0.5));
+        continue;
+      }
       slab_extract<T>(Tg, ss, nL, X0 + q, ldx0, P);
       __syncthreads();
       const T* Vq = p.vgrid + Tm.off_nq + (int64_t)q * NQs;
