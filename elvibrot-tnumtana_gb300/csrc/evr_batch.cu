@@ -12,19 +12,16 @@
 //
 // evr_batch_davidson runs sub_propagation_Davidson (sub_module_Davidson.f90:54-748, as in
 // evr_davidson.cu) for every problem at once: all problems share the subspace size, so the
-// per-problem projections and Ritz combinations are grouped cuBLAS GEMMs (one group per
-// problem), the small projected eigenproblems are solved by a batched Jacobi kernel (one
+// per-problem projections and Ritz combinations are segmented products over row chunks
+// of the stack (partial Grams summed per problem in a fixed order), the small projected eigenproblems are solved by a batched Jacobi kernel (one
 // CTA per problem), and the H.psi of the new directions of all problems is one call.
 // Mixed precision follows evr_davidson (FP32 phase, then FP64 H.psi of the kept Ritz
 // vectors and FP32 H.psi for new directions with the FP64 side of every mixed product).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <functional>
 #include <numeric>
 #include <vector>
-
-#include <cublas_v2.h>
 
 #include "evr_internal.h"
 
@@ -85,10 +82,11 @@ __global__ void batch_to_float(const double* __restrict__ a, float* __restrict__
 // (relative to its own diagonal, so very large diagonal entries -- the flagged empty
 // directions -- do not hide the others); at most max_sweeps sweeps, stopping after a
 // sweep without rotations.  Eigenvalues ascending into W, eigenvectors as the columns of
-// V (column-major, ld ldv).
+// V (column-major, ld ldv).  The sweep flag is reset only after every thread has read it
+// (a barrier on both sides), so all threads leave the sweep loop together.
 __global__ void batched_jacobi_kernel(const double* __restrict__ A, int lda, int64_t sa, int n,
                                       double* __restrict__ W, int64_t sw, double* __restrict__ V, int ldv, int64_t sv,
-                                      int max_sweeps, double tol) {
+                                      int max_sweeps, double tol, int* __restrict__ err) {
   extern __shared__ double sm[];
   const int np = (n + 1) & ~1;
   double* a = sm;             // np x np, a[i + np*j]
@@ -105,6 +103,7 @@ __global__ void batched_jacobi_kernel(const double* __restrict__ A, int lda, int
   __syncthreads();
   const int npair = np / 2;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    __syncthreads();  // every thread has read the previous sweep's flag
     if (threadIdx.x == 0) s_rot = 0;
     __syncthreads();
     for (int r = 0; r < np - 1; ++r) {
@@ -149,7 +148,8 @@ __global__ void batched_jacobi_kernel(const double* __restrict__ A, int lda, int
       }
       __syncthreads();
     }
-    if (!s_rot) break;
+    const int rot = s_rot;
+    if (!rot) break;
   }
   // ascending order of the n real eigenvalues (the padding index, if any, is np - 1 = n
   // and stays decoupled)
@@ -169,9 +169,147 @@ __global__ void batched_jacobi_kernel(const double* __restrict__ A, int lda, int
   double* Vb = V + blockIdx.x * sv;
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
     const int i = e % n, j = e / n;
-    Vb[i + (int64_t)ldv * j] = v[i + np * ord[j]];
+    const int oj = ord[j];
+    if (oj < 0 || oj >= n) {  // cannot happen with a consistent sort: flag it, skip the access
+      atomicOr(err, 1);
+      continue;
+    }
+    Vb[i + (int64_t)ldv * j] = v[i + np * oj];
   }
-  for (int j = threadIdx.x; j < n; j += blockDim.x) Wb[j] = a[ord[j] + np * ord[j]];
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    const int oj = ord[j];
+    if (oj >= 0 && oj < n) Wb[j] = a[oj + np * oj];
+  }
+}
+
+// Segmented products over the stacked rows.  The rows of every problem are cut into
+// chunks (crow[c] .. crow[c+1]-1, never across a problem boundary; chunk c belongs to
+// problem cq[c] and the chunks of problem q are cb[q] .. cb[q+1]-1).  Row g of a stacked
+// block X with leading dimension ldx holds X[g*ldx + 0 .. n-1] (the column-major layout of
+// cuBLAS with the roles of rows and columns swapped).
+
+// partial Gram of one chunk: part[c] (na x nb, column-major) = sum_rows A_g^T B_g; a
+// thread owns a 4 x 4 tile of the result and groups of threads take interleaved rows,
+// summed in a fixed order at the end (no atomics: the sums are reproducible)
+constexpr int kSegRows = 32;
+__global__ void __launch_bounds__(256) seg_gram_kernel(const double* __restrict__ A, int lda,
+                                                       const double* __restrict__ B, int ldb, int na, int nb,
+                                                       const int64_t* __restrict__ crow, double* __restrict__ part) {
+  __shared__ double sm[2 * kSegRows * 64];
+  double* sA = sm;
+  double* sB = sm + kSegRows * 64;
+  const int tI = (na + 3) / 4, tJ = (nb + 3) / 4, nt = tI * tJ;
+  const int PA = 4 * tI, PB = 4 * tJ;
+  const int G = blockDim.x / nt;
+  const int tid = threadIdx.x;
+  const int g = tid / nt, w = tid % nt, ti = w % tI, tj = w / tI;
+  const bool act = g < G;
+  double acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+  const int64_t rb = crow[blockIdx.x], re = crow[blockIdx.x + 1];
+  for (int64_t r0 = rb; r0 < re; r0 += kSegRows) {
+    const int nr = (int)(re - r0 < kSegRows ? re - r0 : kSegRows);
+    __syncthreads();
+    for (int e = tid; e < nr * PA; e += blockDim.x) {
+      const int r = e / PA, i = e % PA;
+      sA[e] = i < na ? A[(r0 + r) * lda + i] : 0.0;
+    }
+    for (int e = tid; e < nr * PB; e += blockDim.x) {
+      const int r = e / PB, j = e % PB;
+      sB[e] = j < nb ? B[(r0 + r) * ldb + j] : 0.0;
+    }
+    __syncthreads();
+    if (act)
+      for (int r = g; r < nr; r += G) {
+        double x[4], y[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          x[a] = sA[r * PA + 4 * ti + a];
+          y[a] = sB[r * PB + 4 * tj + a];
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) acc[a][b] = fma(x[a], y[b], acc[a][b]);
+      }
+  }
+  __syncthreads();
+  // G * nt * 16 <= 16 * blockDim.x = 4096 doubles: the tiles reuse sA and sB
+  if (act) {
+    double* red = sm + (size_t)(g * nt + w) * 16;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) red[a * 4 + b] = acc[a][b];
+  }
+  __syncthreads();
+  double* out = part + (int64_t)blockIdx.x * na * nb;
+  for (int e = tid; e < na * nb; e += blockDim.x) {
+    const int i = e % na, j = e / na;
+    const int ww = i / 4 + tI * (j / 4), k = (i % 4) * 4 + j % 4;
+    double sum = 0.0;
+    for (int gg = 0; gg < G; ++gg) sum += sm[(size_t)(gg * nt + ww) * 16 + k];
+    out[e] = sum;
+  }
+}
+
+// C_q (ld ldc, at C + q*cstride) = sum of its chunks' partial Grams + beta C_q
+__global__ void seg_gram_reduce_kernel(const double* __restrict__ part, const int* __restrict__ cb, int na, int nb,
+                                       double* __restrict__ C, int ldc, int64_t cstride, double beta) {
+  const int q = blockIdx.x;
+  double* Cq = C + q * cstride;
+  const int c0 = cb[q], c1 = cb[q + 1];
+  for (int e = threadIdx.x; e < na * nb; e += blockDim.x) {
+    const int i = e % na, j = e / na;
+    double sum = 0.0;
+    for (int c = c0; c < c1; ++c) sum += part[(int64_t)c * na * nb + e];
+    double* dst = Cq + i + (int64_t)ldc * j;
+    *dst = beta == 0.0 ? sum : sum + beta * *dst;
+  }
+}
+
+// Y_g (k entries) = alpha X_g (n entries) Mat_q + beta Y_g for the rows g of one chunk;
+// Mat_q (n x k, column-major, ld ldm) at Mat + q*mstride.  Mat_q and a tile of rows sit
+// in shared memory; a thread forms 4 consecutive entries of one row.
+__global__ void __launch_bounds__(256) seg_combine_kernel(const double* __restrict__ X, int ldx, int n,
+                                                          const double* __restrict__ Mat, int ldm, int64_t mstride,
+                                                          int k, double* __restrict__ Y, int ldy, double alpha,
+                                                          double beta, const int64_t* __restrict__ crow,
+                                                          const int* __restrict__ cq) {
+  extern __shared__ double dsm[];
+  const int kq = (k + 3) / 4, PK = 4 * kq;
+  const int TR = min(64, (int)blockDim.x / kq);
+  double* sM = dsm;            // n x PK, row i = row i of Mat_q
+  double* sX = dsm + n * PK;   // TR x n
+  const double* Mq = Mat + cq[blockIdx.x] * mstride;
+  for (int e = threadIdx.x; e < n * PK; e += blockDim.x) {
+    const int i = e / PK, j = e % PK;
+    sM[e] = j < k ? Mq[i + (int64_t)ldm * j] : 0.0;
+  }
+  const int64_t rb = crow[blockIdx.x], re = crow[blockIdx.x + 1];
+  const int r = threadIdx.x / kq, c = threadIdx.x % kq;
+  for (int64_t r0 = rb; r0 < re; r0 += TR) {
+    const int nr = (int)(re - r0 < TR ? re - r0 : TR);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nr * n; e += blockDim.x) sX[e] = X[(r0 + e / n) * ldx + e % n];
+    __syncthreads();
+    if (r < nr) {
+      double acc[4] = {0.0, 0.0, 0.0, 0.0};
+      for (int i = 0; i < n; ++i) {
+        const double x = sX[r * n + i];
+        const double* m = sM + i * PK + 4 * c;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) acc[a] = fma(x, m[a], acc[a]);
+      }
+      double* y = Y + (r0 + r) * ldy + 4 * c;
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+        if (4 * c + a < k) y[a] = beta == 0.0 ? alpha * acc[a] : alpha * acc[a] + beta * y[a];
+    }
+  }
 }
 
 // mirror the new columns of every projected matrix into its rows and, for dropped
@@ -539,41 +677,51 @@ int evr_batch_offsets(const evr_ctx* c, int64_t* offsets) {
 // ---------------------------------------------------------------------------------------
 namespace {
 
-struct Grouped {
-  // one GEMM per problem: C_s = op(A_s) op(B_s), sizes and pointers per problem
-  std::vector<cublasOperation_t> ta, tb;
-  std::vector<int> m, n, k, lda, ldb, ldc, gsz;
-  std::vector<double> alpha, beta;
-  std::vector<const double*> A, B;
-  std::vector<double*> C;
-  DBuf dptr;  // device copies of the pointer arrays
-  size_t cap = 0;
-};
-
 struct BatchDavidson {
   evr_ctx* c;
   cudaStream_t s;
-  cublasHandle_t blas = nullptr;
-  int nsys = 0, M = 0, nkeep = 0, bmax = 0, op = OP_H;
+  int nsys = 0, M = 0, nkeep = 0, bmax = 0, op = OP_H, nch = 0;
   int64_t N = 0;
   std::vector<int64_t> off;
   const int* sys_d = nullptr;
-  DBuf Pt, HPt, X, HX, R, T, Tt, Hs, Wv, Ev, Cm, Gm, Um, Lm, Mt, nrm, sel, dead, ptrs, actv;
+  DBuf Pt, HPt, X, HX, R, T, Tt, Hs, Wv, Ev, Cm, Gm, Um, Lm, Mt, nrm, sel, dead, actv;
+  DBuf crow, cq, cb, part;  // row chunks of the segmented products and their partial Grams
+  DBuf errf;                // consistency flag of the batched Jacobi kernel
   std::vector<unsigned char> active;      // problems still iterating
   const std::vector<int>* term_sys = nullptr;
   int64_t sh = 0;  // stride of one projected matrix (M*M)
-  Grouped g;
 
-  ~BatchDavidson() {
-    if (blas) cublasDestroy(blas);
-  }
   int fail(int code, const std::string& m) { return set_error(c, code, "evr_batch_davidson: " + m); }
 
   int init() {
-    if (cublasCreate(&blas) != CUBLAS_STATUS_SUCCESS) return fail(EVR_EDEVICE, "cublasCreate");
-    cublasSetStream(blas, s);
-    cublasSetPointerMode(blas, CUBLAS_POINTER_MODE_HOST);
+    if (M > 64 || bmax > 64) return fail(EVR_EINVAL, "subspace larger than 64");
     sh = (int64_t)M * M;
+    // row chunks: about four per SM over the whole stack, none across a problem boundary
+    const int64_t rc = std::max<int64_t>(256, (N + 4 * c->num_sms - 1) / (4 * c->num_sms));
+    std::vector<int64_t> hrow;
+    std::vector<int> hq, hb(nsys + 1);
+    for (int q = 0; q < nsys; ++q) {
+      hb[q] = (int)hrow.size();
+      for (int64_t r = off[q]; r < off[q + 1]; r += rc) {
+        hrow.push_back(r);
+        hq.push_back(q);
+      }
+    }
+    nch = (int)hrow.size();
+    hb[nsys] = nch;
+    hrow.push_back(N);
+    if (crow.alloc(hrow.size() * sizeof(int64_t)) || cq.alloc(hq.size() * sizeof(int)) ||
+        cb.alloc(hb.size() * sizeof(int)) || part.alloc((size_t)nch * M * M * 8) || errf.alloc(sizeof(int)))
+      return fail(EVR_ENOMEM, "device allocation");
+    if (cudaMemsetAsync(errf.p, 0, sizeof(int), s)) return fail(EVR_EDEVICE, "memset");
+    if (cudaMemcpyAsync(crow.p, hrow.data(), hrow.size() * sizeof(int64_t), cudaMemcpyHostToDevice, s) ||
+        cudaMemcpyAsync(cq.p, hq.data(), hq.size() * sizeof(int), cudaMemcpyHostToDevice, s) ||
+        cudaMemcpyAsync(cb.p, hb.data(), hb.size() * sizeof(int), cudaMemcpyHostToDevice, s) ||
+        cudaStreamSynchronize(s))
+      return fail(EVR_EDEVICE, "chunk upload");
+    if (cudaFuncSetAttribute(seg_combine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 64 * 64 * 8) !=
+        cudaSuccess)
+      return fail(EVR_EDEVICE, "combine attribute");
     const size_t nm = (size_t)N * M;
     if (Pt.alloc(nm * 8) || HPt.alloc(nm * 8) || X.alloc((size_t)N * nkeep * 8) || HX.alloc((size_t)N * nkeep * 8) ||
         R.alloc((size_t)N * nkeep * 8) || T.alloc((size_t)N * bmax * 8) || Tt.alloc((size_t)N * bmax * 8) ||
@@ -581,8 +729,7 @@ struct BatchDavidson {
         Cm.alloc((size_t)nsys * M * bmax * 8) || Gm.alloc((size_t)nsys * bmax * bmax * 8) ||
         Um.alloc((size_t)nsys * bmax * bmax * 8) || Lm.alloc((size_t)nsys * bmax * 8) ||
         Mt.alloc((size_t)nsys * bmax * bmax * 8) || nrm.alloc((size_t)nsys * nkeep * 8) ||
-        sel.alloc((size_t)nsys * bmax * sizeof(int)) || dead.alloc((size_t)nsys * M) ||
-        ptrs.alloc((size_t)3 * nsys * sizeof(double*)) || actv.alloc((size_t)nsys))
+        sel.alloc((size_t)nsys * bmax * sizeof(int)) || dead.alloc((size_t)nsys * M) || actv.alloc((size_t)nsys))
       return fail(EVR_ENOMEM, "device allocation");
     if (cudaMemsetAsync(dead.p, 0, (size_t)nsys * M, s)) return fail(EVR_EDEVICE, "memset");
     const int np = ((std::max(M, bmax) + 1) & ~1);
@@ -592,71 +739,28 @@ struct BatchDavidson {
     return EVR_OK;
   }
 
-  // per problem q: C_q (m_q x n_q, ld ldc) = alpha op(A_q) op(B_q) + beta C_q, inner size k_q
-  using IntF = std::function<int(int)>;
-  using PtrF = std::function<const double*(int)>;
-  using OutF = std::function<double*(int)>;
-  int grouped(cublasOperation_t ta, cublasOperation_t tb, IntF mfun, IntF nfun, IntF kfun, PtrF afun, int lda,
-              PtrF bfun, int ldb, OutF cfun, int ldc, double alpha, double beta) {
-    g.ta.assign(nsys, ta);
-    g.tb.assign(nsys, tb);
-    g.m.resize(nsys);
-    g.n.resize(nsys);
-    g.k.resize(nsys);
-    g.lda.assign(nsys, lda);
-    g.ldb.assign(nsys, ldb);
-    g.ldc.assign(nsys, ldc);
-    g.gsz.assign(nsys, 1);
-    g.alpha.assign(nsys, alpha);
-    g.beta.assign(nsys, beta);
-    g.A.resize(nsys);
-    g.B.resize(nsys);
-    g.C.resize(nsys);
-    for (int q = 0; q < nsys; ++q) {
-      g.m[q] = mfun(q);
-      g.n[q] = nfun(q);
-      g.k[q] = kfun(q);
-      g.A[q] = afun(q);
-      g.B[q] = bfun(q);
-      g.C[q] = cfun(q);
-    }
-    const double** dA = (const double**)ptrs.p;
-    const double** dB = dA + nsys;
-    double** dC = (double**)(dB + nsys);
-    std::vector<const void*> hp(3 * (size_t)nsys);
-    for (int q = 0; q < nsys; ++q) {
-      hp[q] = g.A[q];
-      hp[nsys + q] = g.B[q];
-      hp[2 * nsys + q] = g.C[q];
-    }
-    if (cudaMemcpyAsync(ptrs.p, hp.data(), hp.size() * sizeof(void*), cudaMemcpyHostToDevice, s) ||
-        cudaStreamSynchronize(s))
-      return fail(EVR_EDEVICE, "pointer upload");
-    if (cublasDgemmGroupedBatched(blas, g.ta.data(), g.tb.data(), g.m.data(), g.n.data(), g.k.data(), g.alpha.data(),
-                                  dA, g.lda.data(), dB, g.ldb.data(), g.beta.data(), dC, g.ldc.data(), nsys,
-                                  g.gsz.data()) != CUBLAS_STATUS_SUCCESS)
-      return fail(EVR_EDEVICE, "cublasDgemmGroupedBatched");
-    return EVR_OK;
+  // C_q (na x nb, ld ldc, at C + q*cstride) = A_q^T B_q + beta C_q over the rows of problem q
+  int gram(const double* A, int lda, const double* B, int ldb, int na, int nb, double* C, int ldc, int64_t cstride,
+           double beta = 0.0) {
+    if (na < 1 || nb < 1 || na > 64 || nb > 64) return fail(EVR_EINVAL, "gram size");
+    seg_gram_kernel<<<nch, kBT, 0, s>>>(A, lda, B, ldb, na, nb, (const int64_t*)crow.p, part.d());
+    seg_gram_reduce_kernel<<<nsys, kBT, 0, s>>>(part.d(), (const int*)cb.p, na, nb, C, ldc, cstride, beta);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? EVR_OK : fail(EVR_EDEVICE, std::string("gram launch: ") + cudaGetErrorString(e));
+  }
+  // Y_q (rows x k, ld ldy) = alpha X_q (rows x n, ld ldx) Mat_q (n x k, ld ldm, at Mat + q*mstride) + beta Y_q
+  int combine(const double* Xb, int ldx, int n, const double* Mat, int ldm, int64_t mstride, int k, double* Y, int ldy,
+              double alpha, double beta) {
+    if (n < 1 || k < 1 || n > 64 || k > 64) return fail(EVR_EINVAL, "combine size");
+    const int kq = (k + 3) / 4, tr = std::min(64, kBT / kq);
+    const size_t smem = (size_t)(n * 4 * kq + tr * n) * sizeof(double);
+    seg_combine_kernel<<<nch, kBT, smem, s>>>(Xb, ldx, n, Mat, ldm, mstride, k, Y, ldy, alpha, beta,
+                                              (const int64_t*)crow.p, (const int*)cq.p);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? EVR_OK : fail(EVR_EDEVICE, std::string("combine launch: ") + cudaGetErrorString(e));
   }
 
   int rows(int q) const { return (int)(off[q + 1] - off[q]); }
-
-  // C_s (na x nb, ld ldc) = A_s^T B_s over the problem's rows: A, B interleaved blocks
-  int gram(const double* A, int lda, const double* B, int ldb, int na, int nb, double* C, int ldc, int64_t cstride,
-           double beta = 0.0) {
-    return grouped(CUBLAS_OP_N, CUBLAS_OP_T, [=](int) { return na; }, [=](int) { return nb; },
-                   [this](int q) { return rows(q); }, [=](int q) { return A + off[q] * lda; }, lda,
-                   [=](int q) { return B + off[q] * ldb; }, ldb, [=](int q) { return C + q * cstride; }, ldc, 1.0,
-                   beta);
-  }
-  // Y_s (rows x k, interleaved ld ldy) = alpha X_s (rows x n, ld ldx) Mat_s (n x k, ld ldm) + beta Y_s
-  int combine(const double* Xb, int ldx, int n, const double* Mat, int ldm, int64_t mstride, int k, double* Y, int ldy,
-              double alpha, double beta) {
-    return grouped(CUBLAS_OP_T, CUBLAS_OP_N, [=](int) { return k; }, [this](int q) { return rows(q); },
-                   [=](int) { return n; }, [=](int q) { return Mat + q * mstride; }, ldm,
-                   [=](int q) { return Xb + off[q] * ldx; }, ldx, [=](int q) { return Y + off[q] * ldy; }, ldy, alpha,
-                   beta);
-  }
 
   // H.psi of n columns for the active problems only (the others' rows come out zero)
   int hop(double* x, int ldx, double* y, int ldy, int n, int prec, int64_t& c64, int64_t& c32) {
@@ -682,8 +786,10 @@ struct BatchDavidson {
 
   int jacobi(const double* A, int lda, int64_t sa, int n, double* W, int64_t sw, double* V, int ldv, int64_t sv) {
     const int np = (n + 1) & ~1;
-    batched_jacobi_kernel<<<nsys, kBT, 2 * np * np * sizeof(double), s>>>(A, lda, sa, n, W, sw, V, ldv, sv, 40, 1e-15);
-    return cudaGetLastError() == cudaSuccess ? EVR_OK : fail(EVR_EDEVICE, "jacobi launch");
+    batched_jacobi_kernel<<<nsys, kBT, 2 * np * np * sizeof(double), s>>>(A, lda, sa, n, W, sw, V, ldv, sv, 40, 1e-15,
+                                                                         (int*)errf.p);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? EVR_OK : fail(EVR_EDEVICE, std::string("jacobi launch: ") + cudaGetErrorString(e));
   }
 
   // orthonormalise the ns columns of T against Pt(:, 0:n1) and among themselves, append
@@ -799,10 +905,12 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
     if (cudaMemsetAsync(d.nrm.p, 0, sizeof(double) * nsys * k, s)) return set_error(c, EVR_EDEVICE, "memset");
     batch_residual_kernel<<<c->num_sms * 8, kBT, 0, s>>>(d.X.d(), d.HX.d(), d.nkeep, d.Ev.d(), M, d.sys_d, k, N,
                                                          d.R.d(), d.nrm.d());
+    int jerr = 0;
     if (cudaMemcpyAsync(rn.data(), d.nrm.p, sizeof(double) * nsys * k, cudaMemcpyDeviceToHost, s) ||
         cudaMemcpyAsync(Eh.data(), d.Ev.p, sizeof(double) * nsys * M, cudaMemcpyDeviceToHost, s) ||
-        cudaStreamSynchronize(s))
+        cudaMemcpyAsync(&jerr, d.errf.p, sizeof(int), cudaMemcpyDeviceToHost, s) || cudaStreamSynchronize(s))
       return set_error(c, EVR_EDEVICE, "evr_batch_davidson: residual norms");
+    if (jerr) return set_error(c, EVR_EDEVICE, "evr_batch_davidson: inconsistent eigenvalue order in the Jacobi kernel");
     const int nt = std::min(nlev, k);
     double rmax = 0.0;
     std::vector<std::vector<int>> todo(nsys);

@@ -147,7 +147,8 @@ int evr_set_kernel_path(evr_ctx *ctx, int path);
  * not enter the CUDA allocator at that point -- this variant of evr_hpsi_device takes its
  * scratch (item counter, term-basis output, per-CTA work buffers) from one file-scope
  * device array of 32 MiB that every GPU loading the library holds until the process
- * exits.  psi/hpsi: DEVICE pointers, interleaved layout (ld >= nvec), FP64, operator H.
+ * exits.  psi/hpsi: DEVICE pointers, interleaved layout (ld >= nvec), FP64, operator H
+ * (evr_set_operator and evr_set_field do not apply; batched contexts are rejected).
  * Problems whose scratch exceeds 32 MiB are rejected with EVR_EINVAL (message gives the
  * size needed).  The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.  All calls
