@@ -224,13 +224,26 @@ def run_suite(args):
                         "create_s": time.perf_counter() - t0})
             out["autotune"] = b.autotune(nvec=10, prec="fp32")
             res = {}
-            for prec in ("fp64", "fp32"):
+            out["conv_resi_au"] = args.batch_tol
+            runs = [("fp64", "fp64", args.batch_tol), ("fp32", "fp32", args.batch_tol)]
+            if args.batch_check:  # a tighter FP64 solve as the reference of both
+                runs.append(("fp64_tight", "fp64", args.batch_tol * 1e-2))
+            for name, prec, tol in runs:
                 t0 = time.perf_counter()
-                e, st = b.davidson(10, block=10, conv_resi=1e-7, conv_ene=1e-10, prec=prec, max_it=100)
-                res[prec] = e
-                out[prec] = {"s": time.perf_counter() - t0, **st}
+                e, st = b.davidson(10, block=10, conv_resi=tol, conv_ene=tol * 1e-3, prec=prec, max_it=200)
+                res[name] = e
+                out[name] = {"s": time.perf_counter() - t0, **st}
             out["speedup"] = out["fp64"]["s"] / out["fp32"]["s"]
-            out["max_abs_diff_cm"] = float(np.abs(res["fp64"] - res["fp32"]).max() * S.AU_TO_CM)
+            d = np.abs(res["fp64"] - res["fp32"]) * S.AU_TO_CM
+            out["max_abs_diff_cm"] = float(d.max())
+            q, j = np.unravel_index(int(np.argmax(d)), d.shape)
+            out["max_diff_at"] = {"problem": int(q), "level": int(j),
+                                  "levels_cm": [float(x * S.AU_TO_CM) for x in res["fp64"][q]]}
+            out["levels_above_1e-4_cm"] = int((d > 1e-4).sum())
+            if args.batch_check:
+                for name in ("fp64", "fp32"):
+                    out[name]["max_abs_diff_vs_tight_cm"] = float(
+                        (np.abs(res[name] - res["fp64_tight"]) * S.AU_TO_CM).max())
         elif w == "prop12d":
             # D=12 SG4 L=6, Gaussian displaced by 1.0 in modes 1-3, Chebyshev dt = 10 au
             sp = S.config_sg4_12d_l6()
@@ -331,6 +344,9 @@ def main():
                     help="the other workloads (one JSON line each): direct-product Davidson, 256 batched "
                          "problems, D=12 Chebyshev propagation, optimal-control gradient")
     ap.add_argument("--batch-n", type=int, default=256, help="problems in the batch workload")
+    ap.add_argument("--batch-tol", type=float, default=1e-7, help="residual tolerance of the batch Davidson (au)")
+    ap.add_argument("--batch-check", action="store_true",
+                    help="also solve the batch in FP64 at 1/100 of the tolerance and compare both against it")
     ap.add_argument("--prop-steps", type=int, default=200, help="time steps timed in the propagation workload")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -979,6 +979,20 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
       return set_error(c, EVR_EDEVICE, "copy");
     batch_zero_rows_kernel<<<c->num_sms * 8, kBT, 0, s>>>(d.T.d(), d.bmax, 0, ns, d.sys_d,
                                                           (const unsigned char*)d.actv.p, N);
+    if (n1 + ns > M && refine) {
+      // refinement: a refresh, the Ritz vectors' H.psi recomputed in FP64 (their combined
+      // H.psi holds FP32 columns and must not serve as an exact column)
+      const int kr = std::min(k, nlev);
+      if (cudaMemcpy2DAsync(d.Pt.p, sizeof(double) * M, d.X.p, sizeof(double) * d.nkeep, sizeof(double) * kr, N,
+                            cudaMemcpyDeviceToDevice, s) ||
+          cudaMemsetAsync(d.dead.p, 0, (size_t)nsys * M, s))
+        return set_error(c, EVR_EDEVICE, "restart copy");
+      std::fill(d.active.begin(), d.active.end(), 1);
+      ke = kr;
+      n1 = kr;
+      n0 = 0;
+      continue;
+    }
     if (n1 + ns > M) {
       if (cudaMemcpy2DAsync(d.Pt.p, sizeof(double) * M, d.X.p, sizeof(double) * d.nkeep, sizeof(double) * k, N,
                             cudaMemcpyDeviceToDevice, s) ||

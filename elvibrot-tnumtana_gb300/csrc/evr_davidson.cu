@@ -449,7 +449,19 @@ extern "C" int evr_davidson(evr_ctx* c, const evr_davidson_opts* o, const double
       return set_error(c, EVR_EDEVICE, "copy");
     precondition_kernel<<<c->num_sms * 8, 256, 0, s>>>(d.R.p, d.nkeep, d.sel_d, d.E.p, c->dp.e0diag, ns, N, d.T.p,
                                                        d.bmax, 1e-3 * std::max(1e-300, std::fabs(Eh[0])) + 1e-12);
-    // restart when the subspace would overflow
+    // restart when the subspace would overflow.  In the refinement the restart is a refresh:
+    // the Ritz vectors' H.psi combines FP32 columns, so it is recomputed in FP64 before the
+    // kept columns serve as exact ones (the FP64 side of the mixed products)
+    if (n1 + ns > M && refine) {
+      const int kr = std::min(k, nlev);
+      if (cudaMemcpy2DAsync(d.Pt.p, sizeof(double) * M, d.X.p, sizeof(double) * d.nkeep, sizeof(double) * kr, N,
+                            cudaMemcpyDeviceToDevice, s))
+        return set_error(c, EVR_EDEVICE, "restart copy");
+      ke = kr;
+      n1 = kr;
+      n0 = 0;
+      continue;
+    }
     if (n1 + ns > M) {
       if (cudaMemcpy2DAsync(d.Pt.p, sizeof(double) * M, d.X.p, sizeof(double) * d.nkeep, sizeof(double) * k, N,
                             cudaMemcpyDeviceToDevice, s) ||

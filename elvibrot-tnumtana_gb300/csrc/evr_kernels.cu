@@ -302,6 +302,11 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
         if (slab_wg_smem_elems(P, Tm, 1, false) * sizeof(double) + mats > (size_t)w.smem_slab_bytes) continue;
         sb = std::max(sb, slab_wg_global_elems(Tm, 1) * sizeof(double));
       }
+    // FP32 terms run in the W-in-global mode when it allows a wider vector tile (below):
+    // room for tiles of 4 vectors, at most 4 MB per CTA
+    if (P.nb0 == 1)
+      for (const TermDesc& Tm : P.terms)
+        if (Tm.weight != 0.0) sb = std::max(sb, std::min<size_t>(slab_wg_global_elems(Tm, 4) * sizeof(float), 4u << 20));
     w.slab_slab_bytes = (sb + 255) & ~(size_t)255;
     const size_t total = std::max(slab * w.grid, w.slab_slab_bytes * w.grid_slab);
     w.counter = (int*)dev_alloc<int>(4, rc);  // item counters of both kernels, item-bounds flag
@@ -334,6 +339,27 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
     const size_t mats = (size_t)((Tm.msz + 3) & ~3) * esz;  // staged 1-D matrices
     if (mats > (size_t)w.smem_bytes) return set_error(c, EVR_EINVAL, "1-D matrices exceed shared memory");
     const bool small = (int64_t)Tm.NQ * std::min(nvec, c->vt_cap_slab) < c->slab_min_points;
+    // W-in-global tile (shared memory holds only the slab arrays)
+    auto wg_fits = [&](int v) {
+      return slab_wg_smem_elems(P, Tm, v, f32) * esz + mats <= (size_t)w.smem_slab_bytes &&
+             slab_wg_global_elems(Tm, v) * esz <= w.slab_slab_bytes;
+    };
+    if (f32 && slab_ok && !small && wg_fits(1)) {
+      // FP32 is bound by the instructions per grid point, not by the L2 traffic of W: the
+      // W-in-global mode wins where it allows at least twice the tile of the shared-memory mode
+      int v3 = 1, v1 = 0;
+      while (v3 * 2 <= nvec && v3 * 2 <= c->vt_cap_slab && wg_fits(v3 * 2)) v3 *= 2;
+      if (slab_need_elems(P, Tm, 1, f32) * esz + mats <= (size_t)w.smem_slab_bytes) {
+        v1 = 1;
+        while (v1 * 2 <= nvec && v1 * 2 <= c->vt_cap_slab &&
+               slab_need_elems(P, Tm, v1 * 2, f32) * esz + mats <= (size_t)w.smem_slab_bytes)
+          v1 *= 2;
+      }
+      if (v3 >= 2 * v1) {
+        for (int v0 = 0; v0 < nvec; v0 += v3) sitems.push_back(WorkItem{t, v0, std::min(v3, nvec - v0), 3});
+        continue;
+      }
+    }
     if (slab_ok && !small && slab_need_elems(P, Tm, 1, f32) * esz + mats <= (size_t)w.smem_slab_bytes) {
       // FP32: the partially transformed tensor also in shared memory when a tile of
       // min(4, nvec) vectors fits (its per-slab re-reads then stay on the SM); FP64 keeps it
@@ -350,14 +376,9 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
       continue;
     }
     // W in global memory: the slab pipeline with only the slab arrays in shared memory
-    if (slab_ok && !small && slab_wg_smem_elems(P, Tm, 1, f32) * esz + mats <= (size_t)w.smem_slab_bytes &&
-        slab_wg_global_elems(Tm, 1) * esz <= w.slab_slab_bytes) {
-      auto fits = [&](int v) {
-        return slab_wg_smem_elems(P, Tm, v, f32) * esz + mats <= (size_t)w.smem_slab_bytes &&
-               slab_wg_global_elems(Tm, v) * esz <= w.slab_slab_bytes;
-      };
+    if (slab_ok && !small && wg_fits(1)) {
       int vt = 1;
-      while (vt * 2 <= nvec && vt * 2 <= c->vt_cap_slab && fits(vt * 2)) vt *= 2;
+      while (vt * 2 <= nvec && vt * 2 <= c->vt_cap_slab && wg_fits(vt * 2)) vt *= 2;
       for (int v0 = 0; v0 < nvec; v0 += vt) sitems.push_back(WorkItem{t, v0, std::min(vt, nvec - v0), 3});
       continue;
     }

@@ -402,7 +402,13 @@ __device__ __forceinline__ void items_pointwise_G(const ItemParams<T>& p, const 
 #pragma unroll
         for (int j = i; j < DM; ++j) G[i * DM - i * (i - 1) / 2 + (j - i)] = gget(i, j);
     }
-    for (int v = ch; v < Vt; v += nch) {
+    // the thread's vectors ch, ch + nch, ... in an order rotated by the point, so that the
+    // lanes of a warp (neighbouring points, Vt elements apart) fall in different banks
+    const int cnt = (Vt - ch + nch - 1) / nch;
+    int jv = cnt > 0 ? q % cnt : 0;
+    for (int iv = 0; iv < cnt; ++iv) {
+      const int v = ch + nch * jv;
+      jv = (jv + 1 == cnt) ? 0 : jv + 1;
       const int64_t idx = (int64_t)q * Vt + v;
       T y[DM], z[DM];
 #pragma unroll
@@ -722,7 +728,12 @@ __device__ __forceinline__ void slab_pointwise_G(const ItemParams<T>& p, const T
 #pragma unroll
         for (int j = i; j < DM; ++j) G[i * DM - i * (i - 1) / 2 + (j - i)] = gload(i, j);
     }
-    for (int v = ch; v < Vt; v += nch) {
+    // vectors in an order rotated by the point (bank-conflict free, as in items_pointwise_G)
+    const int cnt = (Vt - ch + nch - 1) / nch;
+    int jv = cnt > 0 ? pt % cnt : 0;
+    for (int iv = 0; iv < cnt; ++iv) {
+      const int v = ch + nch * jv;
+      jv = (jv + 1 == cnt) ? 0 : jv + 1;
       const int64_t a = (int64_t)pt * Vt + v;
       T y[DM], z[DM];
 #pragma unroll
