@@ -75,7 +75,9 @@ struct WorkItem {
   int32_t v0;
   int32_t vt;            // vectors in the tile
   int32_t smem;          // general kernel: 1 buffers in shared memory, 0 in the CTA's global buffer;
-                         // slab kernel: 2 partially transformed tensor in shared memory too
+                         // slab kernel: 1 partially transformed tensor in the CTA's global buffer,
+                         // 2 in shared memory too, 3 W and the ping-pong tensors in global,
+                         // 4 as 3 plus the staged term grid (FP32 type 10)
 };
 
 struct HostProblem {

@@ -266,6 +266,11 @@ static size_t slab_wg_global_elems(const TermDesc& Tm, int vt) {
   const int L = Tm.D - 1;
   return 3 * (size_t)(Tm.NQ / Tm.nq[L]) * vt * Tm.nb[L];
 }
+// grid-staged mode (FP32 type 10): the W-in-global tensors and the staged term grid (psi
+// and d_L psi on all NQ points)
+static size_t slab_staged_global_elems(const TermDesc& Tm, int vt) {
+  return slab_wg_global_elems(Tm, vt) + 2 * (size_t)Tm.NQ * vt;
+}
 
 // Work decomposition for a block of nvec vectors.  Terms whose slab pipeline fits the
 // shared memory of one CTA (one electronic state) go to the slab kernel, with the widest
@@ -302,11 +307,12 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
         if (slab_wg_smem_elems(P, Tm, 1, false) * sizeof(double) + mats > (size_t)w.smem_slab_bytes) continue;
         sb = std::max(sb, slab_wg_global_elems(Tm, 1) * sizeof(double));
       }
-    // FP32 terms run in the W-in-global mode when it allows a wider vector tile (below):
-    // room for tiles of 4 vectors, at most 4 MB per CTA
+    // FP32 terms run in the W-in-global or grid-staged mode when it allows a wider vector
+    // tile (below): room for tiles of 4 vectors, at most 8 MB per CTA
     if (P.nb0 == 1)
       for (const TermDesc& Tm : P.terms)
-        if (Tm.weight != 0.0) sb = std::max(sb, std::min<size_t>(slab_wg_global_elems(Tm, 4) * sizeof(float), 4u << 20));
+        if (Tm.weight != 0.0)
+          sb = std::max(sb, std::min<size_t>(slab_staged_global_elems(Tm, 4) * sizeof(float), 8u << 20));
     w.slab_slab_bytes = (sb + 255) & ~(size_t)255;
     const size_t total = std::max(slab * w.grid, w.slab_slab_bytes * w.grid_slab);
     w.counter = (int*)dev_alloc<int>(4, rc);  // item counters of both kernels, item-bounds flag
@@ -354,6 +360,23 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
         while (v1 * 2 <= nvec && v1 * 2 <= c->vt_cap_slab &&
                slab_need_elems(P, Tm, v1 * 2, f32) * esz + mats <= (size_t)w.smem_slab_bytes)
           v1 *= 2;
+      }
+      // type 10: the grid-staged variant (the streamed position's transforms as two
+      // contractions instead of a sweep over Tg and W per grid slab) where its buffer allows
+      int v4 = 0;
+      if (P.keo_type == 10) {
+        auto st_fits = [&](int v) {
+          return slab_wg_smem_elems(P, Tm, v, f32) * esz + mats <= (size_t)w.smem_slab_bytes &&
+                 slab_staged_global_elems(Tm, v) * esz <= w.slab_slab_bytes;
+        };
+        if (st_fits(1)) {
+          v4 = 1;
+          while (v4 * 2 <= nvec && v4 * 2 <= c->vt_cap_slab && st_fits(v4 * 2)) v4 *= 2;
+        }
+      }
+      if (v4 >= 2 * v1 && v4 * 2 >= v3) {
+        for (int v0 = 0; v0 < nvec; v0 += v4) sitems.push_back(WorkItem{t, v0, std::min(v4, nvec - v0), 4});
+        continue;
       }
       if (v3 >= 2 * v1) {
         for (int v0 = 0; v0 < nvec; v0 += v3) sitems.push_back(WorkItem{t, v0, std::min(v3, nvec - v0), 3});

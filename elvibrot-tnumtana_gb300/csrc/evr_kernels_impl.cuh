@@ -760,6 +760,38 @@ __device__ __forceinline__ void slab_pointwise_G(const ItemParams<T>& p, const T
   }
 }
 
+// Type-10 kinetic part of one grid slab of the streamed position, from psi (P) and its
+// derivative along the streamed position (P1 = Y[L]):  Y[j] = d1_j psi (j < L),
+// Phi = G(Q) y in place, Acc += -1/2 sum_{i<L} d1_i Phi_i  (Phi_L stays in P1 for the
+// grid->basis side of the streamed position).  Starts after a barrier, ends with one.
+template <typename T, bool GFLY>
+__device__ __forceinline__ void slab_keo10(const ItemParams<T>& p, const TermDesc& Tm, const T* mb, T* P, T* Y, T* P1,
+                                           T* Acc, int64_t ss, int Vt, int q, int NQs, int nG) {
+  const int D = Tm.D, L = D - 1;
+  int A = 1, Bq = NQs;
+  for (int j = 0; j < L; ++j) {  // Y[j] = d1_j psi
+    Bq /= Tm.nq[j];
+    contract<T>(P, Vt, Y + j * ss, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, mb + Tm.m_d1[j], T(1), false);
+    A *= Tm.nq[j];
+  }
+  __syncthreads();
+  // Phi_i = sum_j G_ij(Q) y_j, in place (Y[i], i <= L)
+  if (D <= 4) slab_pointwise_G<T, 4, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
+  else if (D <= 6) slab_pointwise_G<T, 6, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
+  else if (D <= 8) slab_pointwise_G<T, 8, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
+  else if (D <= 12) slab_pointwise_G<T, 12, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
+  else slab_pointwise_G<T, 16, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
+  __syncthreads();
+  A = 1;
+  Bq = NQs;
+  for (int i = 0; i < L; ++i) {  // Acc += -1/2 d1_i Phi_i
+    Bq /= Tm.nq[i];
+    contract<T>(Y + i * ss, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d1[i], T(-0.5), true);
+    __syncthreads();
+    A *= Tm.nq[i];
+  }
+}
+
 // Slab-streaming pipeline for one (term, vector tile) item, one electronic state.  Positions
 // 0..L-1 of the term's mode order are transformed whole, position L = D-1 is streamed:
 //   A: gather + B->G over positions 0..L-1 (shared-memory ping-pong) -> Tg (global, L2)
@@ -797,7 +829,10 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
       // type 10: the first derivatives, and d_L psi in FP32 (fused extraction)
       const int64_t ny = p.keo_type == 10 ? L + (sizeof(T) == 4 ? 1 : 0) : 1;
       const int64_t need = max(2 * tsz0, tsz0 + (2 + ny) * ss0), mp = (s_term.msz + 3) & ~3;
-      const bool bad = w.smem == 3 ? (mp + (2 + ny) * ss0 > p.smem_elems || 3 * tsz0 > p.slab_per_cta)
+      // modes: 1 Tg global, 2 Tg in shared memory, 3 W in global, 4 W and the staged term
+      // grid (two tensors of NQ vectors) in global
+      const int64_t gst = w.smem == 4 ? 2 * ss0 * s_term.nq[L] : 0;
+      const bool bad = w.smem >= 3 ? (mp + (2 + ny) * ss0 > p.smem_elems || 3 * tsz0 + gst > p.slab_per_cta)
                                    : (mp + need + (w.smem == 2 ? tsz0 : 0) > p.smem_elems ||
                                       (w.smem != 2 && tsz0 > p.slab_per_cta));
       if (bad) {
@@ -817,8 +852,9 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
     // The partially transformed tensor Tg: after the phase buffers in shared memory
     // (smem == 2) or in the CTA's global buffer.  smem == 3 (terms whose W does not fit):
     // W and the ping-pong tensors of phases A and C also in the global buffer
-    // [Tg | W (= A ping) | A and C pong], only the slab arrays in shared memory.
-    const bool wg = w.smem == 3;
+    // [Tg | W (= A ping) | A and C pong], only the slab arrays in shared memory.  smem == 4
+    // (FP32 type 10): as 3, followed by the staged term grid [Psi | DPsi].
+    const bool wg = w.smem >= 3;
     T* const gbuf = p.slab + (int64_t)blockIdx.x * p.slab_per_cta;
     T* Tg = w.smem == 2 ? sm + max(2 * tsz, tsz + (2 + (p.keo_type == 10 ? L + (sizeof(T) == 4 ? 1 : 0) : 1)) * ss)
                         : gbuf;
@@ -859,12 +895,54 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
     T* Acc = slabs;
     T* P = Acc + ss;
     T* Y = P + ss;
-    for (int64_t i = threadIdx.x; i < tsz; i += blockDim.x) W[i] = T(0);
     const int ldx0 = (gL + 3) & ~3, ldo = (nL + 3) & ~3;
     const T* X0 = mb + Tm.m_d0b[L];
     const T* OUT = mb + Tm.m_bgw[L];
     const int nG = Tm.Dp * (Tm.Dp + 1) / 2;  // G-table slots per point (term offset)
-    for (int q = 0; q < gL; ++q) {
+    const bool staged = sizeof(T) == 4 && w.smem == 4 && p.keo_on && p.keo_type == 10;
+    if (staged) {
+      // grid-staged (FP32 type 10, buffers in global memory): the streamed position's
+      // grid<-basis transform of psi and of d_L psi for all slabs at once (Psi, DPsi: the
+      // term grid), each slab's kinetic and potential part in shared memory, written back
+      // over its Psi and DPsi slab (Acc, Phi_L), then one basis<-grid contraction into W
+      T* const Psi = gbuf + 3 * tsz;
+      T* const DPsi = Psi + (int64_t)gL * ss;
+      contract<T>(Tg, Vt, Psi, Vt, NQs, nL, gL, 1, Vt, X0, T(1), false);
+      contract<T>(Tg, Vt, DPsi, Vt, NQs, nL, gL, 1, Vt, mb + Tm.m_x1L, T(1), false);
+      const T mw = p.mu_dev ? (T)__ldg(p.mu_dev) : p.mw;
+      const T vw = p.mugrid ? p.vw : T(1);
+      const int s32 = (int)ss;
+      T* P1 = Y + (int64_t)L * ss;
+      for (int q = 0; q < gL; ++q) {
+        __syncthreads();
+        const T* Vq = p.vgrid + Tm.off_nq + (int64_t)q * NQs;
+        const T* Mq = p.mugrid ? p.mugrid + Tm.off_nq + (int64_t)q * NQs : nullptr;
+        T* ps = Psi + (int64_t)q * ss;
+        T* ds = DPsi + (int64_t)q * ss;
+        for (int a = threadIdx.x; a < s32; a += blockDim.x) {
+          const T x = ps[a];
+          const int pt = (int)dvt.div((uint32_t)a);
+          T v = __ldg(Vq + pt);
+          if (Mq) v = fma(mw, __ldg(Mq + pt), vw * v);
+          P[a] = x;
+          P1[a] = ds[a];
+          Acc[a] = v * x;
+        }
+        __syncthreads();
+        slab_keo10<T, GFLY>(p, Tm, mb, P, Y, P1, Acc, ss, Vt, q, NQs, nG);
+        for (int a = threadIdx.x; a < s32; a += blockDim.x) {
+          ps[a] = Acc[a];
+          ds[a] = P1[a];
+        }
+      }
+      __syncthreads();
+      contract<T>(Psi, Vt, W, Vt, NQs, gL, nL, 1, Vt, OUT, T(1), false);
+      __syncthreads();
+      contract<T>(DPsi, Vt, W, Vt, NQs, gL, nL, 1, Vt, mb + Tm.m_e1L, T(-0.5), true);
+    } else {
+      for (int64_t i = threadIdx.x; i < tsz; i += blockDim.x) W[i] = T(0);
+    }
+    for (int q = 0; q < (staged ? 0 : gL); ++q) {
       __syncthreads();
       if (sizeof(T) == 4 && p.keo_on && p.keo_type == 10) {
         // FP32: psi, d_L psi (kept in Y[L], later Phi_L) and Acc = V psi in one pass (FP64
@@ -875,28 +953,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         slab_extract_fused<T>(Tg, ss, nL, X0 + q, mb + Tm.m_x1L + q, ldx0, P, P1, Acc,
                               p.vgrid + Tm.off_nq + (int64_t)q * NQs, Mq, p.mugrid ? p.vw : T(1), mw, dvt);
         __syncthreads();
-        int A = 1, Bq = NQs;
-        for (int j = 0; j < L; ++j) {  // Y[j] = d1_j psi
-          Bq /= Tm.nq[j];
-          contract<T>(P, Vt, Y + j * ss, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, mb + Tm.m_d1[j], T(1), false);
-          A *= Tm.nq[j];
-        }
-        __syncthreads();
-        // Phi_i = sum_j G_ij(Q) y_j, in place (Y[i], i <= L)
-        if (D <= 4) slab_pointwise_G<T, 4, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
-        else if (D <= 6) slab_pointwise_G<T, 6, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
-        else if (D <= 8) slab_pointwise_G<T, 8, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
-        else if (D <= 12) slab_pointwise_G<T, 12, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
-        else slab_pointwise_G<T, 16, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
-        __syncthreads();
-        A = 1;
-        Bq = NQs;
-        for (int i = 0; i < L; ++i) {  // Acc += -1/2 d1_i Phi_i
-          Bq /= Tm.nq[i];
-          contract<T>(Y + i * ss, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d1[i], T(-0.5), true);
-          __syncthreads();
-          A *= Tm.nq[i];
-        }
+        slab_keo10<T, GFLY>(p, Tm, mb, P, Y, P1, Acc, ss, Vt, q, NQs, nG);
         slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), mb + Tm.m_e1L + (int64_t)ldo * q, P1,
                            T(-0.5));
         continue;
