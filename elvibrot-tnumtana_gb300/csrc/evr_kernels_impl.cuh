@@ -96,14 +96,42 @@ __device__ __forceinline__ void fma_column(T (&accv)[MAXM], const T* __restrict_
 
 // Division by a loop-invariant divisor d >= 1 for 0 <= n < 2^31 with one multiply-high:
 // q = (umulhi(m, n) + n) >> l, l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1.
+// Division by a run-time constant d (1 <= d <= 2^31) as a multiply-high and a shift.  The
+// magic number costs a 64-bit division, so the kernels build the divisors of a work item
+// once (the prefix products of its grid and basis sizes and the vector tile) in shared
+// memory and pass them to the contractions.
 struct FastDiv {
   uint32_t d, m, l;
-  __device__ __forceinline__ explicit FastDiv(uint32_t dd) : d(dd), l(0) {
-    while ((1u << l) < d) ++l;
-    m = (uint32_t)((((uint64_t)1 << 32) * (((uint64_t)1 << l) - d)) / d + 1);
+  static __device__ __forceinline__ FastDiv make(uint32_t dd) {
+    FastDiv f;
+    f.d = dd;
+    f.l = 0;
+    while ((1u << f.l) < dd) ++f.l;
+    f.m = (uint32_t)((((uint64_t)1 << 32) * (((uint64_t)1 << f.l) - dd)) / dd + 1);
+    return f;
   }
   __device__ __forceinline__ uint32_t div(uint32_t n) const { return (__umulhi(m, n) + n) >> l; }
 };
+
+// divisors of one work item: fq[j] = prod_{k<j} nq_k, fb[j] = prod_{k<j} nb_k (j <= D) and
+// the vector tile; filled by threads 0..D+1, read after the next barrier
+struct ItemDivs {
+  FastDiv fq[kMaxD + 1], fb[kMaxD + 1], fv;
+};
+__device__ __forceinline__ void fill_item_divs(ItemDivs& dv, const TermDesc& Tm, int vt) {
+  const int t = threadIdx.x, D = Tm.D;
+  if (t <= D) {
+    uint32_t pq = 1, pb = 1;
+    for (int k = 0; k < t; ++k) {
+      pq *= (uint32_t)Tm.nq[k];
+      pb *= (uint32_t)Tm.nb[k];
+    }
+    dv.fq[t] = FastDiv::make(pq);
+    dv.fb[t] = FastDiv::make(pb);
+  } else if (t == D + 1) {
+    dv.fv = FastDiv::make((uint32_t)vt);
+  }
+}
 
 // Matrix-stationary contraction: a thread owns MG consecutive output rows m0.. of the 1-D
 // matrix (held in registers) and one (a, v) lane, and walks the B dimension; each step
@@ -111,8 +139,9 @@ struct FastDiv {
 // when there are fewer lanes than threads the B dimension is split among them.
 template <typename T, int MAXK, int MG>
 __device__ __forceinline__ void contract_ms(const T* __restrict__ in, int64_t ldi, T* __restrict__ out, int64_t ldo,
-                                            int A, int K, int M, int B, int Vt, const T* __restrict__ mat, T alpha,
-                                            bool acc) {
+                                            const FastDiv& da, int K, int M, int B, const FastDiv& dvt,
+                                            const T* __restrict__ mat, T alpha, bool acc) {
+  const int A = (int)da.d, Vt = (int)dvt.d;
   const int ldm = (M + 3) & ~3;
   const int nmg = (M + MG - 1) / MG;
   const int AV = A * Vt;
@@ -122,15 +151,15 @@ __device__ __forceinline__ void contract_ms(const T* __restrict__ in, int64_t ld
   if (nbg < 1) nbg = 1;
   if (nbg > B) nbg = B;
   const int tasks = lanes * nbg;
-  const FastDiv dvt((uint32_t)Vt), dlanes((uint32_t)lanes), dav((uint32_t)AV);
   const int64_t istr = (int64_t)A * ldi, ostr = (int64_t)A * ldo;
   for (int task = threadIdx.x; task < tasks; task += nthr) {
-    const int bg = (int)dlanes.div((uint32_t)task);
-    const int lane = task - bg * lanes;
-    const int mg = (int)dav.div((uint32_t)lane);
-    const int av = lane - mg * AV;
-    const int a = (int)dvt.div((uint32_t)av);
-    const int v = av - a * Vt;
+    // task = v + Vt (a + A (mg + nmg bg))
+    const int t1 = (int)dvt.div((uint32_t)task);
+    const int v = task - t1 * Vt;
+    const int t2 = (int)da.div((uint32_t)t1);
+    const int a = t1 - t2 * A;
+    const int bg = nmg == 1 ? t2 : t2 / nmg;
+    const int mg = t2 - bg * nmg;
     const int m0 = mg * MG;
     T strip[MG][MAXK];
 #pragma unroll
@@ -166,11 +195,11 @@ __device__ __forceinline__ void contract_ms(const T* __restrict__ in, int64_t ld
 // columns so that every matrix load feeds eight FMAs.
 template <typename T, int MAXM, int COLS>
 __device__ __forceinline__ void contract_m(const T* __restrict__ in, int64_t ldi, T* __restrict__ out, int64_t ldo,
-                                           int A, int K, int M, int B, int Vt, const T* __restrict__ mat, T alpha,
-                                           bool acc) {
+                                           const FastDiv& da, int K, int M, int B, const FastDiv& dv,
+                                           const T* __restrict__ mat, T alpha, bool acc) {
+  const int A = (int)da.d, Vt = (int)dv.d;
   const int ncol = A * B * Vt;
   const int ldm = (M + 3) & ~3;
-  const FastDiv dv((uint32_t)Vt), da((uint32_t)A);
   // strides along the contracted and produced index: 32-bit (a tensor of one item holds
   // fewer than 2^31 elements), so the per-load address arithmetic stays 32-bit
   const int istr = (int)(A * ldi), ostr = (int)(A * ldo);
@@ -235,8 +264,8 @@ __device__ __forceinline__ void contract_m(const T* __restrict__ in, int64_t ldi
 }
 
 template <typename T>
-__device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64_t ldo, int A, int K, int M, int B,
-                                         int Vt, const T* mat, T alpha, bool acc) {
+__device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64_t ldo, const FastDiv& A, int K, int M,
+                                         int B, const FastDiv& Vt, const T* mat, T alpha, bool acc) {
   if constexpr (sizeof(T) == 4) {  // FP32: two columns per thread, matrix coefficients from shared memory
     if (M <= 4) contract_m<T, 4, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else if (M <= 8) contract_m<T, 8, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
@@ -258,11 +287,11 @@ __device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64
 // in(k, b, v) = x[(map[off_nb + k + K*b] + Np*e) * ldx + v0 + v]  (0 when excluded)
 template <typename T, int MAXM>
 __device__ __forceinline__ void gather_contract_m(const double* __restrict__ x, int64_t ldx, const int* __restrict__ mp,
-                                                  int64_t eoff, T* __restrict__ out, int K, int M, int B, int Vt,
-                                                  const T* __restrict__ mat) {
+                                                  int64_t eoff, T* __restrict__ out, int K, int M, int B,
+                                                  const FastDiv& dv, const T* __restrict__ mat) {
+  const int Vt = (int)dv.d;
   const int ncol = B * Vt;
   const int ldm = (M + 3) & ~3;
-  const FastDiv dv((uint32_t)Vt);
   for (int col = threadIdx.x; col < ncol; col += blockDim.x) {
     const int b = (int)dv.div((uint32_t)col);
     const int v = col - b * Vt;
@@ -289,7 +318,7 @@ __device__ __forceinline__ void gather_contract_m(const double* __restrict__ x, 
 
 template <typename T>
 __device__ __forceinline__ void gather_contract(const double* x, int64_t ldx, const int* mp, int64_t eoff, T* out,
-                                                int K, int M, int B, int Vt, const T* mat) {
+                                                int K, int M, int B, const FastDiv& Vt, const T* mat) {
   if (M <= 4) gather_contract_m<T, 4>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
   else if (M <= 8) gather_contract_m<T, 8>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
   else if (M <= 12) gather_contract_m<T, 12>(x, ldx, mp, eoff, out, K, M, B, Vt, mat);
@@ -439,6 +468,7 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
   __shared__ int s_item;
   __shared__ TermDesc s_term;
   __shared__ StageBlocks s_blocks;
+  __shared__ ItemDivs s_div;
   const int nb0 = p.nb0;
   while (true) {
     if (threadIdx.x == 0) s_item = atomicAdd(p.counter, 1);
@@ -470,6 +500,7 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
       }
     }
     T* const mb = reinterpret_cast<T*>(smem_raw);
+    fill_item_divs(s_div, s_term, w.vt);  // visible after the barriers of stage_matrices
     stage_matrices<T>(s_term, D, p.mats, mb, s_blocks);
     const TermDesc& Tm = s_term;
     const int NQ = Tm.NQ, NB = Tm.NB, Vt = w.vt;
@@ -486,14 +517,14 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
       T* A1 = X1 + e * stride;
       T* cur = (D % 2) ? A0 : A1;   // so that the chain ends in A0
       int nb_rest = NB / Tm.nb[0];
-      gather_contract<T>(p.x + w.v0, p.ldx, p.map + Tm.off_nb, p.Np * e, cur, Tm.nb[0], Tm.nq[0], nb_rest, Vt,
+      gather_contract<T>(p.x + w.v0, p.ldx, p.map + Tm.off_nb, p.Np * e, cur, Tm.nb[0], Tm.nq[0], nb_rest, s_div.fv,
                          mb + Tm.m_d0b[0]);
       __syncthreads();
       int A = Tm.nq[0];
       for (int i = 1; i < D; ++i) {
         nb_rest /= Tm.nb[i];
         T* nxt = (cur == A0) ? A1 : A0;
-        contract<T>(cur, Vt, nxt, Vt, A, Tm.nb[i], Tm.nq[i], nb_rest, Vt, mb + Tm.m_d0b[i], T(1), false);
+        contract<T>(cur, Vt, nxt, Vt, s_div.fq[i], Tm.nb[i], Tm.nq[i], nb_rest, s_div.fv, mb + Tm.m_d0b[i], T(1), false);
         __syncthreads();
         cur = nxt;
         A *= Tm.nq[i];
@@ -531,7 +562,7 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
         int A = 1, Bq = NQ;
         for (int j = 0; j < D; ++j) {  // Y[j] = d1_j . psi_G
           Bq /= Tm.nq[j];
-          contract<T>(P0, Vt, Y + j * stride, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, mb + Tm.m_d1[j], T(1), false);
+          contract<T>(P0, Vt, Y + j * stride, Vt, s_div.fq[j], Tm.nq[j], Tm.nq[j], Bq, s_div.fv, mb + Tm.m_d1[j], T(1), false);
           A *= Tm.nq[j];
         }
         __syncthreads();
@@ -544,7 +575,7 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
         A = 1; Bq = NQ;
         for (int i = 0; i < D; ++i) {  // Acc += -1/2 d1_i . Y[i]; same-fibre updates per mode
           Bq /= Tm.nq[i];
-          contract<T>(Y + i * stride, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d1[i], T(-0.5), true);
+          contract<T>(Y + i * stride, Vt, Acc, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bq, s_div.fv, mb + Tm.m_d1[i], T(-0.5), true);
           __syncthreads();
           A *= Tm.nq[i];
         }
@@ -559,7 +590,7 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
           Bq /= Tm.nq[i];
           const T f = (T)(-0.5 * __ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[i]));
           if (f != T(0))
-            contract<T>(P0, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d2[i], f, true);
+            contract<T>(P0, Vt, Acc, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bq, s_div.fv, mb + Tm.m_d2[i], f, true);
           __syncthreads();
           A *= Tm.nq[i];
         }
@@ -572,9 +603,9 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
               const int Bj = NQ / (Aj * Tm.nq[j]);
               const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]));
               if (f != T(0)) {
-                contract<T>(P0, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, mb + Tm.m_d1[i], T(1), false);
+                contract<T>(P0, Vt, Y, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bi, s_div.fv, mb + Tm.m_d1[i], T(1), false);
                 __syncthreads();
-                contract<T>(Y, Vt, Acc, Vt, Aj, Tm.nq[j], Tm.nq[j], Bj, Vt, mb + Tm.m_d1[j], f, true);
+                contract<T>(Y, Vt, Acc, Vt, s_div.fq[j], Tm.nq[j], Tm.nq[j], Bj, s_div.fv, mb + Tm.m_d1[j], f, true);
                 __syncthreads();
               }
               Aj *= Tm.nq[j];
@@ -595,10 +626,10 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
         Bq /= Tm.nq[i];
         if (i == D - 1) {
           T* dst = p.ht + (Tm.off_nb * nb0 + (int64_t)e * NB) * p.ldh + w.v0;
-          contract<T>(cur, Vt, dst, p.ldh, A, Tm.nq[i], Tm.nb[i], Bq, Vt, mb + Tm.m_bgw[i], T(1), false);
+          contract<T>(cur, Vt, dst, p.ldh, s_div.fb[i], Tm.nq[i], Tm.nb[i], Bq, s_div.fv, mb + Tm.m_bgw[i], T(1), false);
         } else {
           T* nxt = (cur == A0) ? A1 : A0;
-          contract<T>(cur, Vt, nxt, Vt, A, Tm.nq[i], Tm.nb[i], Bq, Vt, mb + Tm.m_bgw[i], T(1), false);
+          contract<T>(cur, Vt, nxt, Vt, s_div.fb[i], Tm.nq[i], Tm.nb[i], Bq, s_div.fv, mb + Tm.m_bgw[i], T(1), false);
           cur = nxt;
         }
         __syncthreads();
@@ -765,13 +796,14 @@ __device__ __forceinline__ void slab_pointwise_G(const ItemParams<T>& p, const T
 // Phi = G(Q) y in place, Acc += -1/2 sum_{i<L} d1_i Phi_i  (Phi_L stays in P1 for the
 // grid->basis side of the streamed position).  Starts after a barrier, ends with one.
 template <typename T, bool GFLY>
-__device__ __forceinline__ void slab_keo10(const ItemParams<T>& p, const TermDesc& Tm, const T* mb, T* P, T* Y, T* P1,
-                                           T* Acc, int64_t ss, int Vt, int q, int NQs, int nG) {
+__device__ __forceinline__ void slab_keo10(const ItemParams<T>& p, const TermDesc& Tm, const ItemDivs& s_div,
+                                           const T* mb, T* P, T* Y, T* P1, T* Acc, int64_t ss, int Vt, int q,
+                                           int NQs, int nG) {
   const int D = Tm.D, L = D - 1;
   int A = 1, Bq = NQs;
   for (int j = 0; j < L; ++j) {  // Y[j] = d1_j psi
     Bq /= Tm.nq[j];
-    contract<T>(P, Vt, Y + j * ss, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, mb + Tm.m_d1[j], T(1), false);
+    contract<T>(P, Vt, Y + j * ss, Vt, s_div.fq[j], Tm.nq[j], Tm.nq[j], Bq, s_div.fv, mb + Tm.m_d1[j], T(1), false);
     A *= Tm.nq[j];
   }
   __syncthreads();
@@ -786,7 +818,7 @@ __device__ __forceinline__ void slab_keo10(const ItemParams<T>& p, const TermDes
   Bq = NQs;
   for (int i = 0; i < L; ++i) {  // Acc += -1/2 d1_i Phi_i
     Bq /= Tm.nq[i];
-    contract<T>(Y + i * ss, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d1[i], T(-0.5), true);
+    contract<T>(Y + i * ss, Vt, Acc, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bq, s_div.fv, mb + Tm.m_d1[i], T(-0.5), true);
     __syncthreads();
     A *= Tm.nq[i];
   }
@@ -811,6 +843,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
   __shared__ int s_item;
   __shared__ TermDesc s_term;
   __shared__ StageBlocks s_blocks;
+  __shared__ ItemDivs s_div;
   while (true) {
     if (threadIdx.x == 0) s_item = atomicAdd(p.counter, 1);
     __syncthreads();
@@ -841,6 +874,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
       }
     }
     T* const mb = reinterpret_cast<T*>(smem_raw);
+    fill_item_divs(s_div, s_term, w.vt);  // visible after the barriers of stage_matrices
     stage_matrices<T>(s_term, D, p.mats, mb, s_blocks);
     const TermDesc& Tm = s_term;
     const int Vt = w.vt;
@@ -861,7 +895,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
     T* const wbuf = wg ? gbuf + tsz : sm;            // W, and the first ping-pong tensor
     T* const pong = wg ? gbuf + 2 * tsz : sm + tsz;  // second ping-pong tensor of phases A and C
     T* const slabs = wg ? sm : sm + tsz;             // Acc, P, Y
-    const FastDiv dvt((uint32_t)Vt);
+    const FastDiv& dvt = s_div.fv;
 
     // ---- A: gather + B->G over positions 0..L-1
     if (L == 0) {
@@ -875,14 +909,14 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
       T* b1 = pong;
       int nb_rest = Tm.NB / Tm.nb[0];
       T* cur = (L == 1) ? Tg : b0;
-      gather_contract<T>(p.x + w.v0, p.ldx, p.map + Tm.off_nb, 0, cur, Tm.nb[0], Tm.nq[0], nb_rest, Vt,
+      gather_contract<T>(p.x + w.v0, p.ldx, p.map + Tm.off_nb, 0, cur, Tm.nb[0], Tm.nq[0], nb_rest, s_div.fv,
                          mb + Tm.m_d0b[0]);
       __syncthreads();
       int A = Tm.nq[0];
       for (int i = 1; i < L; ++i) {
         nb_rest /= Tm.nb[i];
         T* nxt = (i == L - 1) ? Tg : (cur == b0 ? b1 : b0);
-        contract<T>(cur, Vt, nxt, Vt, A, Tm.nb[i], Tm.nq[i], nb_rest, Vt, mb + Tm.m_d0b[i], T(1), false);
+        contract<T>(cur, Vt, nxt, Vt, s_div.fq[i], Tm.nb[i], Tm.nq[i], nb_rest, s_div.fv, mb + Tm.m_d0b[i], T(1), false);
         __syncthreads();
         cur = nxt;
         A *= Tm.nq[i];
@@ -907,8 +941,8 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
       // over its Psi and DPsi slab (Acc, Phi_L), then one basis<-grid contraction into W
       T* const Psi = gbuf + 3 * tsz;
       T* const DPsi = Psi + (int64_t)gL * ss;
-      contract<T>(Tg, Vt, Psi, Vt, NQs, nL, gL, 1, Vt, X0, T(1), false);
-      contract<T>(Tg, Vt, DPsi, Vt, NQs, nL, gL, 1, Vt, mb + Tm.m_x1L, T(1), false);
+      contract<T>(Tg, Vt, Psi, Vt, s_div.fq[L], nL, gL, 1, s_div.fv, X0, T(1), false);
+      contract<T>(Tg, Vt, DPsi, Vt, s_div.fq[L], nL, gL, 1, s_div.fv, mb + Tm.m_x1L, T(1), false);
       const T mw = p.mu_dev ? (T)__ldg(p.mu_dev) : p.mw;
       const T vw = p.mugrid ? p.vw : T(1);
       const int s32 = (int)ss;
@@ -929,16 +963,16 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
           Acc[a] = v * x;
         }
         __syncthreads();
-        slab_keo10<T, GFLY>(p, Tm, mb, P, Y, P1, Acc, ss, Vt, q, NQs, nG);
+        slab_keo10<T, GFLY>(p, Tm, s_div, mb, P, Y, P1, Acc, ss, Vt, q, NQs, nG);
         for (int a = threadIdx.x; a < s32; a += blockDim.x) {
           ps[a] = Acc[a];
           ds[a] = P1[a];
         }
       }
       __syncthreads();
-      contract<T>(Psi, Vt, W, Vt, NQs, gL, nL, 1, Vt, OUT, T(1), false);
+      contract<T>(Psi, Vt, W, Vt, s_div.fq[L], gL, nL, 1, s_div.fv, OUT, T(1), false);
       __syncthreads();
-      contract<T>(DPsi, Vt, W, Vt, NQs, gL, nL, 1, Vt, mb + Tm.m_e1L, T(-0.5), true);
+      contract<T>(DPsi, Vt, W, Vt, s_div.fq[L], gL, nL, 1, s_div.fv, mb + Tm.m_e1L, T(-0.5), true);
     } else {
       for (int64_t i = threadIdx.x; i < tsz; i += blockDim.x) W[i] = T(0);
     }
@@ -953,7 +987,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         slab_extract_fused<T>(Tg, ss, nL, X0 + q, mb + Tm.m_x1L + q, ldx0, P, P1, Acc,
                               p.vgrid + Tm.off_nq + (int64_t)q * NQs, Mq, p.mugrid ? p.vw : T(1), mw, dvt);
         __syncthreads();
-        slab_keo10<T, GFLY>(p, Tm, mb, P, Y, P1, Acc, ss, Vt, q, NQs, nG);
+        slab_keo10<T, GFLY>(p, Tm, s_div, mb, P, Y, P1, Acc, ss, Vt, q, NQs, nG);
         slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), mb + Tm.m_e1L + (int64_t)ldo * q, P1,
                            T(-0.5));
         continue;
@@ -978,7 +1012,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         int A = 1, Bq = NQs;
         for (int j = 0; j < L; ++j) {  // Y[j] = d1_j P
           Bq /= Tm.nq[j];
-          contract<T>(P, Vt, Y + j * ss, Vt, A, Tm.nq[j], Tm.nq[j], Bq, Vt, mb + Tm.m_d1[j], T(1), false);
+          contract<T>(P, Vt, Y + j * ss, Vt, s_div.fq[j], Tm.nq[j], Tm.nq[j], Bq, s_div.fv, mb + Tm.m_d1[j], T(1), false);
           A *= Tm.nq[j];
         }
         __syncthreads();
@@ -995,7 +1029,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         Bq = NQs;
         for (int i = 0; i < L; ++i) {  // Acc += -1/2 d1_i Phi_i
           Bq /= Tm.nq[i];
-          contract<T>(Y + i * ss, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d1[i], T(-0.5), true);
+          contract<T>(Y + i * ss, Vt, Acc, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bq, s_div.fv, mb + Tm.m_d1[i], T(-0.5), true);
           __syncthreads();
           A *= Tm.nq[i];
         }
@@ -1008,7 +1042,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
           Bq /= Tm.nq[i];
           const T f = (T)(-0.5 * __ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[i]));
           if (f != T(0))
-            contract<T>(P, Vt, Acc, Vt, A, Tm.nq[i], Tm.nq[i], Bq, Vt, mb + Tm.m_d2[i], f, true);
+            contract<T>(P, Vt, Acc, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bq, s_div.fv, mb + Tm.m_d2[i], f, true);
           __syncthreads();
           A *= Tm.nq[i];
         }
@@ -1021,9 +1055,9 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
               const int Bj = NQs / (Aj * Tm.nq[j]);
               const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]));
               if (f != T(0)) {
-                contract<T>(P, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, mb + Tm.m_d1[i], T(1), false);
+                contract<T>(P, Vt, Y, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bi, s_div.fv, mb + Tm.m_d1[i], T(1), false);
                 __syncthreads();
-                contract<T>(Y, Vt, Acc, Vt, Aj, Tm.nq[j], Tm.nq[j], Bj, Vt, mb + Tm.m_d1[j], f, true);
+                contract<T>(Y, Vt, Acc, Vt, s_div.fq[j], Tm.nq[j], Tm.nq[j], Bj, s_div.fv, mb + Tm.m_d1[j], f, true);
                 __syncthreads();
               }
               Aj *= Tm.nq[j];
@@ -1041,7 +1075,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
             const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[L]));
             if (f != T(0)) {
               __syncthreads();
-              contract<T>(P, Vt, Y, Vt, Ai, Tm.nq[i], Tm.nq[i], Bi, Vt, mb + Tm.m_d1[i], T(1), false);
+              contract<T>(P, Vt, Y, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bi, s_div.fv, mb + Tm.m_d1[i], T(1), false);
               __syncthreads();
               slab_accumulate<T>(W, ss, nL, mb + Tm.m_e1L + (int64_t)ldo * q, Y, f, nullptr, nullptr, T(0));
             }
@@ -1068,10 +1102,10 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         Bq /= Tm.nq[i];
         const int Bt = Bq * nL;
         if (i == L - 1) {
-          contract<T>(cur, Vt, dst, p.ldh, A, Tm.nq[i], Tm.nb[i], Bt, Vt, mb + Tm.m_bgw[i], T(1), false);
+          contract<T>(cur, Vt, dst, p.ldh, s_div.fb[i], Tm.nq[i], Tm.nb[i], Bt, s_div.fv, mb + Tm.m_bgw[i], T(1), false);
         } else {
           T* nxt = (cur == b0) ? b1 : b0;
-          contract<T>(cur, Vt, nxt, Vt, A, Tm.nq[i], Tm.nb[i], Bt, Vt, mb + Tm.m_bgw[i], T(1), false);
+          contract<T>(cur, Vt, nxt, Vt, s_div.fb[i], Tm.nq[i], Tm.nb[i], Bt, s_div.fv, mb + Tm.m_bgw[i], T(1), false);
           cur = nxt;
         }
         __syncthreads();
