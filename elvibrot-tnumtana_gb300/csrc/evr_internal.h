@@ -13,6 +13,9 @@
 namespace evr {
 
 constexpr int kMaxD = 16;      // modes
+// G(Q) table: point-major, the D(D+1)/2 symmetric entries of a point padded to a multiple
+// of four (16-byte rows in FP32, 32-byte in FP64) so that a point's row loads as vectors
+__host__ __device__ constexpr int g_table_stride(int D) { return (D * (D + 1) / 2 + 3) & ~3; }
 constexpr int kMaxN1 = 24;     // largest 1-D nq (and nb)
 constexpr int kMaxNb0 = 4;     // electronic states
 

@@ -93,15 +93,14 @@ __global__ void grid_eval_kernel(const TermDesc* __restrict__ terms, int n_terms
       V[(int64_t)(melec[2 * m] + nb0 * melec[2 * m + 1]) * NQ + q] += v;
     }
     if (ggrid) {
-      const int nG = D * (D + 1) / 2;
-      double* Gp = ggrid + T.off_nq * nG + q;
+      double* Gp = ggrid + (T.off_nq + q) * g_table_stride(D);
       int c = 0;
       for (int i = 0; i < T.D; ++i)  // (i, j) positions of the term's mode order
         for (int j = i; j < T.D; ++j) {
           const int oi = T.perm[i], oj = T.perm[j];
           double s = G0[oi + D * oj];
           for (int k = 0; k < D; ++k) s += g[oi + D * (oj + D * k)] * Q[k];
-          Gp[(int64_t)c * NQ] = s;
+          Gp[c] = s;
           ++c;
         }
     }
@@ -196,7 +195,9 @@ int upload_problem(evr_ctx* c) {
   EVR_CU(cudaMalloc((void**)&d.vgrid, nv * sizeof(double)), "cudaMalloc vgrid");
   double* gg = nullptr;
   if (P.keo_type == 10 && g_nonzero) {
-    EVR_CU(cudaMalloc((void**)&gg, P.sum_nq * (D * (D + 1) / 2) * sizeof(double)), "cudaMalloc ggrid");
+    const size_t ng = (size_t)P.sum_nq * g_table_stride(D);
+    EVR_CU(cudaMalloc((void**)&gg, ng * sizeof(double)), "cudaMalloc ggrid");
+    EVR_CU(cudaMemsetAsync(gg, 0, ng * sizeof(double), c->stream), "memset ggrid");  // row padding
   }
   c->dp_ggrid = gg;
   grid_eval_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(d.terms, (int)P.terms.size(), d.mats, P.sum_nq, D, nb0,
@@ -209,7 +210,7 @@ int upload_problem(evr_ctx* c) {
   to_float_kernel<<<c->num_sms * 4, 256, 0, c->stream>>>(d.mats, d.mats32, (int64_t)P.mat_pool.size());
   to_float_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(d.vgrid, d.vgrid32, nv);
   if (gg) {
-    const int64_t ng = P.sum_nq * (D * (D + 1) / 2);
+    const int64_t ng = P.sum_nq * g_table_stride(D);
     EVR_CU(cudaMalloc((void**)&c->dp_ggrid32, ng * sizeof(float)), "cudaMalloc ggrid32");
     to_float_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(gg, c->dp_ggrid32, ng);
   }

@@ -18,7 +18,7 @@ struct ItemParams {
   const TermDesc* terms;
   const T* mats;
   const T* vgrid;
-  const T* ggrid;          // SoA symmetric G per term grid point, or nullptr (G constant)
+  const T* ggrid;          // symmetric G per grid point (rows of g_table_stride(D)), or nullptr
   const double* G0;        // D*D per problem, at the term's g0off (used when ggrid == nullptr)
   const double* gco;       // g_ijk per problem at the term's goff: G(Q) = G0 + g.Q evaluated per point
                            // (problems without a G table: gfly != 0)
@@ -130,6 +130,30 @@ __device__ __forceinline__ void fill_item_divs(ItemDivs& dv, const TermDesc& Tm,
     dv.fb[t] = FastDiv::make(pb);
   } else if (t == D + 1) {
     dv.fv = FastDiv::make((uint32_t)vt);
+  }
+}
+
+// The packed G(Q) row of one point (the D(D+1)/2 entries of i <= j < D, i-major) into
+// registers with 16-byte loads; the row is padded to a multiple of four entries and
+// 16-byte aligned (g_table_stride).  For D == DM the row order is the register order.
+template <typename T, int KG>
+__device__ __forceinline__ void load_g_row(const T* __restrict__ gp, T (&G)[KG]) {
+  if constexpr (sizeof(T) == 4) {
+#pragma unroll
+    for (int c = 0; c < KG; c += 4) {
+      const float4 u = __ldg(reinterpret_cast<const float4*>(gp + c));
+      G[c] = u.x;
+      if (c + 1 < KG) G[c + 1] = u.y;
+      if (c + 2 < KG) G[c + 2] = u.z;
+      if (c + 3 < KG) G[c + 3] = u.w;
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < KG; c += 2) {
+      const double2 u = __ldg(reinterpret_cast<const double2*>(gp + c));
+      G[c] = u.x;
+      if (c + 1 < KG) G[c + 1] = u.y;
+    }
   }
 }
 
@@ -409,27 +433,31 @@ template <typename T, int DM, bool GFLY>
 __device__ __forceinline__ void items_pointwise_G(const ItemParams<T>& p, const TermDesc& Tm, T* Y, int64_t stride,
                                                   int Vt, int NQ) {
   const int D = Tm.D;
-  const int nG = Tm.Dp * (Tm.Dp + 1) / 2;  // the table reserves the problem's slots per point
+  const int nG = g_table_stride(Tm.Dp);  // table row of a point (the problem's slots, padded)
   constexpr bool kCache = DM <= (sizeof(T) == 4 ? 8 : 6);
   constexpr int kG = kCache ? DM * (DM + 1) / 2 : 1;
   const int nch = max(1, min(Vt, (int)blockDim.x / max(NQ, 1)));
   auto slot = [D](int i, int j) { return i * D - i * (i - 1) / 2 + (j - i); };
   for (int task = threadIdx.x; task < NQ * nch; task += blockDim.x) {
     const int q = task / nch, ch = task - q * nch;
-    const T* Gp = p.ggrid ? p.ggrid + Tm.off_nq * nG + q : nullptr;
+    const T* Gp = p.ggrid ? p.ggrid + (Tm.off_nq + q) * nG : nullptr;
     double xq[DM];
     if constexpr (GFLY) point_coords<T, DM>(p, Tm, q, D, xq);
     auto gget = [&](int i, int j) -> T {
       if (i >= D || j >= D) return T(0);
       if constexpr (GFLY) return g_model<T, DM>(p, Tm, xq, i, j);
-      return Gp ? __ldg(Gp + (int64_t)slot(i, j) * NQ) : (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]);
+      return Gp ? __ldg(Gp + slot(i, j)) : (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]);
     };
     T G[kG];
     if constexpr (kCache) {
+      if (!GFLY && Gp && D == DM) {
+        load_g_row<T, kG>(Gp, G);
+      } else {
 #pragma unroll
-      for (int i = 0; i < DM; ++i)
+        for (int i = 0; i < DM; ++i)
 #pragma unroll
-        for (int j = i; j < DM; ++j) G[i * DM - i * (i - 1) / 2 + (j - i)] = gget(i, j);
+          for (int j = i; j < DM; ++j) G[i * DM - i * (i - 1) / 2 + (j - i)] = gget(i, j);
+      }
     }
     // the thread's vectors ch, ch + nch, ... in an order rotated by the point, so that the
     // lanes of a warp (neighbouring points, Vt elements apart) fall in different banks
@@ -738,7 +766,7 @@ __device__ __forceinline__ void slab_pointwise_G(const ItemParams<T>& p, const T
   for (int task = threadIdx.x; task < NQs * nch; task += blockDim.x) {
     const int pt = task / nch, ch = task - pt * nch;
     T G[kG];
-    const T* Gp = p.ggrid ? p.ggrid + Tm.off_nq * nG + (int64_t)q * NQs + pt : nullptr;
+    const T* Gp = p.ggrid ? p.ggrid + (Tm.off_nq + (int64_t)q * NQs + pt) * nG : nullptr;
     double xq[DM];
     if constexpr (GFLY) {
       point_coords<T, DM>(p, Tm, pt, L, xq);
@@ -751,13 +779,17 @@ __device__ __forceinline__ void slab_pointwise_G(const ItemParams<T>& p, const T
     auto gload = [&](int i, int j) -> T {
       if (i >= D || j >= D) return T(0);
       if constexpr (GFLY) return g_model<T, DM>(p, Tm, xq, i, j);
-      return Gp ? __ldg(Gp + (int64_t)slot(i, j) * Tm.NQ) : (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]);
+      return Gp ? __ldg(Gp + slot(i, j)) : (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]);
     };
     if constexpr (kCache) {
+      if (!GFLY && Gp && D == DM) {
+        load_g_row<T, kG>(Gp, G);
+      } else {
 #pragma unroll
-      for (int i = 0; i < DM; ++i)
+        for (int i = 0; i < DM; ++i)
 #pragma unroll
-        for (int j = i; j < DM; ++j) G[i * DM - i * (i - 1) / 2 + (j - i)] = gload(i, j);
+          for (int j = i; j < DM; ++j) G[i * DM - i * (i - 1) / 2 + (j - i)] = gload(i, j);
+      }
     }
     // vectors in an order rotated by the point (bank-conflict free, as in items_pointwise_G)
     const int cnt = (Vt - ch + nch - 1) / nch;
@@ -932,7 +964,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
     const int ldx0 = (gL + 3) & ~3, ldo = (nL + 3) & ~3;
     const T* X0 = mb + Tm.m_d0b[L];
     const T* OUT = mb + Tm.m_bgw[L];
-    const int nG = Tm.Dp * (Tm.Dp + 1) / 2;  // G-table slots per point (term offset)
+    const int nG = g_table_stride(Tm.Dp);  // G-table row of a point
     const bool staged = sizeof(T) == 4 && w.smem == 4 && p.keo_on && p.keo_type == 10;
     if (staged) {
       // grid-staged (FP32 type 10, buffers in global memory): the streamed position's

@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(kStageThreads) stg_grid(GridArgs ga, const T* 
       }
       if (ga.keo_type == 10) {
         if (ggrid) {
-          const T* Gp = ggrid + q;
+          const T* Gp = ggrid + (int64_t)q * g_table_stride(D);
           int c = 0;
 #pragma unroll
           for (int i = 0; i < DM; ++i) {
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(kStageThreads) stg_grid(GridArgs ga, const T* 
 #pragma unroll
             for (int j = i; j < DM; ++j) {
               if (j >= D) break;
-              const T gij = __ldg(Gp + (int64_t)c * NQ);
+              const T gij = __ldg(Gp + c);
               ++c;
               z[i] = fma(gij, y[j], z[i]);
               if (j != i) z[j] = fma(gij, y[i], z[j]);
@@ -349,7 +349,7 @@ int stage_chain(evr_ctx* c, const TermDesc& Tm, bool transposed, const double* x
   const T* ggrid = f32 ? (const T*)c->dp_ggrid32 : (const T*)c->dp_ggrid;
   vgrid += Tm.off_nq * nb0 * nb0;
   if (mugrid) mugrid += Tm.off_nq * nb0 * nb0;
-  if (ggrid) ggrid += Tm.off_nq * (D * (D + 1) / 2);
+  if (ggrid) ggrid += Tm.off_nq * g_table_stride(D);
   const int gb = blocks_for(c, (int64_t)Tm.NQ * V);
   const T vw = (T)ex.vw, mw = (T)ex.mw;
   if (D <= 4) launch_grid<T, 4>(ga, gb, s, g, Acc, Z, cs, mats, vgrid, mugrid, vw, mw, ex.mu_dev, ggrid, c->dp.G0);
