@@ -172,10 +172,11 @@ def run_profile(args):
     return 0
 
 
-# DRAM bytes (read + write) of one FP64 64-vector launch of the term kernels: the D=6 L=6
-# capture of profiles/hpsi_slab_kernel_sg4_6d_l6.md (1.25 GB, dominated by the per-point
-# G table and V) scaled to the L=8 grid (37.77 M / 6.49 M points)
-TRAFFIC_PER_LAUNCH = 1.25e9 * 37.769167 / 6.487975
+# DRAM bytes (read + write) of one FP64 64-vector launch of the term kernels: an ncu
+# capture of the D=6 L=6 launch (`--profile sg4_6d_l6 --prec fp64`; 1.335 GB read + 0.074 GB
+# written, dominated by the per-point G table and V) scaled to the L=8 grid (37.77 M /
+# 6.49 M points)
+TRAFFIC_PER_LAUNCH = (1335056896 + 73895168) * 37.769167 / 6.487975
 DAV_LEVELS, DAV_BLOCK, DAV_RESI = 50, 64, 1e-7
 
 
