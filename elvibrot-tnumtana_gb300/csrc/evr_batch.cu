@@ -13,10 +13,10 @@
 // evr_batch_davidson runs sub_propagation_Davidson (sub_module_Davidson.f90:54-748, as in
 // evr_davidson.cu) for every problem at once: all problems share the subspace size, so the
 // per-problem projections and Ritz combinations are segmented products over row chunks
-// of the stack (partial Grams summed per problem in a fixed order), the small projected eigenproblems are solved by a batched Jacobi kernel (one
-// CTA per problem), and the H.psi of the new directions of all problems is one call.
-// Mixed precision follows evr_davidson (FP32 phase, then FP64 H.psi of the kept Ritz
-// vectors and FP32 H.psi for new directions with the FP64 side of every mixed product).
+// of the stack (partial Grams summed per problem in a fixed order), the small projected
+// eigenproblems are solved by a batched Jacobi kernel (one CTA per problem), and the H.psi
+// of the new directions of all problems is one call.  Mixed precision: an FP32 phase as in
+// evr_davidson, then the FP64 iteration continued from its Ritz vectors.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -815,12 +815,10 @@ struct BatchDavidson {
     return EVR_OK;
   }
 
-  // projected matrices, new columns n0..n1; columns 0..ke-1 carry an FP64 H.psi
-  int rayleigh_ritz(int n0, int n1, int ke) {
+  // projected matrices, new columns n0..n1 (all columns carry an H.psi of one precision)
+  int rayleigh_ritz(int n0, int n1) {
     int rc = gram(Pt.d(), M, HPt.d() + n0, M, n1, n1 - n0, Hs.d() + (int64_t)M * n0, M, sh);
     if (rc) return rc;
-    const int kx = std::min(ke, n0);
-    if (kx > 0 && (rc = gram(HPt.d(), M, Pt.d() + n0, M, kx, n1 - n0, Hs.d() + (int64_t)M * n0, M, sh))) return rc;
     batch_mirror_kernel<<<nsys, kBT, 0, s>>>(Hs.d(), M, sh, n0, n1, (const unsigned char*)dead.p, M);
     return jacobi(Hs.d(), M, sh, n1, Ev.d(), M, Wv.d(), M, sh);
   }
@@ -882,21 +880,14 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
     n1 = ninit;
   }
   int prec = o->prec;
-  bool refine = false;
-  int ke = 0;
   int64_t c64 = 0, c32 = 0;
   std::vector<double> Eh((size_t)nsys * M), Eold((size_t)nsys * nlev, 1e300), rn((size_t)nsys * d.nkeep);
   double best_r = 1e300;
   int stall = 0, it = 0;
   bool converged = false;
   for (it = 0; it < o->max_it; ++it) {
-    if (refine && n0 < ke) {
-      if ((rc = d.hop(d.Pt.d() + n0, M, d.HPt.d() + n0, M, ke - n0, EVR_PREC_FP64, c64, c32))) return rc;
-      if (n1 > ke && (rc = d.hop(d.Pt.d() + ke, M, d.HPt.d() + ke, M, n1 - ke, EVR_PREC_FP32, c64, c32))) return rc;
-    } else if ((rc = d.hop(d.Pt.d() + n0, M, d.HPt.d() + n0, M, n1 - n0, prec, c64, c32))) {
-      return rc;
-    }
-    if ((rc = d.rayleigh_ritz(n0, n1, refine ? ke : 0))) return rc;
+    if ((rc = d.hop(d.Pt.d() + n0, M, d.HPt.d() + n0, M, n1 - n0, prec, c64, c32))) return rc;
+    if ((rc = d.rayleigh_ritz(n0, n1))) return rc;
     n0 = n1;
     const int k = std::min(d.nkeep, n1);
     // Ritz vectors and their H.psi
@@ -928,7 +919,7 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
     }
     // problems with nothing left to do stop taking H.psi (their new columns are empty)
     for (int q = 0; q < nsys; ++q) d.active[q] = (nt < nlev || !todo[q].empty()) ? 1 : 0;
-    if (nt == nlev && most == 0 && (prec == EVR_PREC_FP64 || refine)) {
+    if (nt == nlev && most == 0 && prec == EVR_PREC_FP64) {
       converged = true;
       break;
     }
@@ -936,20 +927,24 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
       double hscale = 0.0;
       for (int q = 0; q < nsys; ++q)
         hscale = std::max(hscale, std::max(std::fabs(Eh[(size_t)q * M]), std::fabs(Eh[(size_t)q * M + nt - 1])));
-      const bool floor_hit = !refine && rmax < std::max(o->conv_resi, 1e-4 * hscale);
-      if (rmax < (refine ? 0.7 : 0.5) * best_r) { best_r = rmax; stall = 0; } else ++stall;
-      if (floor_hit || stall >= (refine ? 3 : 1) || (!refine && most == 0)) {
+      // the FP32 phase ends at a residual of 1e-4 of the level energies, when the largest
+      // residual stops halving, or when every level meets the tolerance; the solve then
+      // continues as the FP64 iteration from the Ritz vectors (in lock step a mixed
+      // refinement would recompute the Ritz vectors' H.psi in FP64 after every subspace
+      // restart, as many FP64 H.psi as the plain solve)
+      const bool floor_hit = rmax < std::max(o->conv_resi, 1e-4 * hscale);
+      if (rmax < 0.5 * best_r) { best_r = rmax; stall = 0; } else ++stall;
+      if (floor_hit || stall >= 1 || most == 0) {
         const int kr = std::min(k, nlev);
         if (cudaMemcpy2DAsync(d.Pt.p, sizeof(double) * M, d.X.p, sizeof(double) * d.nkeep, sizeof(double) * kr, N,
                               cudaMemcpyDeviceToDevice, s) ||
             cudaMemsetAsync(d.dead.p, 0, (size_t)nsys * M, s))
           return set_error(c, EVR_EDEVICE, "restart copy");
-        refine = true;
-        ke = kr;
+        prec = EVR_PREC_FP64;
         n1 = kr;
         n0 = 0;
         std::fill(Eold.begin(), Eold.end(), 1e300);
-        std::fill(d.active.begin(), d.active.end(), 1);  // every problem refines its Ritz vectors
+        std::fill(d.active.begin(), d.active.end(), 1);  // every problem continues in FP64
         best_r = 1e300;
         stall = 0;
         continue;
@@ -979,20 +974,6 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
       return set_error(c, EVR_EDEVICE, "copy");
     batch_zero_rows_kernel<<<c->num_sms * 8, kBT, 0, s>>>(d.T.d(), d.bmax, 0, ns, d.sys_d,
                                                           (const unsigned char*)d.actv.p, N);
-    if (n1 + ns > M && refine) {
-      // refinement: a refresh, the Ritz vectors' H.psi recomputed in FP64 (their combined
-      // H.psi holds FP32 columns and must not serve as an exact column)
-      const int kr = std::min(k, nlev);
-      if (cudaMemcpy2DAsync(d.Pt.p, sizeof(double) * M, d.X.p, sizeof(double) * d.nkeep, sizeof(double) * kr, N,
-                            cudaMemcpyDeviceToDevice, s) ||
-          cudaMemsetAsync(d.dead.p, 0, (size_t)nsys * M, s))
-        return set_error(c, EVR_EDEVICE, "restart copy");
-      std::fill(d.active.begin(), d.active.end(), 1);
-      ke = kr;
-      n1 = kr;
-      n0 = 0;
-      continue;
-    }
     if (n1 + ns > M) {
       if (cudaMemcpy2DAsync(d.Pt.p, sizeof(double) * M, d.X.p, sizeof(double) * d.nkeep, sizeof(double) * k, N,
                             cudaMemcpyDeviceToDevice, s) ||
@@ -1002,7 +983,6 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
         return set_error(c, EVR_EDEVICE, "restart copy");
       batch_diag_kernel<<<nsys, kBT, 0, s>>>(d.Hs.d(), M, d.sh, d.Ev.d(), M, k);
       n1 = n0 = k;
-      ke = k;
     }
     if ((rc = d.orthonormalize(ns, n1))) return rc;
     n1 += ns;
