@@ -144,6 +144,20 @@ def test_linearity_and_oracle_sg4_6d_l8():
     assert rel(pg.hpsi(a), ref) <= FP64_TOL
 
 
+def test_fp32_slab_modes_sg4_6d_l6():
+    # D=6 L=6 with 32 vectors: in FP32 most grid points run in the grid-staged slab mode
+    # (tiles of up to 4 vectors), the rest in the shared-memory and W-in-global modes;
+    # every mode is checked against the oracle, and FP64 on the same block
+    spec = S.config_sg4(6, 6, seed=1)
+    pg = E.Problem(spec, device=0)
+    po = O.OracleProblem(spec)
+    rng = np.random.default_rng(13)
+    psi = rng.standard_normal((pg.N, 32))
+    ref = po.hpsi(psi)
+    assert rel(pg.hpsi(psi, prec="fp32"), ref) <= FP32_TOL
+    assert rel(pg.hpsi(psi, prec="fp64"), ref) <= FP64_TOL
+
+
 def test_errors_are_reported_not_fatal():
     spec, pg, po = problems("hh6d_l3_type1")
     with pytest.raises(E.EvrError) as ei:
