@@ -270,7 +270,9 @@ int evr_oc_backward(evr_ctx *ctx, double *grad, double *ref, int64_t *info);
  * n_sys + 1 values), and evr_hpsi_* apply the block-diagonal H -- every problem, every
  * column -- in one launch of the term kernels.  evr_batch_davidson: the lowest n_levels of
  * every problem (eig: n_sys x n_levels, problem-major), one state per problem (nb0 = 1),
- * subspace at most 64; info as evr_davidson (H.psi counts are per problem summed).
+ * subspace at most 64; info as evr_davidson (H.psi counts are per problem summed).  With
+ * prec = EVR_PREC_FP32 an FP32 phase runs first and the FP64 iteration continues from its
+ * Ritz vectors, so the levels are those of the FP64 operator.
  */
 int evr_create_batch(evr_ctx **ctx, const evr_problem_desc *descs, int n_sys, int device);
 int evr_batch_offsets(const evr_ctx *ctx, int64_t *offsets);
