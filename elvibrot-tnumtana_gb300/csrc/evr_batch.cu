@@ -18,8 +18,10 @@
 // of the new directions of all problems is one call.  Mixed precision: an FP32 phase as in
 // evr_davidson, then the FP64 iteration continued from its Ritz vectors.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <numeric>
 #include <vector>
 
@@ -626,10 +628,25 @@ int evr_create_batch(evr_ctx** out, const evr_problem_desc* descs, int n_sys, in
   c->batch = b;
   b->sub.resize(n_sys);
   b->off.assign(n_sys + 1, 0);
+  {
+    // the problems' host tables are independent: built on up to 16 host threads, each
+    // taking the next problem; errors are reported for the first failing problem in order
+    std::vector<int> rcs(n_sys, EVR_OK);
+    std::vector<std::string> errs(n_sys);
+    std::atomic<int> next{0};
+    auto work = [&]() {
+      for (int s = next.fetch_add(1); s < n_sys; s = next.fetch_add(1))
+        rcs[s] = build_host_problem(&descs[s], b->sub[s], errs[s]);
+    };
+    const int nthr = std::max(1, std::min({n_sys, 16, (int)std::thread::hardware_concurrency()}));
+    std::vector<std::thread> pool;
+    for (int i = 1; i < nthr; ++i) pool.emplace_back(work);
+    work();
+    for (std::thread& t : pool) t.join();
+    for (int s = 0; s < n_sys; ++s)
+      if (rcs[s]) return set_error(c, rcs[s], "evr_create_batch: problem " + std::to_string(s) + ": " + errs[s]);
+  }
   for (int s = 0; s < n_sys; ++s) {
-    std::string err;
-    int rc = build_host_problem(&descs[s], b->sub[s], err);
-    if (rc) return set_error(c, rc, "evr_create_batch: problem " + std::to_string(s) + ": " + err);
     b->off[s + 1] = b->off[s] + b->sub[s].Np;
     b->term_sys.insert(b->term_sys.end(), b->sub[s].terms.size(), s);
   }

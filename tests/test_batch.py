@@ -24,6 +24,21 @@ def test_batch_tables_on_host():
     assert abs(b.flop_per_hpsi - sum(p.flop_per_hpsi for p in singles)) <= 1e-9 * b.flop_per_hpsi
 
 
+def test_batch_merged_tables_match_single_problems():
+    # the stacked map and weights (host tables built on several threads) equal the single
+    # problems' tables with the packed indices shifted by each problem's row offset
+    sp = specs()
+    for _ in range(2):
+        b = E.BatchProblem(sp, device=-1)
+        tb = b.tables()
+        singles = [E.Problem(x, device=-1) for x in sp]
+        ts = [p.tables() for p in singles]
+        w = np.concatenate([t["weight"] for t in ts])
+        m = np.concatenate([np.where(t["map"] >= 0, t["map"] + off, -1) for t, off in zip(ts, b.offsets[:-1])])
+        assert np.array_equal(tb["weight"], w)
+        assert np.array_equal(tb["map"], m)
+
+
 def test_batch_rejects_mixed_state_counts():
     sp = specs()[:2] + [S.pyrazine_12d(1)]
     with pytest.raises(E.EvrError) as ei:
