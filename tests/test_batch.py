@@ -39,6 +39,18 @@ def test_batch_merged_tables_match_single_problems():
         assert np.array_equal(tb["map"], m)
 
 
+def test_batch_reports_the_first_invalid_problem():
+    import dataclasses
+    sp = specs()
+    bad = dataclasses.replace(sp[2], scaleQ=-np.abs(np.asarray(sp[2].scaleQ)))  # scaleQ must be > 0
+    sp[2] = bad
+    sp[4] = dataclasses.replace(sp[4], scaleQ=-np.abs(np.asarray(sp[4].scaleQ)))
+    with pytest.raises(E.EvrError) as ei:
+        E.BatchProblem(sp, device=-1)
+    assert ei.value.code == E.EVR_EINVAL
+    assert "problem 2:" in str(ei.value)
+
+
 def test_batch_rejects_mixed_state_counts():
     sp = specs()[:2] + [S.pyrazine_12d(1)]
     with pytest.raises(E.EvrError) as ei:
