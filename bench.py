@@ -101,6 +101,23 @@ def dist_info():
     return rank, world, local
 
 
+def max_over_ranks(x: float, device) -> float:
+    """The largest x over the ranks of the default process group (x itself on one rank)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: float, seconds_max: float, world: int) -> float:
+    """Whole-job throughput: the units of every rank over the slowest rank's time."""
+    return world * units_per_rank / seconds_max
+
+
 def cpu_oracle_rate(spec, nvec_sample, threads):
     """Oracle H.psi/s on the host cores for a bounded sample of the block."""
     from oracle import oracle as O
@@ -414,12 +431,8 @@ def main():
         launches = p.last_launch_count()[0] * args.steps
         t32, k32 = timed("fp32", y32)
         launches += p.last_launch_count()[0] * args.steps
-    total64 = sum(t64)
-    if world > 1:
-        tt = torch.tensor([total64], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total64 = float(tt.item())
-    value = world * NVEC * args.steps / total64
+    total64 = max_over_ranks(sum(t64), "cuda")
+    value = job_rate(NVEC * args.steps, total64, world)
     mixed = NVEC * args.steps / sum(t32)
     err32 = float((y32 - y).abs().max() / y.abs().max())
 
@@ -432,11 +445,13 @@ def main():
     te = []
     for _ in range(args.steps):
         flush.fill_(1.0)
+        if world > 1:
+            torch.distributed.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         p.hpsi_host_ptr(hx.data_ptr(), N, hy.data_ptr(), N, NVEC, E.LAYOUT_COLMAJOR)
         te.append(time.perf_counter() - t0)
-    e2e = NVEC * args.steps / sum(te)
+    e2e = job_rate(NVEC * args.steps, max_over_ranks(sum(te), "cuda"), world)
     e2e_err = float((hy.t().cuda() - y).abs().max() / y.abs().max())
 
     # roofline of the dominant kernel: algorithmic FLOPs of one 64-vector launch over the

@@ -1,0 +1,48 @@
+"""The multi-rank side of bench.py on CPU: two gloo ranks on 127.0.0.1 take the slowest
+rank's time and report the whole-job rate (the same helpers run over NCCL on GPUs)."""
+import os
+import socket
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port):
+    import torch.distributed as dist
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    try:
+        seconds = 1.5 + rank  # rank 1 is the slow one
+        slowest = bench.max_over_ranks(seconds, "cpu")
+        assert slowest == 1.5 + (world - 1)
+        assert bench.job_rate(64 * 5, slowest, world) == pytest.approx(world * 64 * 5 / slowest)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_max_over_ranks_and_job_rate_gloo():
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+
+    if not torch.distributed.is_available():
+        pytest.skip("torch.distributed unavailable")
+    mp.spawn(_rank_main, args=(2, _free_port()), nprocs=2, join=True)
+
+
+def test_single_rank_helpers():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert bench.max_over_ranks(2.25, "cpu") == 2.25
+    assert bench.job_rate(320, 4.0, 1) == 80.0
