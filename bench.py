@@ -113,6 +113,22 @@ def max_over_ranks(x: float, device) -> float:
     return float(t.item())
 
 
+def hbm_roofline(traffic_bytes: float, kernel_s: float, peaks_path: str = None) -> dict:
+    """The DRAM side of the dominant kernel: its measured bytes per launch over its
+    event-timed duration, against the measured copy bandwidth of the GB300s (the
+    fallback figure when the peaks file is absent).  It shows how far HBM is from bounding
+    the kernel."""
+    peaks_path = peaks_path or os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(peaks_path) as f:
+            peak, src = float(json.load(f)["hbm_gbs"]), "measured (hbm_gbs)"
+    except (OSError, KeyError, TypeError, ValueError):
+        peak, src = 6800.0, "fallback"
+    achieved = traffic_bytes / kernel_s / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic_bytes, "peak_source": src}
+
+
 def job_rate(units_per_rank: float, seconds_max: float, world: int) -> float:
     """Whole-job throughput: the units of every rank over the slowest rank's time."""
     return world * units_per_rank / seconds_max
@@ -484,6 +500,7 @@ def main():
                          "algorithmic_flop_per_launch": flop_launch, "dgemm_tflops": dgemm,
                          "peak_source": "FP64 FMA issue rate measured in this run (evr_fma_peak); no FP64 figure "
                                         "in the measured-peaks file"},
+            "roofline_hbm": hbm_roofline(TRAFFIC_PER_LAUNCH, items_ms / 1e3),
             "davidson": dav,
             "autotune": tuned,
             "gpu_launches": launches,

@@ -46,3 +46,17 @@ def test_single_rank_helpers():
 
     assert bench.max_over_ranks(2.25, "cpu") == 2.25
     assert bench.job_rate(320, 4.0, 1) == 80.0
+
+
+def test_hbm_roofline(tmp_path):
+    sys.path.insert(0, ROOT)
+    import bench
+
+    pk = tmp_path / "peaks.json"
+    pk.write_text('{"hbm_gbs": 6000.0}')
+    r = bench.hbm_roofline(3.0e9, 0.5, str(pk))
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s"
+    assert r["achieved"] == 6.0 and r["peak"] == 6000.0 and abs(r["frac"] - 1e-3) < 1e-15
+    assert r["peak_source"].startswith("measured")
+    r = bench.hbm_roofline(3.0e9, 0.5, str(tmp_path / "absent.json"))
+    assert r["peak"] == 6800.0 and r["peak_source"] == "fallback"
