@@ -63,7 +63,9 @@ EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_
            "evr_last_kernel_ms",
            "evr_davidson",
            "evr_cheby_propagate", "evr_fma_peak", "evr_hpsi_noalloc", "evr_set_dipole", "evr_set_field",
-           "evr_oc_forward", "evr_oc_backward", "evr_create_batch", "evr_batch_offsets", "evr_batch_davidson", "evr_autotune"]
+           "evr_oc_forward", "evr_oc_backward", "evr_create_batch", "evr_batch_offsets", "evr_batch_davidson", "evr_autotune",
+           "evr_psi_write", "evr_psi_read"]
+WP_FORMAT = {"v0": 0, "v1": 1, "unformatted": 2, "sparse": 3}
 
 _lib = None
 
@@ -107,6 +109,8 @@ def load(build: bool = True):
     L.evr_set_field.argtypes = [vp, C.c_double, C.c_double, C.c_int]
     L.evr_oc_forward.argtypes = [vp, C.POINTER(OcOpts), _dp, _dp, _dp, _dp, _dp, _lp]
     L.evr_oc_backward.argtypes = [vp, _dp, _dp, _lp]
+    L.evr_psi_write.argtypes = [vp, C.c_char_p, C.c_int, _dp, C.c_int64, C.c_int, C.c_int, C.c_double]
+    L.evr_psi_read.argtypes = [vp, C.c_char_p, _dp, C.c_int64, C.c_int, C.c_int, _ip, _lp]
     if hasattr(L, "evr_davidson"):
         L.evr_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _dp, _dp, _dp, _lp]
     if hasattr(L, "evr_cheby_propagate"):
@@ -234,6 +238,37 @@ class Problem:
         v = np.zeros(self.sum_nq * self.spec.nb0 ** 2)
         self._check(load().evr_get_vgrid(self.h, _p(v, _dp)))
         return v
+
+    # ---- wave-packet files ------------------------------------------------------------
+    def write_psi(self, path, psi, fmt="v0", epsi=0.0):
+        """Packets (columns of psi, N x npsi, real or complex) to a file in the reference's
+        save format (sub_save_psi, Source_ElVibRot/sub_WP/sub_module_psi_io.f90:365):
+        fmt "v0" (its default), "v1", "unformatted" or "sparse" (entries of modulus >= epsi)."""
+        psi = np.asarray(psi)
+        if psi.ndim == 1:
+            psi = psi[:, None]
+        cplx = np.iscomplexobj(psi)
+        a = np.asfortranarray(psi, dtype=np.complex128 if cplx else np.float64)
+        if a.shape[0] != self.N:
+            raise EvrError(EVR_EINVAL, f"psi has {a.shape[0]} rows, expected {self.N}")
+        ptr = a.ctypes.data_as(_dp)
+        self._check(load().evr_psi_write(self.h, os.fsencode(path), WP_FORMAT[fmt], ptr, self.N, a.shape[1],
+                                         1 if cplx else 0, float(epsi)))
+
+    def read_psi(self, path, npsi_max=64, cplx=False, renorm=False):
+        """Packets of a file in any of the reference's save formats, mapped onto this basis by
+        their tuples (sub_read_psi0, sub_module_psi_io.f90:55).  Returns (psi N x npsi,
+        dropped entries).  renorm=True normalises each packet as sub_read_psi0 does."""
+        a = np.zeros((self.N, max(npsi_max, 1)), dtype=np.complex128 if cplx else np.float64, order="F")
+        n = C.c_int()
+        dropped = C.c_int64()
+        self._check(load().evr_psi_read(self.h, os.fsencode(path), a.ctypes.data_as(_dp), self.N, npsi_max,
+                                        1 if cplx else 0, C.byref(n), C.byref(dropped)))
+        a = a[:, : n.value]
+        if renorm:
+            nrm = np.sqrt(np.sum(np.abs(a) ** 2, axis=0))
+            a = a / np.where(nrm > 0, nrm, 1.0)
+        return a, dropped.value
 
     # ---- H.psi ----------------------------------------------------------------------
     def hpsi(self, psi, prec: str = "fp64"):

@@ -278,6 +278,45 @@ int evr_create_batch(evr_ctx **ctx, const evr_problem_desc *descs, int n_sys, in
 int evr_batch_offsets(const evr_ctx *ctx, int64_t *offsets);
 int evr_batch_davidson(evr_ctx *ctx, const evr_davidson_opts *opts, double *eig, int64_t *info);
 
+/*
+ * Wave-packet files in the reference's save formats (host only; any context but a batch,
+ * host-only contexts included).  A basis function is written as its tuple
+ * n_1..n_D i_h i_e (1-based; i_h = 1, i_e = electronic state), as Rec_ndim_index gives it.
+ *   EVR_WP_FORMATTED_V0   "nb_psi nb_tot", then per packet every entry "n.. i_h i_e a [b]"
+ *                         and " end wp k" -- sub_save_psi with FilePsiVersion = 0, the
+ *                         reference's default (Source_ElVibRot/sub_WP/sub_module_psi_io.f90:
+ *                         365-424, Write_Psi_nDBasis version 0 :1607-1700)
+ *   EVR_WP_FORMATTED_V1   &headerFile namelist, the nb_tot tuples, then each packet as one
+ *                         list-directed record (complex as (re,im)) (:1441-1604, :1736-1760)
+ *   EVR_WP_UNFORMATTED_V1 Fortran sequential unformatted records with 4-byte markers:
+ *                         'X', nb_psi, nb_tot, 1, 'X', one int32 record of D+2 per
+ *                         function, one record of nb_tot values per packet (:1483-1489)
+ *   EVR_WP_SPARSE         "nb_psi", then per packet the entries of modulus >= epsi and
+ *                         " end wp k" (ecri_psiBasisRepnotall_nD :783-917)
+ * psi: N x npsi column-major host array (N = Np*nb0, ld >= N); cplx = 1: Fortran COMPLEX(8)
+ * layout, (re, im) of element k of packet j at psi[2*(k + ld*j)].
+ */
+#define EVR_WP_FORMATTED_V0   0
+#define EVR_WP_FORMATTED_V1   1
+#define EVR_WP_UNFORMATTED_V1 2
+#define EVR_WP_SPARSE         3
+int evr_psi_write(evr_ctx *ctx, const char *path, int format, const double *psi, int64_t ld, int npsi, int cplx,
+                  double epsi);
+/* Replaces sub_read_psi0's file branch (sub_module_psi_io.f90:55-263 with
+ * Read_header_saveFile_psi :1294-1439, Read_list_nDindBasis1_TO_nDindBasis2 :1143-1292,
+ * Read_psi_nDBasis :920-1141, lect_psiBasisRepnotall_nD :563-780).  The form is detected:
+ * unformatted version 1, or formatted with a headerFile namelist (version 1), an
+ * "nb_psi nb_tot" line (version 0, entries read by position after the first packet's
+ * tuples), an "nb_psi" line (sparse packets), or no header (sparse packets as in an input
+ * file after its namelists).  Each file function goes to the function of this basis with
+ * the same tuple; functions this basis does not hold are dropped and counted in
+ * *n_dropped (entries over the packets read), functions absent from the file stay zero.
+ * Reads min(packets in the file, npsi_max) packets (*npsi_read).  Unlike sub_read_psi0
+ * it does not renormalise the packets.  A malformed file returns EVR_EINVAL with the
+ * line or record at fault, where the reference STOPs. */
+int evr_psi_read(evr_ctx *ctx, const char *path, double *psi, int64_t ld, int npsi_max, int cplx, int *npsi_read,
+                 int64_t *n_dropped);
+
 #ifdef __cplusplus
 }
 #endif

@@ -11,11 +11,44 @@ Contents:
   hh6d_levels  -> column 1 of Working_tests/MPI_tests/6D_Davidson_S0/benchmark
                   (28 Davidson levels of the 6-D Henon-Heiles SG4 L=3 model, au);
   pyr12d_autocorr -> Working_tests/MPI_tests/12D_propagation_S0/benchmark
-                  (t in au, Re C, Im C, |C| of the 12-D pyrazine SG4 L=1 Chebyshev run).
+                  (t in au, Re C, Im C, |C| of the 12-D pyrazine SG4 L=1 Chebyshev run);
+  wp_inputs    -> the start packets written after the namelists of two input files, in
+                  the sparse form that lect_psiBasisRepnotall_nD reads
+                  (Source_ElVibRot/sub_WP/sub_module_psi_io.f90:563-780):
+                  Working_tests/exa_hcn-test/dat_Davidson (3 modes, 4 real packets) and
+                  Working_tests/MPI_tests/12D_propagation_S0/shell_run (12 modes, one
+                  complex packet on the second electronic state, ended by the file's end).
 """
 import json
 import os
+import re
 import sys
+
+_ENTRY = re.compile(r"^\s*[-+0-9][-+0-9.eEdD\s]*$")
+
+
+def packet_lines(path):
+    """The packet lines (entries and 'end wp' lines) after the namelist that closes just
+    before them ('/' line), up to the first other line."""
+    with open(path) as f:
+        lines = f.read().splitlines()
+
+    def next_nonblank(i):
+        while i < len(lines) and not lines[i].strip():
+            i += 1
+        return i
+
+    start = max(i for i, ln in enumerate(lines) if ln.strip() == "/" and next_nonblank(i + 1) < len(lines)
+                and _ENTRY.match(lines[next_nonblank(i + 1)]))
+    out = []
+    for ln in lines[start + 1:]:
+        if not ln.strip():
+            continue
+        if ln.strip().startswith("end wp") or _ENTRY.match(ln):
+            out.append(ln)
+        else:
+            break
+    return out
 
 
 def main(root):
@@ -32,6 +65,12 @@ def main(root):
         out["hh6d_levels"] = [float(line.split()[0]) for line in f if line.strip()]
     with open(os.path.join(root, "Working_tests", "MPI_tests", "12D_propagation_S0", "benchmark")) as f:
         out["pyr12d_autocorr"] = [[float(v) for v in line.split()] for line in f if line.strip()]
+    out["wp_inputs"] = {
+        "hcn_dat_Davidson": dict(D=3, nb0=1, cplx=False, lines=packet_lines(
+            os.path.join(root, "Working_tests", "exa_hcn-test", "dat_Davidson"))),
+        "pyr12d_shell_run": dict(D=12, nb0=2, cplx=True, lines=packet_lines(
+            os.path.join(root, "Working_tests", "MPI_tests", "12D_propagation_S0", "shell_run"))),
+    }
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.json")
     with open(dst, "w") as f:
         json.dump(out, f, indent=0)
