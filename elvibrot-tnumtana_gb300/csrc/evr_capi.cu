@@ -134,6 +134,42 @@ int evr_get_vgrid(const evr_ctx* c0, double* v) {
   return EVR_OK;
 }
 
+// Replaces the device V table (and its FP32 copy) with caller-supplied grid values: the
+// inverse of evr_get_vgrid's mapping, done on the host and uploaded with plain copies.
+int evr_set_vgrid(evr_ctx* c, const double* v, int layout) {
+  if (!c) return EVR_EINVAL;
+  if (!v || (layout != EVR_VGRID_TERMS && layout != EVR_VGRID_REF))
+    return set_error(c, EVR_EINVAL, "evr_set_vgrid: null values or unknown layout");
+  if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
+  if (c->batch) return set_error(c, EVR_EINVAL, "evr_set_vgrid: not for batched contexts");
+  EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
+  const HostProblem& P = c->hp;
+  const int nb2 = P.nb0 * P.nb0;
+  const size_t n = (size_t)P.sum_nq * nb2;
+  std::vector<double> dev(n);
+  std::vector<float> dev32(n);
+  for (const TermDesc& T : P.terms)
+    for (int ab = 0; ab < nb2; ++ab) {
+      const double shift = ab % (P.nb0 + 1) == 0 ? T.vshift : 0.0;
+      for (int64_t qp = 0; qp < T.NQ; ++qp) {
+        const int64_t q = P.grid_perm[(size_t)T.off_nq + qp] - T.off_nq;
+        const size_t src = layout == EVR_VGRID_TERMS ? (size_t)T.off_nq * nb2 + (size_t)ab * T.NQ + q
+                                                     : (size_t)(T.off_nq + q) + (size_t)P.sum_nq * ab;
+        const size_t dst = (size_t)T.off_nq * nb2 + (size_t)ab * T.NQ + qp;
+        dev[dst] = v[src] + shift;
+        dev32[dst] = (float)dev[dst];
+      }
+    }
+  // an H.psi still reading the old table may run on a caller's stream: wait for the device
+  EVR_CU(cudaDeviceSynchronize(), "sync before vgrid update");
+  EVR_CU(cudaMemcpyAsync(c->dp.vgrid, dev.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+         "copy vgrid");
+  EVR_CU(cudaMemcpyAsync(c->dp.vgrid32, dev32.data(), n * sizeof(float), cudaMemcpyHostToDevice, c->stream),
+         "copy vgrid32");
+  EVR_CU(cudaStreamSynchronize(c->stream), "sync");
+  return EVR_OK;
+}
+
 int evr_set_kernel_path(evr_ctx* c, int path) {
   if (!c) return EVR_EINVAL;
   if (path < 0 || path > 2) return set_error(c, EVR_EINVAL, "evr_set_kernel_path: 0, 1 or 2");

@@ -64,7 +64,8 @@ EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_
            "evr_davidson",
            "evr_cheby_propagate", "evr_fma_peak", "evr_hpsi_noalloc", "evr_set_dipole", "evr_set_field",
            "evr_oc_forward", "evr_oc_backward", "evr_create_batch", "evr_batch_offsets", "evr_batch_davidson", "evr_autotune",
-           "evr_psi_write", "evr_psi_read"]
+           "evr_psi_write", "evr_psi_read", "evr_set_vgrid"]
+VGRID_LAYOUT = {"terms": 0, "ref": 1}
 WP_FORMAT = {"v0": 0, "v1": 1, "unformatted": 2, "sparse": 3}
 
 _lib = None
@@ -93,6 +94,7 @@ def load(build: bool = True):
     L.evr_get_tables.argtypes = [vp, _ip, _dp, _ip, _ip]
     L.evr_get_basis.argtypes = [vp, C.c_int, C.c_int, _ip] + [_dp] * 8
     L.evr_get_vgrid.argtypes = [vp, _dp]
+    L.evr_set_vgrid.argtypes = [vp, _dp, C.c_int]
     L.evr_hpsi_host.argtypes = [vp, _dp, C.c_int64, _dp, C.c_int64, C.c_int, C.c_int, C.c_int]
     L.evr_hpsi_device.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.c_int, C.c_int, C.c_int, vp]
     L.evr_last_launch_count.argtypes = [vp, _lp, _lp]
@@ -238,6 +240,15 @@ class Problem:
         v = np.zeros(self.sum_nq * self.spec.nb0 ** 2)
         self._check(load().evr_get_vgrid(self.h, _p(v, _dp)))
         return v
+
+    def set_vgrid(self, v, layout="terms"):
+        """Potential given as grid values (a host's calcN_op grid cache) in place of the one
+        evaluated from the monomials; layout "terms" (as vgrid()) or "ref" (the reference's
+        OpGrid%Grid(sum_nq, nb0, nb0), column-major)."""
+        v = _darr(np.asarray(v, dtype=np.float64).ravel(order="F"))
+        if v.size != self.sum_nq * self.spec.nb0 ** 2:
+            raise EvrError(EVR_EINVAL, f"V grid has {v.size} values, expected {self.sum_nq * self.spec.nb0 ** 2}")
+        self._check(load().evr_set_vgrid(self.h, _p(v, _dp), VGRID_LAYOUT[layout]))
 
     # ---- wave-packet files ------------------------------------------------------------
     def write_psi(self, path, psi, fmt="v0", epsi=0.0):

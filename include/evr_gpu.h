@@ -113,6 +113,20 @@ int evr_get_basis(const evr_ctx *ctx, int mode, int level, int *nb_nq, double *x
                   double *d1b, double *d2b, double *bgw, double *d1gg, double *d2gg);
 /* Potential on the grid, sum_nq*nb0*nb0 values (term-major, point fastest, then (a,b)). */
 int evr_get_vgrid(const evr_ctx *ctx, double *v);
+/* Potential given as grid values, for a host whose potential is not a polynomial: the
+ * values its calcN_op plugin put in the grid cache (Source_PrimOperator/sub_PrimOp.f90:
+ * 283-655; SG4 fill Source_ElVibRot/sub_Operator/sub_OpPsi_SG4.f90:2754-2767, read per
+ * term through tabR2gridbis_TO_tabR1_AT_iG :2655-2666).  Replaces the V the context evaluated from its
+ * monomials for every later H.psi, Davidson, Chebyshev and control call (FP64 and FP32
+ * tables).  layout EVR_VGRID_TERMS: the layout of evr_get_vgrid; EVR_VGRID_REF: the
+ * reference's OpGrid(iterm)%Grid(sum_nq, nb0, nb0), element (iq, a, b) at
+ * iq + sum_nq*(a + nb0*b), with iq the point of the whole Smolyak grid (terms in the
+ * reference's order, first mode fastest inside a term) and a the output state.  The two
+ * layouts agree for nb0 = 1.  Synchronous (waits for the device first); a set-up call,
+ * not for use inside stream capture; not for batched contexts. */
+#define EVR_VGRID_TERMS 0
+#define EVR_VGRID_REF   1
+int evr_set_vgrid(evr_ctx *ctx, const double *v, int layout);
 
 /* H.psi on a block of vectors.
  * Replaces sub_TabOpPsi (Source_ElVibRot/sub_Operator/sub_OpPsi.f90:701-795) on SG4,

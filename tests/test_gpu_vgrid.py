@@ -1,0 +1,71 @@
+"""evr_set_vgrid: a potential handed over as grid values (as a Fortran host's calcN_op grid
+cache holds it) replaces the one the context evaluated from its monomials.
+
+Parity: after set_vgrid(values), H.psi equals H.psi of the problem whose potential gave
+those values (FP64 1e-12 relative, FP32 2e-5), in both layouts, on the Smolyak term kernels
+(two states, dropped 1-point modes) and the direct-product stage kernels.
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from evrgpu import spec as S
+from evrgpu import lib as E
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+FP32_TOL = 2e-5
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+def with_v_scaled(spec, s):
+    return dataclasses.replace(spec, mono_coef=np.asarray(spec.mono_coef) * s)
+
+
+def terms_to_ref(v, pg, spec):
+    """Terms layout (evr_get_vgrid) -> the reference's OpGrid%Grid(sum_nq, nb0, nb0)."""
+    nb2 = spec.nb0 ** 2
+    term_l = pg.tables()["term_l"]
+    nq = [[pg.basis(d, l)["nq"] for l in range(spec.LG + 1)] for d in range(spec.D)]
+    out = np.zeros(pg.sum_nq * nb2)
+    off = 0
+    for t in range(pg.nterm):
+        NQ = int(np.prod([nq[d][term_l[t, d]] for d in range(spec.D)]))
+        blk = v[off * nb2:(off + NQ) * nb2].reshape(nb2, NQ)
+        for ab in range(nb2):
+            out[ab * pg.sum_nq + off: ab * pg.sum_nq + off + NQ] = blk[ab]
+        off += NQ
+    assert off == pg.sum_nq
+    return out
+
+
+def test_set_vgrid_sg4_two_states_both_layouts():
+    spec = S.pyrazine_12d(1)
+    pa = E.Problem(spec)
+    pb = E.Problem(with_v_scaled(spec, 0.0))
+    v = pa.vgrid()
+    psi = np.random.default_rng(4).standard_normal((pa.N, 5))
+    ref64, ref32 = pa.hpsi(psi), pa.hpsi(psi, prec="fp32")
+    assert rel(pb.hpsi(psi), ref64) > 1e-3  # the zero-potential problem differs before the update
+    pb.set_vgrid(v)
+    assert np.abs(pb.vgrid() - v).max() <= 1e-15 * np.abs(v).max()
+    assert rel(pb.hpsi(psi), ref64) <= FP64_TOL
+    assert rel(pb.hpsi(psi, prec="fp32"), ref32) <= FP32_TOL
+    pc = E.Problem(with_v_scaled(spec, 0.0))
+    pc.set_vgrid(terms_to_ref(v, pc, spec), layout="ref")
+    assert rel(pc.hpsi(psi), ref64) <= FP64_TOL
+
+
+def test_set_vgrid_direct_product_stage_kernels():
+    spec = S.config_dp3(nb=8, nq=10)
+    pg = E.Problem(spec)
+    pg.set_vgrid(2.0 * pg.vgrid())
+    po = O.OracleProblem(with_v_scaled(spec, 2.0))
+    psi = np.random.default_rng(5).standard_normal((pg.N, 4))
+    assert rel(pg.hpsi(psi), po.hpsi(psi)) <= FP64_TOL

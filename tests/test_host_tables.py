@@ -69,3 +69,17 @@ def test_device_calls_fail_loudly_on_host_only_context():
     with pytest.raises(E.EvrError) as ei:
         pg.hpsi(np.ones(pg.N))
     assert ei.value.code == E.EVR_EDEVICE
+
+
+def test_set_vgrid_argument_checks():
+    pg = E.Problem(S.henon_heiles(3, 2), device=-1)
+    v = np.zeros(pg.sum_nq)
+    with pytest.raises(E.EvrError) as ei:  # the table lives on the device
+        pg.set_vgrid(v)
+    assert ei.value.code == E.EVR_EDEVICE
+    L = E.load()
+    assert L.evr_set_vgrid(pg.h, v.ctypes.data_as(E._dp), 7) == E.EVR_EINVAL
+    assert L.evr_set_vgrid(pg.h, None, 0) == E.EVR_EINVAL
+    with pytest.raises(E.EvrError) as ei:
+        pg.set_vgrid(v[:-1])
+    assert ei.value.code == E.EVR_EINVAL
