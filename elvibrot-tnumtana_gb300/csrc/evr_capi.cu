@@ -15,6 +15,30 @@ using namespace evr;
     if (_rc != EVR_OK) return _rc;                      \
   } while (0)
 
+namespace evr {
+
+void grid_values_to_device(const HostProblem& P, const double* v, int layout, bool with_shift,
+                           std::vector<double>& dev, std::vector<float>& dev32) {
+  const int nb2 = P.nb0 * P.nb0;
+  const size_t n = (size_t)P.sum_nq * nb2;
+  dev.assign(n, 0.0);
+  dev32.assign(n, 0.0f);
+  for (const TermDesc& T : P.terms)
+    for (int ab = 0; ab < nb2; ++ab) {
+      const double shift = with_shift && ab % (P.nb0 + 1) == 0 ? T.vshift : 0.0;
+      for (int64_t qp = 0; qp < T.NQ; ++qp) {
+        const int64_t q = P.grid_perm[(size_t)T.off_nq + qp] - T.off_nq;
+        const size_t src = layout == EVR_VGRID_TERMS ? (size_t)T.off_nq * nb2 + (size_t)ab * T.NQ + q
+                                                     : (size_t)(T.off_nq + q) + (size_t)P.sum_nq * ab;
+        const size_t dst = (size_t)T.off_nq * nb2 + (size_t)ab * T.NQ + qp;
+        dev[dst] = v[src] + shift;
+        dev32[dst] = (float)dev[dst];
+      }
+    }
+}
+
+}  // namespace evr
+
 extern "C" {
 
 int evr_create(evr_ctx** out, const evr_problem_desc* desc, int device) {
@@ -143,23 +167,10 @@ int evr_set_vgrid(evr_ctx* c, const double* v, int layout) {
   if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
   if (c->batch) return set_error(c, EVR_EINVAL, "evr_set_vgrid: not for batched contexts");
   EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
-  const HostProblem& P = c->hp;
-  const int nb2 = P.nb0 * P.nb0;
-  const size_t n = (size_t)P.sum_nq * nb2;
-  std::vector<double> dev(n);
-  std::vector<float> dev32(n);
-  for (const TermDesc& T : P.terms)
-    for (int ab = 0; ab < nb2; ++ab) {
-      const double shift = ab % (P.nb0 + 1) == 0 ? T.vshift : 0.0;
-      for (int64_t qp = 0; qp < T.NQ; ++qp) {
-        const int64_t q = P.grid_perm[(size_t)T.off_nq + qp] - T.off_nq;
-        const size_t src = layout == EVR_VGRID_TERMS ? (size_t)T.off_nq * nb2 + (size_t)ab * T.NQ + q
-                                                     : (size_t)(T.off_nq + q) + (size_t)P.sum_nq * ab;
-        const size_t dst = (size_t)T.off_nq * nb2 + (size_t)ab * T.NQ + qp;
-        dev[dst] = v[src] + shift;
-        dev32[dst] = (float)dev[dst];
-      }
-    }
+  std::vector<double> dev;
+  std::vector<float> dev32;
+  grid_values_to_device(c->hp, v, layout, true, dev, dev32);
+  const size_t n = dev.size();
   // an H.psi still reading the old table may run on a caller's stream: wait for the device
   EVR_CU(cudaDeviceSynchronize(), "sync before vgrid update");
   EVR_CU(cudaMemcpyAsync(c->dp.vgrid, dev.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream),

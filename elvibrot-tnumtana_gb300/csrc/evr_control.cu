@@ -392,6 +392,45 @@ int evr_set_dipole(evr_ctx* c, int n_mono, const double* coef, const int* idx, c
   return rc;
 }
 
+int evr_set_dipole_grid(evr_ctx* c, const double* mu, int layout) {
+  if (!c) return EVR_EINVAL;
+  if (!mu || (layout != EVR_VGRID_TERMS && layout != EVR_VGRID_REF))
+    return set_error(c, EVR_EINVAL, "evr_set_dipole_grid: null values or unknown layout");
+  if (c->batch) return set_error(c, EVR_EINVAL, "evr_set_dipole_grid: not for batched contexts");
+  if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
+  int rc = cuda_check(c, cudaSetDevice(c->device), "cudaSetDevice");
+  if (rc) return rc;
+  const HostProblem& P = c->hp;
+  std::vector<double> dev;
+  std::vector<float> dev32;
+  grid_values_to_device(P, mu, layout, false, dev, dev32);
+  const size_t n = dev.size();
+  // largest row-sum norm sum_b |mu_ab(q)| over the grid points, as evr_set_dipole computes it
+  const int nb0 = P.nb0;
+  double mmax = 0.0;
+  for (const TermDesc& T : P.terms)
+    for (int64_t q = 0; q < T.NQ; ++q)
+      for (int a = 0; a < nb0; ++a) {
+        double r = 0.0;
+        for (int b = 0; b < nb0; ++b) r += std::fabs(dev[(size_t)T.off_nq * nb0 * nb0 + (size_t)(a + nb0 * b) * T.NQ + q]);
+        mmax = std::max(mmax, r);
+      }
+  if ((rc = cuda_check(c, cudaDeviceSynchronize(), "sync before dipole update"))) return rc;
+  if (!c->dp_mugrid) {
+    if ((rc = cuda_check(c, cudaMalloc((void**)&c->dp_mugrid, n * sizeof(double)), "cudaMalloc dipole"))) return rc;
+    if ((rc = cuda_check(c, cudaMalloc((void**)&c->dp_mugrid32, n * sizeof(float)), "cudaMalloc dipole"))) return rc;
+  }
+  cudaStream_t s = c->stream;
+  if ((rc = cuda_check(c, cudaMemcpyAsync(c->dp_mugrid, dev.data(), n * sizeof(double), cudaMemcpyHostToDevice, s),
+                       "copy dipole")) ||
+      (rc = cuda_check(c, cudaMemcpyAsync(c->dp_mugrid32, dev32.data(), n * sizeof(float), cudaMemcpyHostToDevice, s),
+                       "copy dipole")) ||
+      (rc = cuda_check(c, cudaStreamSynchronize(s), "evr_set_dipole_grid")))
+    return rc;
+  c->mu_max = mmax;
+  return EVR_OK;
+}
+
 int evr_set_field(evr_ctx* c, double vw, double mw, int keo) {
   if (!c) return EVR_EINVAL;
   if ((mw != 0.0 || vw != 1.0) && !c->dp_mugrid && !c->host_only)

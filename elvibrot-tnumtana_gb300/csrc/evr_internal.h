@@ -259,6 +259,12 @@ int transpose_to_interleaved(const double* in, int64_t ld_in, double* out, int64
 int transpose_from_interleaved(const double* in, int64_t ld_in, double* out, int64_t ld_out, int64_t N, int nvec,
                                cudaStream_t s);
 int set_error(evr_ctx* c, int code, const std::string& msg);
+// Grid values given in the reference's point order (layout EVR_VGRID_TERMS: term-major with
+// (a,b) blocks per term; EVR_VGRID_REF: (iq, a, b) over the whole grid) -> the device's
+// table order, FP64 and FP32; with_shift adds each term's constant of dropped 1-point
+// modes on the diagonal (the V table holds it, the dipole table does not).
+void grid_values_to_device(const HostProblem& P, const double* v, int layout, bool with_shift,
+                           std::vector<double>& dev, std::vector<float>& dev32);
 // reads (and clears) the flag the term kernels raise when an item would exceed its buffers
 int check_item_bounds(evr_ctx* c);
 void clear_item_sets(evr_ctx* c);

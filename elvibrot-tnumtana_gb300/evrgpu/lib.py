@@ -64,7 +64,7 @@ EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_
            "evr_davidson",
            "evr_cheby_propagate", "evr_fma_peak", "evr_hpsi_noalloc", "evr_set_dipole", "evr_set_field",
            "evr_oc_forward", "evr_oc_backward", "evr_create_batch", "evr_batch_offsets", "evr_batch_davidson", "evr_autotune",
-           "evr_psi_write", "evr_psi_read", "evr_set_vgrid"]
+           "evr_psi_write", "evr_psi_read", "evr_set_vgrid", "evr_set_dipole_grid"]
 VGRID_LAYOUT = {"terms": 0, "ref": 1}
 WP_FORMAT = {"v0": 0, "v1": 1, "unformatted": 2, "sparse": 3}
 
@@ -95,6 +95,7 @@ def load(build: bool = True):
     L.evr_get_basis.argtypes = [vp, C.c_int, C.c_int, _ip] + [_dp] * 8
     L.evr_get_vgrid.argtypes = [vp, _dp]
     L.evr_set_vgrid.argtypes = [vp, _dp, C.c_int]
+    L.evr_set_dipole_grid.argtypes = [vp, _dp, C.c_int]
     L.evr_hpsi_host.argtypes = [vp, _dp, C.c_int64, _dp, C.c_int64, C.c_int, C.c_int, C.c_int]
     L.evr_hpsi_device.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.c_int, C.c_int, C.c_int, vp]
     L.evr_last_launch_count.argtypes = [vp, _lp, _lp]
@@ -356,6 +357,13 @@ class Problem:
         idx = _iarr(np.asarray(idx).reshape(-1, 4))
         elec = _iarr(np.zeros((len(coef), 2)) if elec is None else np.asarray(elec).reshape(-1, 2))
         self._check(load().evr_set_dipole(self.h, len(coef), _p(coef, _dp), _p(idx, _ip), _p(elec, _ip)))
+
+    def set_dipole_grid(self, mu, layout="terms"):
+        """Dipole mu(Q) as grid values (layouts of set_vgrid) instead of monomials."""
+        mu = _darr(np.asarray(mu, dtype=np.float64).ravel(order="F"))
+        if mu.size != self.sum_nq * self.spec.nb0 ** 2:
+            raise EvrError(EVR_EINVAL, f"dipole grid has {mu.size} values, expected {self.sum_nq * self.spec.nb0 ** 2}")
+        self._check(load().evr_set_dipole_grid(self.h, _p(mu, _dp), VGRID_LAYOUT[layout]))
 
     def set_field(self, vw=1.0, mw=0.0, keo=True):
         """Grid operator vw*V + mw*mu (+ kinetic part) of later H.psi / Davidson / Chebyshev calls."""

@@ -243,6 +243,12 @@ int evr_fma_peak(int device, int prec, double *tflops);
  * (sub_module_propa_march.f90:1494-1503) with a static field.
  */
 int evr_set_dipole(evr_ctx *ctx, int n_mono, const double *coef, const int *idx, const int *elec);
+/* The dipole as grid values instead of monomials: the grid of the scalar operator the
+ * reference's plugin fills for the dipole (calcN_op, Source_PrimOperator/sub_PrimOp.f90:
+ * 283-655), in either layout of evr_set_vgrid.  Replaces what evr_set_dipole evaluated, and
+ * the bound max_q sum_b |mu_ab(q)| that widens the control propagator's spectral range.
+ * Synchronous; a set-up call. */
+int evr_set_dipole_grid(evr_ctx *ctx, const double *mu, int layout);
 int evr_set_field(evr_ctx *ctx, double vw, double mw, int keo);
 
 /*

@@ -69,3 +69,34 @@ def test_set_vgrid_direct_product_stage_kernels():
     po = O.OracleProblem(with_v_scaled(spec, 2.0))
     psi = np.random.default_rng(5).standard_normal((pg.N, 4))
     assert rel(pg.hpsi(psi), po.hpsi(psi)) <= FP64_TOL
+
+
+def test_set_dipole_grid_matches_monomial_dipole():
+    """evr_set_dipole_grid against evr_set_dipole on the same mu: the field operators
+    H0 - E mu and mu alone, and the control propagation (whose spectral range the dipole
+    bound widens)."""
+    from oracle import control as OC
+    sp = S.config_oc(seed=1, nb=6, nq=8, D=3)
+    pa = E.Problem(sp)  # dipole from its monomials
+    no_dip = dict(dip_coef=None, dip_idx=None, dip_elec=None)
+    mu = E.Problem(dataclasses.replace(sp, mono_coef=sp.dip_coef, mono_idx=sp.dip_idx, mono_elec=sp.dip_elec,
+                                       **no_dip)).vgrid()  # mu on the grid, as a potential
+    pb = E.Problem(dataclasses.replace(sp, **no_dip))
+    pb.set_dipole_grid(mu)
+    psi = np.random.default_rng(6).standard_normal((pa.N, 3))
+    for vw, mw, keo in ((1.0, -0.02, True), (0.0, 1.0, False)):
+        pa.set_field(vw, mw, keo)
+        pb.set_field(vw, mw, keo)
+        assert rel(pb.hpsi(psi), pa.hpsi(psi)) <= FP64_TOL
+    pa.set_field(1.0, 0.0, True)
+    pb.set_field(1.0, 0.0, True)
+    H0, _ = OC.operators(O.OracleProblem(sp))
+    w = np.sort(np.linalg.eigvals(H0).real)
+    psi0 = np.zeros(pa.N, dtype=complex)
+    psi0[0] = 1.0
+    target = np.zeros(pa.N, dtype=complex)
+    target[3] = 1.0
+    field = S.oc_field(20, 10.0, seed=3, amp=0.01)
+    Ja = pa.oc_forward(field, psi0, target, 10.0, w[0] - 1e-3, w[-1] + 1e-3)[0]
+    Jb = pb.oc_forward(field, psi0, target, 10.0, w[0] - 1e-3, w[-1] + 1e-3)[0]
+    assert abs(Ja - Jb) <= 1e-12

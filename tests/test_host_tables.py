@@ -83,3 +83,7 @@ def test_set_vgrid_argument_checks():
     with pytest.raises(E.EvrError) as ei:
         pg.set_vgrid(v[:-1])
     assert ei.value.code == E.EVR_EINVAL
+    with pytest.raises(E.EvrError) as ei:
+        pg.set_dipole_grid(v)
+    assert ei.value.code == E.EVR_EDEVICE
+    assert L.evr_set_dipole_grid(pg.h, v.ctypes.data_as(E._dp), -1) == E.EVR_EINVAL
