@@ -318,3 +318,260 @@ extern "C" int evr_cheby_propagate(evr_ctx* c, const double* psi0, int npsi, dou
                                          " (spectrum outside [emin, emax]?)");
   return EVR_OK;
 }
+
+// ---------------------------------------------------------------------------------------
+// Short-iterative-Lanczos propagation (march_SIL, sub_module_propa_march.f90:2899-3100).
+// Per time step and packet: q_1 = psi/|psi|, E0 = <q_1|H q_1>; Lanczos on H - E0 with
+// alpha_k = Re<q_k|w>, w = (H - E0) q_k - beta_{k-1} q_{k-1}; after each alpha the
+// propagator column u = exp(-i T_k dt) e_1 of the Lanczos matrix T_k (UPsi_spec :3101) is
+// formed on the host, and the space stops growing when |u_k| < poly_tol (or at npoly);
+// psi(t+dt) = |psi| exp(-i E0 dt) sum_k u_k q_k.  The packets of a call share the H.psi
+// launches (one interleaved block of 2*npsi columns); their Lanczos scalars are separate,
+// and a packet whose space is complete only idles until the last one is.  The scalars
+// come to the host after every H.psi (one small copy), so a step is not a fixed launch
+// sequence and is not captured as a graph.
+#include "evr_krylov.h"
+
+namespace {
+
+constexpr int kMaxPackets = evr::kMaxBlock / 2;
+
+struct PacketCoef {
+  double x[kMaxPackets];
+  double y[kMaxPackets];
+  double z[kMaxPackets];
+};
+
+// w -= x_p q + y_p qprev (qprev may be null); element i of the block is packet i % npsi
+__global__ void sil_residual(const double* __restrict__ q, const double* __restrict__ qprev, double* __restrict__ w,
+                             PacketCoef cf, int npsi, int64_t n2) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += (int64_t)gridDim.x * blockDim.x) {
+    const int p = (int)(i % npsi);
+    const int64_t e = 2 * i;
+    double wr = w[e] - cf.x[p] * q[e], wi = w[e + 1] - cf.x[p] * q[e + 1];
+    if (qprev) {
+      wr -= cf.y[p] * qprev[e];
+      wi -= cf.y[p] * qprev[e + 1];
+    }
+    w[e] = wr;
+    w[e + 1] = wi;
+  }
+}
+
+// out = x_p * in
+__global__ void sil_scale(const double* __restrict__ in, double* __restrict__ out, PacketCoef cf, int npsi, int64_t n2) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += (int64_t)gridDim.x * blockDim.x) {
+    const int p = (int)(i % npsi);
+    out[2 * i] = cf.x[p] * in[2 * i];
+    out[2 * i + 1] = cf.x[p] * in[2 * i + 1];
+  }
+}
+
+// acc (= when first, else +=) (x_p + i y_p) q
+__global__ void sil_accumulate(const double* __restrict__ q, double* __restrict__ acc, PacketCoef cf, int npsi,
+                               int64_t n2, int first) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += (int64_t)gridDim.x * blockDim.x) {
+    const int p = (int)(i % npsi);
+    const int64_t e = 2 * i;
+    const double a = q[e], b = q[e + 1];
+    const double r = cf.x[p] * a - cf.y[p] * b, m = cf.x[p] * b + cf.y[p] * a;
+    acc[e] = first ? r : acc[e] + r;
+    acc[e + 1] = first ? m : acc[e + 1] + m;
+  }
+}
+
+struct DevVecs {
+  std::vector<double*> v;
+  ~DevVecs() {
+    for (double* p : v)
+      if (p) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+extern "C" int evr_sil_propagate(evr_ctx* c, const double* psi0, int npsi, double dt, int nsteps, int npoly,
+                                 double poly_tol, int prec, double* autocorr, double* psi_out, int64_t* info) {
+  if (!c) return EVR_EINVAL;
+  if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
+  if (c->batch) return set_error(c, EVR_EINVAL, "evr_sil_propagate: not for batched contexts");
+  if (!psi0 || npsi < 1 || npsi > kMaxPackets || nsteps < 0 || npoly < 1 || npoly > 256 || !(poly_tol > 0.0) ||
+      !(dt > 0.0))
+    return set_error(c, EVR_EINVAL, "evr_sil_propagate: bad arguments (1 <= npsi <= 32, 1 <= npoly <= 256, dt > 0, "
+                                    "poly_tol > 0)");
+  if (prec != EVR_PREC_FP64 && prec != EVR_PREC_FP32) return set_error(c, EVR_EINVAL, "unknown precision");
+  if (cudaSetDevice(c->device) != cudaSuccess) return set_error(c, EVR_EDEVICE, "cudaSetDevice");
+  const int64_t N = c->hp.Np * c->hp.nb0;
+  const int ncol = 2 * npsi;
+  const size_t ne = (size_t)N * ncol;
+  const int64_t n2 = N * npsi;
+  cudaStream_t s = c->stream;
+  DevBuf d0, dpsi, dw, dred, dac;
+  if (d0.alloc(ne) || dpsi.alloc(ne) || dw.alloc(ne) || dred.alloc((size_t)3 * npsi) ||
+      dac.alloc((size_t)3 * npsi * (nsteps + 1)))
+    return set_error(c, EVR_ENOMEM, "evr_sil_propagate: device allocation");
+  {
+    std::vector<double> h(ne);
+    for (int p = 0; p < npsi; ++p)
+      for (int64_t k = 0; k < N; ++k) {
+        h[k * ncol + 2 * p] = psi0[((size_t)p * N + k) * 2];
+        h[k * ncol + 2 * p + 1] = psi0[((size_t)p * N + k) * 2 + 1];
+      }
+    if (cudaMemcpyAsync(d0.p, h.data(), sizeof(double) * ne, cudaMemcpyHostToDevice, s) ||
+        cudaMemcpyAsync(dpsi.p, d0.p, sizeof(double) * ne, cudaMemcpyDeviceToDevice, s) ||
+        cudaMemsetAsync(dac.p, 0, sizeof(double) * 3 * npsi * (nsteps + 1), s) || cudaStreamSynchronize(s))
+      return set_error(c, EVR_EDEVICE, "evr_sil_propagate: upload");
+  }
+  int rc = ensure_workspace(c, ncol, prec);
+  if (rc) return rc;
+  const int gb = c->num_sms * 4;
+  dim3 og((unsigned)std::min<int64_t>((N + 255) / 256, 1024), (unsigned)npsi);
+  // <a|b> per packet -> host (re, im, |b|^2)
+  std::vector<double> red((size_t)3 * npsi);
+  auto overlap = [&](const double* a, const double* b, double* out_dev) -> int {
+    double* o = out_dev ? out_dev : dred.p;
+    if (!out_dev && cudaMemsetAsync(dred.p, 0, sizeof(double) * 3 * npsi, s) != cudaSuccess) return EVR_EDEVICE;
+    cheby_overlap<<<og, 256, 0, s>>>(a, b, N, npsi, o);
+    if (out_dev) return cudaGetLastError() == cudaSuccess ? EVR_OK : EVR_EDEVICE;
+    if (cudaMemcpyAsync(red.data(), dred.p, sizeof(double) * 3 * npsi, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return EVR_EDEVICE;
+    return EVR_OK;
+  };
+  if ((rc = overlap(d0.p, dpsi.p, dac.p))) return set_error(c, rc, "evr_sil_propagate: overlap");
+  DevVecs Q;  // Krylov vectors, allocated as the space grows, kept across steps
+  auto krylov = [&](int k) -> double* {
+    while ((int)Q.v.size() <= k) {
+      double* p = nullptr;
+      if (cudaMalloc((void**)&p, sizeof(double) * ne) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+      }
+      Q.v.push_back(p);
+    }
+    return Q.v[k];
+  };
+  const int op = c->op_form;
+  int64_t n_hpsi = 0;
+  int max_dim = 0;
+  std::vector<double> nrm(npsi), E0(npsi), ure, uim;
+  std::vector<std::vector<double>> alpha(npsi), beta(npsi), u_re(npsi), u_im(npsi);
+  std::vector<int> dim(npsi);
+  for (int st = 1; st <= nsteps; ++st) {
+    PacketCoef cf{};
+    if ((rc = overlap(dpsi.p, dpsi.p, nullptr))) return set_error(c, rc, "evr_sil_propagate: norm");
+    for (int p = 0; p < npsi; ++p) {
+      nrm[p] = std::sqrt(red[3 * p + 2]);
+      cf.x[p] = nrm[p] > 0.0 ? 1.0 / nrm[p] : 0.0;
+      alpha[p].clear();
+      beta[p].clear();
+      dim[p] = 0;
+    }
+    double* q0 = krylov(0);
+    if (!q0) return set_error(c, EVR_ENOMEM, "evr_sil_propagate: Krylov vectors");
+    sil_scale<<<gb, 256, 0, s>>>(dpsi.p, q0, cf, npsi, n2);
+    int active = npsi;
+    for (int k = 0; k < npoly && active > 0; ++k) {
+      double* qk = Q.v[k];
+      if ((rc = hpsi_interleaved(c, qk, ncol, dw.p, ncol, ncol, prec, s, op)))
+        return set_error(c, rc, "evr_sil_propagate: H.psi");
+      ++n_hpsi;
+      if (k == 0) {
+        if ((rc = overlap(qk, dw.p, nullptr))) return set_error(c, rc, "evr_sil_propagate: E0");
+        for (int p = 0; p < npsi; ++p) E0[p] = red[3 * p];
+      }
+      PacketCoef r{};
+      for (int p = 0; p < npsi; ++p) {  // a complete packet's columns are zero from here on
+        r.x[p] = E0[p];
+        r.y[p] = (k > 0 && (size_t)k <= beta[p].size()) ? beta[p][k - 1] : 0.0;
+      }
+      sil_residual<<<gb, 256, 0, s>>>(qk, k > 0 ? Q.v[k - 1] : nullptr, dw.p, r, npsi, n2);
+      if ((rc = overlap(qk, dw.p, nullptr))) return set_error(c, rc, "evr_sil_propagate: alpha");
+      PacketCoef a{}, sc{};
+      for (int p = 0; p < npsi; ++p) {
+        if (dim[p]) continue;  // complete: the packet idles
+        alpha[p].push_back(red[3 * p]);
+        const int n = k + 1;
+        u_re[p].assign(n, 0.0);
+        u_im[p].assign(n, 0.0);
+        if (!krylov_propagator_column(n, alpha[p].data(), beta[p].data(), dt, u_re[p].data(), u_im[p].data()))
+          return set_error(c, EVR_ENOCONV, "evr_sil_propagate: Lanczos matrix eigen-decomposition");
+        if (std::hypot(u_re[p][k], u_im[p][k]) < poly_tol || k == npoly - 1 || nrm[p] == 0.0) {
+          dim[p] = n;
+          --active;
+        }
+        a.x[p] = alpha[p][k];
+      }
+      if (active == 0) break;
+      sil_residual<<<gb, 256, 0, s>>>(qk, nullptr, dw.p, a, npsi, n2);
+      if ((rc = overlap(dw.p, dw.p, nullptr))) return set_error(c, rc, "evr_sil_propagate: beta");
+      double* qn = krylov(k + 1);
+      if (!qn) return set_error(c, EVR_ENOMEM, "evr_sil_propagate: Krylov vectors");
+      for (int p = 0; p < npsi; ++p) {
+        if (dim[p]) continue;
+        const double b = std::sqrt(red[3 * p + 2]);
+        double tmax = std::fabs(E0[p]);
+        for (double x : alpha[p]) tmax = std::max(tmax, std::fabs(x));
+        for (double x : beta[p]) tmax = std::max(tmax, x);
+        if (!(b > 1e-13 * std::max(tmax, 1e-300))) {  // invariant subspace: the space is complete
+          dim[p] = k + 1;
+          --active;
+          continue;
+        }
+        beta[p].push_back(b);
+        sc.x[p] = 1.0 / b;
+      }
+      sil_scale<<<gb, 256, 0, s>>>(dw.p, qn, sc, npsi, n2);
+    }
+    // psi = |psi| exp(-i E0 dt) sum_k u_k q_k
+    int kmax = 0;
+    for (int p = 0; p < npsi; ++p) kmax = std::max(kmax, dim[p]);
+    max_dim = std::max(max_dim, kmax);
+    for (int k = 0; k < kmax; ++k) {
+      PacketCoef u{};
+      for (int p = 0; p < npsi; ++p) {
+        if (k >= dim[p]) continue;
+        const double cs = std::cos(E0[p] * dt), sn = -std::sin(E0[p] * dt);
+        u.x[p] = nrm[p] * (cs * u_re[p][k] - sn * u_im[p][k]);
+        u.y[p] = nrm[p] * (cs * u_im[p][k] + sn * u_re[p][k]);
+      }
+      sil_accumulate<<<gb, 256, 0, s>>>(Q.v[k], dpsi.p, u, npsi, n2, k == 0);
+    }
+    if ((rc = overlap(d0.p, dpsi.p, dac.p + (size_t)3 * npsi * st))) return set_error(c, rc, "evr_sil_propagate: overlap");
+  }
+  std::vector<double> ac((size_t)3 * npsi * (nsteps + 1));
+  if (cudaMemcpyAsync(ac.data(), dac.p, sizeof(double) * ac.size(), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return set_error(c, EVR_EDEVICE, "evr_sil_propagate: results");
+  int bad_step = -1;
+  const double ntol = prec == EVR_PREC_FP32 ? 1e-3 : 1e-6;
+  for (int st = 0; st <= nsteps && bad_step < 0; ++st)
+    for (int p = 0; p < npsi; ++p) {
+      const double n0 = ac[3 * p + 2], nn = ac[(size_t)3 * npsi * st + 3 * p + 2];
+      if (!(std::fabs(nn - n0) <= ntol * n0 + 1e-300)) { bad_step = st; break; }
+    }
+  if (autocorr)
+    for (int st = 0; st <= nsteps; ++st)
+      for (int p = 0; p < npsi; ++p) {
+        autocorr[((size_t)st * npsi + p) * 2] = ac[(size_t)3 * npsi * st + 3 * p];
+        autocorr[((size_t)st * npsi + p) * 2 + 1] = ac[(size_t)3 * npsi * st + 3 * p + 1];
+      }
+  if (psi_out) {
+    std::vector<double> h(ne);
+    if (cudaMemcpy(h.data(), dpsi.p, sizeof(double) * ne, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return set_error(c, EVR_EDEVICE, "evr_sil_propagate: copy psi");
+    for (int p = 0; p < npsi; ++p)
+      for (int64_t k = 0; k < N; ++k) {
+        psi_out[((size_t)p * N + k) * 2] = h[k * ncol + 2 * p];
+        psi_out[((size_t)p * N + k) * 2 + 1] = h[k * ncol + 2 * p + 1];
+      }
+  }
+  if (info) {
+    info[0] = max_dim;
+    info[1] = n_hpsi * ncol;
+    info[2] = bad_step;
+  }
+  if (bad_step >= 0)
+    return set_error(c, EVR_ENOCONV, "evr_sil_propagate: norm not conserved from step " + std::to_string(bad_step));
+  return EVR_OK;
+}

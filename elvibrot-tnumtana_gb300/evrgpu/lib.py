@@ -64,7 +64,8 @@ EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_
            "evr_davidson",
            "evr_cheby_propagate", "evr_fma_peak", "evr_hpsi_noalloc", "evr_set_dipole", "evr_set_field",
            "evr_oc_forward", "evr_oc_backward", "evr_create_batch", "evr_batch_offsets", "evr_batch_davidson", "evr_autotune",
-           "evr_psi_write", "evr_psi_read", "evr_set_vgrid", "evr_set_dipole_grid"]
+           "evr_psi_write", "evr_psi_read", "evr_set_vgrid", "evr_set_dipole_grid",
+           "evr_sil_propagate"]
 VGRID_LAYOUT = {"terms": 0, "ref": 1}
 WP_FORMAT = {"v0": 0, "v1": 1, "unformatted": 2, "sparse": 3}
 
@@ -119,6 +120,8 @@ def load(build: bool = True):
     if hasattr(L, "evr_cheby_propagate"):
         L.evr_cheby_propagate.argtypes = [vp, _dp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double,
                                           C.c_double, C.c_int, _dp, _dp, _lp]
+    L.evr_sil_propagate.argtypes = [vp, _dp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp,
+                                    _lp]
     _lib = L
     return L
 
@@ -414,6 +417,23 @@ class Problem:
     def set_operator(self, form):
         """'H' (the reference's OpPsi), 'HT' (its transpose) or 'HSYM' ((H+H^T)/2)."""
         self._check(load().evr_set_operator(self.h, {"H": 0, "HT": 1, "HSYM": 2}[form]))
+
+    def sil(self, psi0, dt, nsteps, npoly=64, poly_tol=1e-10, prec="fp64", want_psi=False):
+        """Short-iterative-Lanczos propagation (march_SIL) of complex packets psi0 (N x npsi);
+        returns (autocorr (nsteps+1) x npsi, final packets or None, info)."""
+        psi0 = np.asarray(psi0, dtype=np.complex128)
+        if psi0.ndim == 1:
+            psi0 = psi0[:, None]
+        N, npsi = psi0.shape
+        buf = np.ascontiguousarray(psi0.T).view(np.float64)
+        ac = np.zeros((nsteps + 1) * npsi * 2)
+        out = np.zeros(npsi * 2 * N) if want_psi else None
+        info = np.zeros(3, dtype=np.int64)
+        self._check(load().evr_sil_propagate(self.h, _p(buf, _dp), npsi, dt, nsteps, npoly, poly_tol, PREC[prec],
+                                             _p(ac, _dp), _p(out, _dp), _p(info, _lp)))
+        autocorr = ac.view(np.complex128).reshape(nsteps + 1, npsi)
+        psi = out.view(np.complex128).reshape(npsi, N).T.copy() if want_psi else None
+        return autocorr, psi, dict(krylov_dim=int(info[0]), hpsi=int(info[1]), status=int(info[2]))
 
     def chebyshev(self, psi0, dt, nsteps, emin, emax, poly_tol=1e-10, prec="fp64", want_psi=False):
         """Chebyshev propagation of complex packets psi0 (N x npsi, complex128)."""

@@ -225,6 +225,19 @@ int evr_cheby_propagate(evr_ctx *ctx, const double *psi0, int npsi, double dt, i
                         double emax, double poly_tol, int prec, double *autocorr, double *psi_out,
                         int64_t *info);
 
+/*
+ * Short-iterative-Lanczos propagation of complex wave packets.
+ * Replaces march_SIL (Source_ElVibRot/sub_propagation/sub_module_propa_march.f90:2899-3100)
+ * with UPsi_spec (:3101-3160): per step and packet, q_1 = psi/|psi|, E0 = <q_1|H q_1>, a
+ * Lanczos space of H - E0 grown until the last component of u = exp(-i T_k dt) e_1 falls
+ * below poly_tol (or k = npoly), psi(t+dt) = |psi| exp(-i E0 dt) sum_k u_k q_k.  The
+ * operator is the context's form (evr_set_operator): Lanczos assumes a symmetric H, so for
+ * a type-10 operator with some nq > nb use EVR_OP_HSYM.  Arguments and outputs as
+ * evr_cheby_propagate (no spectral bounds needed); npsi <= 32, npoly <= 256.
+ * info: [largest Krylov dimension used, total H.psi count, status]. */
+int evr_sil_propagate(evr_ctx *ctx, const double *psi0, int npsi, double dt, int nsteps, int npoly,
+                      double poly_tol, int prec, double *autocorr, double *psi_out, int64_t *info);
+
 /* FMA issue-rate micro-benchmark of the device (independent FMA chains, no memory
  * traffic): the peak of the CUDA-core pipe the contractions run on, in TFLOP/s.
  * Utility for roofline reporting; no counterpart in the reference. */

@@ -87,3 +87,10 @@ def test_set_vgrid_argument_checks():
         pg.set_dipole_grid(v)
     assert ei.value.code == E.EVR_EDEVICE
     assert L.evr_set_dipole_grid(pg.h, v.ctypes.data_as(E._dp), -1) == E.EVR_EINVAL
+
+
+def test_sil_needs_a_device():
+    pg = E.Problem(S.henon_heiles(3, 2), device=-1)
+    with pytest.raises(E.EvrError) as ei:
+        pg.sil(np.ones(pg.N, dtype=complex), 1.0, 1)
+    assert ei.value.code == E.EVR_EDEVICE
