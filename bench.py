@@ -318,6 +318,15 @@ def run_suite(args):
                 out[prec] = {"steps": args.prop_steps, "s": dt, "s_per_step": dt / args.prop_steps,
                              "order": st["max_order"], "autocorr_last": [float(ac[-1, 0].real), float(ac[-1, 0].imag)]}
                 out[prec]["s_2000_steps_extrapolated"] = 2000 * dt / args.prop_steps
+            # the same steps by short-iterative Lanczos (march_SIL; nq = nb, H symmetric)
+            p.sil(psi0, 10.0, 2, npoly=64, poly_tol=1e-10)
+            t0 = time.perf_counter()
+            ac_sil, _, st = p.sil(psi0, 10.0, args.prop_steps, npoly=64, poly_tol=1e-10)
+            dt = time.perf_counter() - t0
+            out["sil_fp64"] = {"steps": args.prop_steps, "s": dt, "s_per_step": dt / args.prop_steps,
+                               "krylov_dim": st["krylov_dim"], "hpsi": st["hpsi"],
+                               "autocorr_last": [float(ac_sil[-1, 0].real), float(ac_sil[-1, 0].imag)],
+                               "max_abs_diff_vs_chebyshev": float(np.abs(ac_sil[:, 0] - ac[:, 0]).max())}
         elif w == "control":
             # D=3 nb=20 nq=24 with the dipole; ground state -> level 5, 4000 steps of 5 au
             sp = S.config_oc(seed=0)
