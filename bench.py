@@ -310,11 +310,13 @@ def run_suite(args):
             out.update({"emin": emin, "emax": emax})
             if args.autotune:
                 out["autotune"] = p.autotune(nvec=2, prec="fp64")
+            ac_cheb = {}
             for prec in ("fp64", "fp32"):
                 p.chebyshev(psi0, 10.0, 2, emin, emax, prec=prec)
                 t0 = time.perf_counter()
                 ac, _, st = p.chebyshev(psi0, 10.0, args.prop_steps, emin, emax, prec=prec)
                 dt = time.perf_counter() - t0
+                ac_cheb[prec] = ac
                 out[prec] = {"steps": args.prop_steps, "s": dt, "s_per_step": dt / args.prop_steps,
                              "order": st["max_order"], "autocorr_last": [float(ac[-1, 0].real), float(ac[-1, 0].imag)]}
                 out[prec]["s_2000_steps_extrapolated"] = 2000 * dt / args.prop_steps
@@ -326,7 +328,7 @@ def run_suite(args):
             out["sil_fp64"] = {"steps": args.prop_steps, "s": dt, "s_per_step": dt / args.prop_steps,
                                "krylov_dim": st["krylov_dim"], "hpsi": st["hpsi"],
                                "autocorr_last": [float(ac_sil[-1, 0].real), float(ac_sil[-1, 0].imag)],
-                               "max_abs_diff_vs_chebyshev": float(np.abs(ac_sil[:, 0] - ac[:, 0]).max())}
+                               "max_abs_diff_vs_chebyshev": float(np.abs(ac_sil[:, 0] - ac_cheb["fp64"][:, 0]).max())}
         elif w == "control":
             # D=3 nb=20 nq=24 with the dipole; ground state -> level 5, 4000 steps of 5 au
             sp = S.config_oc(seed=0)
