@@ -60,3 +60,26 @@ def test_hbm_roofline(tmp_path):
     assert r["peak_source"].startswith("measured")
     r = bench.hbm_roofline(3.0e9, 0.5, str(tmp_path / "absent.json"))
     assert r["peak"] == 6800.0 and r["peak_source"] == "fallback"
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` (the CPU oracle on the host cores) prints one JSON line
+    with the keys of the benchmark contract, on the same metric, unit and workload."""
+    import json
+    import subprocess
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "3"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in line, k
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
+    assert line["value"] > 0 and line["cpu_baseline"]["cores"] >= 1 and line["cpu_baseline"]["kind"] == "port"
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["config"]["workload"] == bench.workload_config()["workload"]
