@@ -589,3 +589,146 @@ extern "C" int evr_psi_read(evr_ctx* c, const char* path, double* psi, int64_t l
   if (n_dropped) *n_dropped = R.dropped;
   return EVR_OK;
 }
+
+// ---------------------------------------------------------------- restart and autocorrelation
+namespace {
+
+int read_text(const char* path, std::vector<std::string>& lines) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return EVR_EINVAL;
+  std::string all;
+  char chunk[1 << 16];
+  size_t got;
+  while ((got = fread(chunk, 1, sizeof chunk, f)) > 0) all.append(chunk, got);
+  const bool err = ferror(f) != 0;
+  fclose(f);
+  if (err) return EVR_EINVAL;
+  size_t a = 0;
+  for (size_t i = 0; i <= all.size(); ++i)
+    if (i == all.size() || all[i] == '\n') {
+      size_t e = i;
+      if (e > a && all[e - 1] == '\r') --e;
+      if (i < all.size() || e > a) lines.push_back(all.substr(a, e - a));
+      a = i + 1;
+    }
+  return EVR_OK;
+}
+
+bool write_all(const char* path, const std::string& s, const char* mode) {
+  FILE* f = fopen(path, mode);
+  if (!f) return false;
+  bool ok = s.empty() || fwrite(s.data(), 1, s.size(), f) == s.size();
+  ok = (fclose(f) == 0) && ok;
+  return ok;
+}
+
+}  // namespace
+
+// SaveWP_restart (Source_ElVibRot/sub_propagation/sub_module_propagation.f90:376-424):
+// "T nb_WP size" then each packet's CvecB as one list-directed record.
+extern "C" int evr_restart_write(evr_ctx* c, const char* path, double t, const double* psi, int64_t ld, int npsi) {
+  if (int rc = check_ctx(c, "evr_restart_write")) return rc;
+  const int64_t N = c->hp.Np * c->hp.nb0;
+  if (!path || !psi || npsi < 1 || ld < N) return set_error(c, EVR_EINVAL, "evr_restart_write: bad arguments");
+  std::string s;
+  char b[96];
+  s.reserve((size_t)npsi * N * 56 + 64);
+  put_real(s, t);
+  snprintf(b, sizeof b, " %d %lld\n", npsi, (long long)N);
+  s += b;
+  for (int j = 0; j < npsi; ++j)
+    for (int64_t k = 0; k < N; ++k) {
+      s += " (";
+      put_real(s, psi[2 * (k + ld * j)]);
+      s += ",";
+      put_real(s, psi[2 * (k + ld * j) + 1]);
+      s += ")";
+      if ((k + 1) % 2 == 0 || k + 1 == N) s += '\n';
+    }
+  if (!write_all(path, s, "w")) return set_error(c, EVR_EINVAL, std::string("evr_restart_write: cannot write ") + path);
+  return EVR_OK;
+}
+
+// ReadWP_restart (:425-488): a file whose first record does not hold "T nb_WP size" means
+// no restart (T = 0, packets untouched, *found = 0); a header whose nb_WP or size differ from
+// npsi or N is an error (the reference STOPs).
+extern "C" int evr_restart_read(evr_ctx* c, const char* path, double* t, double* psi, int64_t ld, int npsi,
+                                int* found) {
+  if (int rc = check_ctx(c, "evr_restart_read")) return rc;
+  const int64_t N = c->hp.Np * c->hp.nb0;
+  if (!path || !t || !psi || !found || npsi < 1 || ld < N) return set_error(c, EVR_EINVAL, "evr_restart_read: bad arguments");
+  *found = 0;
+  *t = 0.0;
+  std::vector<std::string> lines;
+  if (read_text(path, lines)) return set_error(c, EVR_EINVAL, std::string("evr_restart_read: cannot read ") + path);
+  if (lines.empty()) return EVR_OK;
+  std::vector<std::string> h = items_of(lines[0]);
+  double t0;
+  long long nw, sz;
+  if (h.size() < 3 || !parse_real(h[0], &t0) || !parse_int(h[1], &nw) || !parse_int(h[2], &sz)) return EVR_OK;
+  if (nw != npsi || sz != N)
+    return set_error(c, EVR_EINVAL, "evr_restart_read: inconsistent sizes (file " + std::to_string(nw) + " x " +
+                                        std::to_string(sz) + ", expected " + std::to_string(npsi) + " x " +
+                                        std::to_string(N) + ")");
+  std::vector<double> tmp((size_t)2 * N * npsi);
+  int64_t e = 0;
+  const int64_t total = N * npsi;
+  for (size_t li = 1; li < lines.size() && e < total; ++li)
+    for (const std::string& it : items_of(lines[li])) {
+      long long rep;
+      double re, im;
+      if (!parse_value_item(it, 1, &rep, &re, &im))
+        return set_error(c, EVR_EINVAL, "evr_restart_read: value '" + it + "' is not a complex (re,im) constant");
+      for (long long r = 0; r < rep && e < total; ++r, ++e) {
+        tmp[2 * e] = re;
+        tmp[2 * e + 1] = im;
+      }
+      if (e >= total) break;
+    }
+  if (e < total) return set_error(c, EVR_EINVAL, "evr_restart_read: file ends before the last packet");
+  for (int j = 0; j < npsi; ++j)
+    for (int64_t k = 0; k < N; ++k) {
+      psi[2 * (k + ld * j)] = tmp[2 * (j * N + k)];
+      psi[2 * (k + ld * j) + 1] = tmp[2 * (j * N + k) + 1];
+    }
+  *t = t0;
+  *found = 1;
+  return EVR_OK;
+}
+
+// Write_AutoCorr / Read_AutoCorr (:548-578): one line "AutoCor T Re Im |C|" per time.
+extern "C" int evr_autocorr_write(const char* path, const double* t, const double* cdot, int n, int append) {
+  if (!path || n < 0 || (n > 0 && (!t || !cdot))) return EVR_EINVAL;
+  std::string s;
+  for (int i = 0; i < n; ++i) {
+    s += " AutoCor ";
+    put_real(s, t[i]);
+    put_real(s, cdot[2 * i]);
+    put_real(s, cdot[2 * i + 1]);
+    put_real(s, std::hypot(cdot[2 * i], cdot[2 * i + 1]));
+    s += '\n';
+  }
+  return write_all(path, s, append ? "a" : "w") ? EVR_OK : EVR_EINVAL;
+}
+
+// Lines that do not read as "name T Re Im |C|" are skipped (Read_AutoCorr gives them 0).
+extern "C" int evr_autocorr_read(const char* path, double* t, double* cdot, int n_max, int* n) {
+  if (!path || !n || n_max < 0 || (n_max > 0 && (!t || !cdot))) return EVR_EINVAL;
+  std::vector<std::string> lines;
+  if (read_text(path, lines)) return EVR_EINVAL;
+  int k = 0;
+  for (const std::string& L : lines) {
+    if (k >= n_max) break;
+    std::vector<std::string> it = items_of(L);
+    double tt, a, b, m;
+    if (it.size() < 5 || !parse_real(it[1], &tt) || !parse_real(it[2], &a) || !parse_real(it[3], &b) ||
+        !parse_real(it[4], &m))
+      continue;
+    t[k] = tt;
+    cdot[2 * k] = a;
+    cdot[2 * k + 1] = b;
+    ++k;
+  }
+  *n = k;
+  return EVR_OK;
+}

@@ -65,7 +65,8 @@ EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_
            "evr_cheby_propagate", "evr_fma_peak", "evr_hpsi_noalloc", "evr_set_dipole", "evr_set_field",
            "evr_oc_forward", "evr_oc_backward", "evr_create_batch", "evr_batch_offsets", "evr_batch_davidson", "evr_autotune",
            "evr_psi_write", "evr_psi_read", "evr_set_vgrid", "evr_set_dipole_grid",
-           "evr_sil_propagate"]
+           "evr_sil_propagate", "evr_restart_write", "evr_restart_read", "evr_autocorr_write",
+           "evr_autocorr_read"]
 VGRID_LAYOUT = {"terms": 0, "ref": 1}
 WP_FORMAT = {"v0": 0, "v1": 1, "unformatted": 2, "sparse": 3}
 
@@ -115,6 +116,10 @@ def load(build: bool = True):
     L.evr_oc_backward.argtypes = [vp, _dp, _dp, _lp]
     L.evr_psi_write.argtypes = [vp, C.c_char_p, C.c_int, _dp, C.c_int64, C.c_int, C.c_int, C.c_double]
     L.evr_psi_read.argtypes = [vp, C.c_char_p, _dp, C.c_int64, C.c_int, C.c_int, _ip, _lp]
+    L.evr_restart_write.argtypes = [vp, C.c_char_p, C.c_double, _dp, C.c_int64, C.c_int]
+    L.evr_restart_read.argtypes = [vp, C.c_char_p, _dp, _dp, C.c_int64, C.c_int, _ip]
+    L.evr_autocorr_write.argtypes = [C.c_char_p, _dp, _dp, C.c_int, C.c_int]
+    L.evr_autocorr_read.argtypes = [C.c_char_p, _dp, _dp, C.c_int, _ip]
     if hasattr(L, "evr_davidson"):
         L.evr_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _dp, _dp, _dp, _lp]
     if hasattr(L, "evr_cheby_propagate"):
@@ -175,6 +180,26 @@ def _describe(spec, keep):
     d.G0 = F(np.asarray(spec.G0).ravel(order="F"))
     d.g = F(np.asarray(spec.g).ravel(order="F"))
     return d
+
+
+def write_autocorr(path, t, cdot, append=False):
+    """Autocorrelation lines "AutoCor T Re Im |C|" (Write_AutoCorr)."""
+    t = _darr(t)
+    c = np.ascontiguousarray(np.asarray(cdot, dtype=np.complex128))
+    rc = load().evr_autocorr_write(os.fsencode(path), _p(t, _dp), c.ctypes.data_as(_dp), len(t), 1 if append else 0)
+    if rc != 0:
+        raise EvrError(rc, f"evr_autocorr_write: cannot write {path}")
+
+
+def read_autocorr(path, n_max=1 << 20):
+    """(t, cdot) of an autocorrelation file (Read_AutoCorr)."""
+    t = np.zeros(n_max)
+    c = np.zeros(n_max, dtype=np.complex128)
+    n = C.c_int()
+    rc = load().evr_autocorr_read(os.fsencode(path), _p(t, _dp), c.ctypes.data_as(_dp), n_max, C.byref(n))
+    if rc != 0:
+        raise EvrError(rc, f"evr_autocorr_read: cannot read {path}")
+    return t[: n.value].copy(), c[: n.value].copy()
 
 
 class Problem:
@@ -284,6 +309,20 @@ class Problem:
             nrm = np.sqrt(np.sum(np.abs(a) ** 2, axis=0))
             a = a / np.where(nrm > 0, nrm, 1.0)
         return a, dropped.value
+
+    def write_restart(self, path, t, psi):
+        """Propagation restart file (SaveWP_restart): time t and complex packets psi (N x npsi)."""
+        a = np.asfortranarray(np.asarray(psi, dtype=np.complex128).reshape(self.N, -1))
+        self._check(load().evr_restart_write(self.h, os.fsencode(path), float(t), a.ctypes.data_as(_dp), self.N,
+                                             a.shape[1]))
+
+    def read_restart(self, path, npsi):
+        """(t, packets N x npsi) of a restart file, or (0.0, None) when it holds no restart."""
+        a = np.zeros((self.N, npsi), dtype=np.complex128, order="F")
+        t, found = C.c_double(), C.c_int()
+        self._check(load().evr_restart_read(self.h, os.fsencode(path), C.byref(t), a.ctypes.data_as(_dp), self.N,
+                                            npsi, C.byref(found)))
+        return (t.value, a) if found.value else (0.0, None)
 
     # ---- H.psi ----------------------------------------------------------------------
     def hpsi(self, psi, prec: str = "fp64"):

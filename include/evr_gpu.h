@@ -349,6 +349,19 @@ int evr_psi_write(evr_ctx *ctx, const char *path, int format, const double *psi,
  * line or record at fault, where the reference STOPs. */
 int evr_psi_read(evr_ctx *ctx, const char *path, double *psi, int64_t ld, int npsi_max, int cplx, int *npsi_read,
                  int64_t *n_dropped);
+/* Propagation restart file: SaveWP_restart / ReadWP_restart
+ * (Source_ElVibRot/sub_propagation/sub_module_propagation.f90:376-488): a "T nb_WP size"
+ * record, then each packet's complex coefficients as one list-directed record.  psi: complex
+ * packets in the Fortran COMPLEX(8) layout (ld >= N).  evr_restart_read: a file without
+ * that first record means no restart (*found = 0, *t = 0, psi untouched); nb_WP != npsi or
+ * size != N returns EVR_EINVAL, where the reference STOPs. */
+int evr_restart_write(evr_ctx *ctx, const char *path, double t, const double *psi, int64_t ld, int npsi);
+int evr_restart_read(evr_ctx *ctx, const char *path, double *t, double *psi, int64_t ld, int npsi, int *found);
+/* Autocorrelation file lines "AutoCor T Re Im |C|" (Write_AutoCorr / Read_AutoCorr, :548-578);
+ * cdot: n complex values (re, im).  append != 0 adds to an existing file.  The reader keeps
+ * the lines that read as such (at most n_max) and skips the others. */
+int evr_autocorr_write(const char *path, const double *t, const double *cdot, int n, int append);
+int evr_autocorr_read(const char *path, double *t, double *cdot, int n_max, int *n);
 
 #ifdef __cplusplus
 }

@@ -1,5 +1,5 @@
 """Restatement of the reference's wave-packet file forms, for checking the library's
-reader and writer (evr_psi_read / evr_psi_write).
+readers and writers (evr_psi_read / evr_psi_write, evr_restart_*, evr_autocorr_*).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/.  The product library never imports it.
 
@@ -11,6 +11,8 @@ NAME=value lines), and reads the same forms back:
       Source_ElVibRot/sub_WP/sub_module_psi_io.f90:365-424, 1441-1498, 1607-1778
   ecri_psiBasisRepnotall_nD   :783-917      (sparse packets, "end wp k" lines)
   Read_header_saveFile_psi    :1294-1439    (the three formatted headers, unformatted)
+  SaveWP_restart / ReadWP_restart, Write_AutoCorr / Read_AutoCorr
+      Source_ElVibRot/sub_propagation/sub_module_propagation.f90:376-488, 548-578
 A function is its tuple n_1..n_D i_h i_e (Rec_ndim_index, sub_module_basis.f90:3156),
 taken here from the oracle's packed table, with i_h = 1 and i_e the electronic state.
 
@@ -173,3 +175,48 @@ def to_block(packets, packed, nb0, cplx):
             else:
                 out[r, j] = v
     return out, dropped
+
+
+def write_restart(path, t, psi):
+    """SaveWP_restart (Source_ElVibRot/sub_propagation/sub_module_propagation.f90:376-424):
+    `write(no,*) T,size(WP),size(CvecB)` then `write(no,*) WP(i)%CvecB` per packet."""
+    psi = np.asarray(psi, dtype=np.complex128)
+    N, npsi = psi.shape
+    lines = [_fr(t) + _fi(npsi) + _fi(N)]
+    for j in range(npsi):
+        lines += [_fc(z.real, z.imag) for z in psi[:, j]]
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def read_restart(path, npsi):
+    with open(path) as f:
+        lines = f.read().splitlines()
+    h = lines[0].split()
+    t, nw, n = _num(h[0]), int(h[1]), int(h[2])
+    assert nw == npsi
+    vals = []
+    for ln in lines[1:]:
+        for item in ln.replace(" ", "").split(")("):
+            if item.strip("()"):
+                a, b = item.strip("()").split(",")
+                vals.append(complex(_num(a), _num(b)))
+    return t, np.array(vals).reshape(npsi, n).T
+
+
+def write_autocorr(path, t, cdot):
+    """Write_AutoCorr (:548-557): `write(no,*) 'AutoCor ',T,real(cdot),aimag(cdot),abs(cdot)`."""
+    with open(path, "w") as f:
+        for tt, z in zip(t, cdot):
+            f.write(" AutoCor " + _fr(tt) + _fr(z.real) + _fr(z.imag) + _fr(abs(z)) + "\n")
+
+
+def read_autocorr(path):
+    t, c = [], []
+    with open(path) as f:
+        for ln in f:
+            p = ln.split()
+            if len(p) >= 5 and p[0] == "AutoCor":
+                t.append(_num(p[1]))
+                c.append(complex(_num(p[2]), _num(p[3])))
+    return np.array(t), np.array(c)

@@ -225,3 +225,55 @@ def test_unformatted_file_with_8_byte_integers(tmp_path):
     f.write_bytes(b"".join(out))
     got, dropped = pg.read_psi(f)
     assert dropped == 0 and np.array_equal(got, psi)
+
+
+def test_restart_file_round_trip_and_oracle(tmp_path):
+    """SaveWP_restart / ReadWP_restart: bit-exact round trip, files of the restated Fortran
+    statements read by the library and the library's read by them."""
+    pg = E.Problem(_two_state_sg4(3, 3), device=-1)
+    psi = _block(np.random.default_rng(12), pg.N, 3, True)
+    f = tmp_path / "restart"
+    pg.write_restart(f, 1234.5678901234567, psi)
+    t, back = pg.read_restart(f, 3)
+    assert t == 1234.5678901234567 and np.array_equal(back, psi)
+    t2, b2 = W.read_restart(f, 3)
+    assert t2 == t and np.array_equal(b2, psi)
+    g = tmp_path / "restart_oracle"
+    W.write_restart(g, 10.0, psi)
+    t3, b3 = pg.read_restart(g, 3)
+    assert t3 == 10.0 and np.array_equal(b3, psi)
+
+
+def test_restart_file_absent_header_and_size_mismatch(tmp_path):
+    pg = E.Problem(S.henon_heiles(3, 2), device=-1)
+    f = tmp_path / "empty_restart"
+    f.write_text("\n")
+    assert pg.read_restart(f, 1) == (0.0, None)  # no restart: start at T = 0
+    psi = _block(np.random.default_rng(13), pg.N, 2, True)
+    g = tmp_path / "restart"
+    pg.write_restart(g, 5.0, psi)
+    with pytest.raises(E.EvrError) as ei:  # two packets in the file, one requested
+        pg.read_restart(g, 1)
+    assert ei.value.code == E.EVR_EINVAL
+    g.write_text("\n".join(g.read_text().splitlines()[:-3]) + "\n")
+    with pytest.raises(E.EvrError):
+        pg.read_restart(g, 2)
+
+
+def test_autocorr_file(tmp_path):
+    rng = np.random.default_rng(14)
+    t = np.arange(7) * 4.134
+    c = rng.standard_normal(7) + 1j * rng.standard_normal(7)
+    f = tmp_path / "file_auto"
+    E.write_autocorr(f, t[:4], c[:4])
+    E.write_autocorr(f, t[4:], c[4:], append=True)
+    with open(f, "a") as h:
+        h.write(" not an autocorrelation line\n")
+    tt, cc = E.read_autocorr(f)
+    assert np.array_equal(tt, t) and np.array_equal(cc, c)
+    to, co = W.read_autocorr(f)
+    assert np.array_equal(to, t) and np.array_equal(co, c)
+    g = tmp_path / "file_auto_oracle"
+    W.write_autocorr(g, t, c)
+    tt, cc = E.read_autocorr(g)
+    assert np.array_equal(tt, t) and np.array_equal(cc, c)
