@@ -1,4 +1,4 @@
-// evr_propagate.cu -- Chebyshev propagation of complex wave packets on the GPU.
+// evr_propagate.cu -- Chebyshev and short-iterative-Lanczos propagation of complex wave packets on the GPU.
 //
 // Restates march_cheby (Source_ElVibRot/sub_propagation/sub_module_propa_march.f90:4142-4434):
 //   psi(t+dt) = exp(-i E0 dt) sum_k c_k phi_k,  phi_k = (-i)^k T_k(Hs) psi(t),
@@ -454,7 +454,7 @@ extern "C" int evr_sil_propagate(evr_ctx* c, const double* psi0, int npsi, doubl
   const int op = c->op_form;
   int64_t n_hpsi = 0;
   int max_dim = 0;
-  std::vector<double> nrm(npsi), E0(npsi), ure, uim;
+  std::vector<double> nrm(npsi), E0(npsi);
   std::vector<std::vector<double>> alpha(npsi), beta(npsi), u_re(npsi), u_im(npsi);
   std::vector<int> dim(npsi);
   for (int st = 1; st <= nsteps; ++st) {
