@@ -337,6 +337,22 @@ void check_graphs(evr_ctx* c, OCState* o) {
 
 namespace evr {
 void free_control(evr_ctx* c) { oc_free(c); }
+
+// The FP64 and FP32 dipole tables, both or neither: a failed allocation frees the other,
+// so a context never holds one without the other.
+int alloc_dipole_tables(evr_ctx* c, size_t n) {
+  if (c->dp_mugrid && c->dp_mugrid32) return EVR_OK;
+  cudaError_t e = cudaSuccess;
+  if (!c->dp_mugrid) e = cudaMalloc((void**)&c->dp_mugrid, n * sizeof(double));
+  if (e == cudaSuccess && !c->dp_mugrid32) e = cudaMalloc((void**)&c->dp_mugrid32, n * sizeof(float));
+  if (e != cudaSuccess) {
+    if (c->dp_mugrid) cudaFree(c->dp_mugrid);
+    if (c->dp_mugrid32) cudaFree(c->dp_mugrid32);
+    c->dp_mugrid = nullptr;
+    c->dp_mugrid32 = nullptr;
+  }
+  return cuda_check(c, e, "cudaMalloc dipole");
+}
 }  // namespace evr
 
 extern "C" {
@@ -359,10 +375,7 @@ int evr_set_dipole(evr_ctx* c, int n_mono, const double* coef, const int* idx, c
   if (rc) return rc;
   cudaStream_t s = c->stream;
   const size_t n = (size_t)P.sum_nq * P.nb0 * P.nb0;
-  if (!c->dp_mugrid) {
-    if ((rc = cuda_check(c, cudaMalloc((void**)&c->dp_mugrid, n * sizeof(double)), "cudaMalloc dipole"))) return rc;
-    if ((rc = cuda_check(c, cudaMalloc((void**)&c->dp_mugrid32, n * sizeof(float)), "cudaMalloc dipole"))) return rc;
-  }
+  if ((rc = alloc_dipole_tables(c, n))) return rc;
   double* dcoef = nullptr;
   int *didx = nullptr, *delec = nullptr;
   const int nm = std::max(n_mono, 1);
@@ -416,10 +429,7 @@ int evr_set_dipole_grid(evr_ctx* c, const double* mu, int layout) {
         mmax = std::max(mmax, r);
       }
   if ((rc = cuda_check(c, cudaDeviceSynchronize(), "sync before dipole update"))) return rc;
-  if (!c->dp_mugrid) {
-    if ((rc = cuda_check(c, cudaMalloc((void**)&c->dp_mugrid, n * sizeof(double)), "cudaMalloc dipole"))) return rc;
-    if ((rc = cuda_check(c, cudaMalloc((void**)&c->dp_mugrid32, n * sizeof(float)), "cudaMalloc dipole"))) return rc;
-  }
+  if ((rc = alloc_dipole_tables(c, n))) return rc;
   cudaStream_t s = c->stream;
   if ((rc = cuda_check(c, cudaMemcpyAsync(c->dp_mugrid, dev.data(), n * sizeof(double), cudaMemcpyHostToDevice, s),
                        "copy dipole")) ||
