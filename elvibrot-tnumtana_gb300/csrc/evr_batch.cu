@@ -777,8 +777,6 @@ struct BatchDavidson {
     return e == cudaSuccess ? EVR_OK : fail(EVR_EDEVICE, std::string("combine launch: ") + cudaGetErrorString(e));
   }
 
-  int rows(int q) const { return (int)(off[q + 1] - off[q]); }
-
   // H.psi of n columns for the active problems only (the others' rows come out zero)
   int hop(double* x, int ldx, double* y, int ldy, int n, int prec, int64_t& c64, int64_t& c32) {
     int na = 0;
