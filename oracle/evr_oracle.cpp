@@ -618,7 +618,7 @@ extern "C" {
 
 void* or_create(int kind, int D, int nb0, int LG, int LB, const int* Aq, const int* Bq, const int* Ab,
                 const int* Bb, const int* nq_dp, const int* nb_dp, const double* scaleQ, const double* Q0) {
-  if (D < 1 || D > 16 || nb0 < 1) return nullptr;
+  if (D < 1 || D > 32 || nb0 < 1) return nullptr;
   return create(kind, D, nb0, LG, LB, Aq, Bq, Ab, Bb, nq_dp, nb_dp, scaleQ, Q0);
 }
 

@@ -10,6 +10,8 @@ Contents:
                   (Source_ElVibRot/sub_Basis/sub_quadra_herm.f90:322-343);
   hh6d_levels  -> column 1 of Working_tests/MPI_tests/6D_Davidson_S0/benchmark
                   (28 Davidson levels of the 6-D Henon-Heiles SG4 L=3 model, au);
+  hh21d_levels -> column 1 of Working_tests/MPI_tests/21D_Davidson_S0/benchmark
+                  (22 Davidson levels of the 21-D Henon-Heiles SG4 L=2 model, au);
   pyr12d_autocorr -> Working_tests/MPI_tests/12D_propagation_S0/benchmark
                   (t in au, Re C, Im C, |C| of the 12-D pyrazine SG4 L=1 Chebyshev run);
   wp_inputs    -> the start packets written after the namelists of two input files, in
@@ -63,6 +65,8 @@ def main(root):
         out["herm"][str(n)] = rows
     with open(os.path.join(root, "Working_tests", "MPI_tests", "6D_Davidson_S0", "benchmark")) as f:
         out["hh6d_levels"] = [float(line.split()[0]) for line in f if line.strip()]
+    with open(os.path.join(root, "Working_tests", "MPI_tests", "21D_Davidson_S0", "benchmark")) as f:
+        out["hh21d_levels"] = [float(line.split()[0]) for line in f if line.strip()]
     with open(os.path.join(root, "Working_tests", "MPI_tests", "12D_propagation_S0", "benchmark")) as f:
         out["pyr12d_autocorr"] = [[float(v) for v in line.split()] for line in f if line.strip()]
     out["wp_inputs"] = {

@@ -31,6 +31,22 @@ def test_hh6d_spectrum_matches_davidson_benchmark(golden):
     assert np.abs(d).max() <= 2e-7
 
 
+def test_hh21d_spectrum_matches_davidson_benchmark(golden):
+    # Working_tests/MPI_tests/21D_Davidson_S0/benchmark: 22 levels of the 21-D Henon-Heiles
+    # model on SG4 L=2 (same potential file as the 6-D case), from a Davidson run with
+    # conv_resi = 5e-4 au.  The oracle's dense spectrum lies at or below each level, within
+    # 2e-7 au.  (The library's term tables hold at most 16 modes, so only the oracle runs it.)
+    ref = np.array(golden["hh21d_levels"])
+    op = O.OracleProblem(S.henon_heiles(21, 2))
+    assert (op.Np, op.nterm, op.sum_nb) == (925, 253, 2059)
+    H = op.dense()
+    assert np.abs(H - H.T).max() < 1e-12
+    ev = np.linalg.eigvalsh(0.5 * (H + H.T))[: len(ref)]
+    d = ev - ref
+    assert d.max() <= 1e-9
+    assert np.abs(d).max() <= 2e-7
+
+
 def test_pyrazine12d_autocorrelation_matches_benchmark(golden):
     # Working_tests/MPI_tests/12D_propagation_S0/benchmark (checked at 1e-8 by MPI_test.sh):
     # exact propagation of psi0 = |1..1> on electronic state 2 with the oracle's operator.
