@@ -172,6 +172,35 @@ def pyrazine_12d(L: int = 1) -> ProblemSpec:
                        name=f"pyrazine12D_L{L}")
 
 
+def pyrazine_vibronic(w, k1, k2, delta, lam, B, L, name="pyrazine") -> ProblemSpec:
+    """Two-state pyrazine vibronic model of the reference's propagation tests for any number
+    of modes (sub_system_pyrazine.f): V11 = 1/2 sum w_i Q_i^2 - delta + sum k1_i Q_i,
+    V22 = 1/2 sum w_i Q_i^2 + delta + sum k2_i Q_i, V12 = lam Q_1 (eV), analytic type-1 KEO
+    F2(i,i) = -w_i/2, HO bases nb = nq = 1 + B_i l on SG4 level L."""
+    D = len(w)
+    ev = 1.0 / AU_TO_EV
+    w = np.asarray(w, dtype=np.float64)
+    p = Poly()
+    for e in (0, 1):
+        for i in range(D):
+            p.add(0.5 * w[i] * ev, [i, i], e, e)
+    p.add(-delta * ev, [], 0, 0)
+    p.add(delta * ev, [], 1, 1)
+    for i in range(D):
+        if k1[i] != 0.0:
+            p.add(k1[i] * ev, [i], 0, 0)
+        if k2[i] != 0.0:
+            p.add(k2[i] * ev, [i], 1, 1)
+    p.add(lam * ev, [0], 0, 1)
+    p.add(lam * ev, [0], 1, 0)
+    c, idx, el = p.arrays()
+    B = np.asarray(B, dtype=np.int32)
+    one = np.ones(D, dtype=np.int32)
+    return ProblemSpec(kind="sg4", D=D, nb0=2, LG=L, LB=L, Aq=one, Bq=B, Ab=one, Bb=B,
+                       mono_coef=c, mono_idx=idx, mono_elec=el, keo_type=1, G0=np.diag(w * ev),
+                       name=f"{name}{D}D_L{L}")
+
+
 # ------------------------------------------------------------------------------------
 # Synthetic benchmark workloads (seeded)
 # ------------------------------------------------------------------------------------

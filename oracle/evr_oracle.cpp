@@ -18,6 +18,7 @@
 #include <cstring>
 #include <cstdio>
 #include <vector>
+#include <string>
 #include <unordered_map>
 #include <algorithm>
 #include <omp.h>
@@ -362,17 +363,11 @@ static Problem* create(int kind, int D, int nb0, int LG, int LB, const int* Aq, 
   P->sum_nb = P->off_nb[nterm]; P->sum_nq = P->off_nq[nterm];
 
   // packed basis
-  std::unordered_map<uint64_t, int> index;
+  std::unordered_map<std::string, int> index;
   std::vector<int> nbmax(D);
   for (int d = 0; d < D; ++d) nbmax[d] = (int)P->ltab[d].size() - 1;
-  // mixed-radix key of a 1-based tuple; the radices are the per-mode sizes, so the key
-  // is exact (the product of the sizes is far below 2^63 for every supported problem)
-  auto key = [&](const int* n) { uint64_t k = 0; for (int d = 0; d < D; ++d) k = k * (uint64_t)(nbmax[d] + 1) + (uint64_t)n[d]; return k; };
-  {
-    long double prod = 1.0L;
-    for (int d = 0; d < D; ++d) prod *= (long double)(nbmax[d] + 1);
-    if (prod > 9.0e18L) { delete P; return nullptr; }
-  }
+  // key of a 1-based tuple: its bytes, exact for any number of modes and sizes
+  auto key = [&](const int* n) { return std::string((const char*)n, sizeof(int) * (size_t)D); };
   std::vector<int> n(D, 1);
   if (kind == 0) {
     // type 5 nDindB, last index fastest, sum_i l(n_i) <= LB

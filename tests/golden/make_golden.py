@@ -14,6 +14,12 @@ Contents:
                   (22 Davidson levels of the 21-D Henon-Heiles SG4 L=2 model, au);
   pyr12d_autocorr -> Working_tests/MPI_tests/12D_propagation_S0/benchmark
                   (t in au, Re C, Im C, |C| of the 12-D pyrazine SG4 L=1 Chebyshev run);
+  pyr24d_autocorr -> Working_tests/MPI_tests/24D_propagation_S0/benchmark (same columns,
+                  24-D pyrazine SG4 L=2);
+  pyr24d_model -> the parameters of that run's potential, read from the data statements of
+                  Working_tests/MPI_tests/24D_propagation_S0/sub_system_pyrazine.f
+                  (w, k1, k2 per mode, delta, lambda, in eV) and the mode rule
+                  L_TO_nq_B of its shell_run (B1..B4, then B);
   wp_inputs    -> the start packets written after the namelists of two input files, in
                   the sparse form that lect_psiBasisRepnotall_nD reads
                   (Source_ElVibRot/sub_WP/sub_module_psi_io.f90:563-780):
@@ -53,6 +59,30 @@ def packet_lines(path):
     return out
 
 
+def fortran_array(text, name):
+    """Values of a Fortran array constructor `name(ndim) = (/ ... /)` (fixed form)."""
+    m = re.search(name + r"\(ndim\)\s*=\s*\(/(.*?)/\)", text, flags=re.S)
+    body = re.sub(r"\n\s*\*", " ", m.group(1)).replace("_Rkind", "")
+    return [0.0 if v.strip().upper() == "ZERO" else float(v) for v in body.split(",")]
+
+
+def fortran_scalar(text, name):
+    return float(re.search(name + r"\s*=\s*([-0-9.eEdD+]+)_Rkind", text).group(1))
+
+
+def pyrazine24_model(root):
+    d = os.path.join(root, "Working_tests", "MPI_tests", "24D_propagation_S0")
+    with open(os.path.join(d, "sub_system_pyrazine.f")) as f:
+        src = f.read()
+    with open(os.path.join(d, "shell_run")) as f:
+        sh = f.read()
+    b = {k: int(re.search(r"^" + k + r"=(\d+)", sh, flags=re.M).group(1)) for k in ("B1", "B2", "B3", "B4", "B")}
+    L = int(open(os.path.join(d, "run_jobs")).read().split()[2])
+    return dict(w=fortran_array(src, "w"), k1=fortran_array(src, "k1"), k2=fortran_array(src, "k2"),
+                delta=fortran_scalar(src, "delta"), lam=fortran_scalar(src, "lambda"),
+                B=[b["B1"], b["B2"], b["B3"], b["B4"]] + [b["B"]] * 20, L=L)
+
+
 def main(root):
     out = {"herm": {}}
     for n in range(1, 41):
@@ -69,6 +99,9 @@ def main(root):
         out["hh21d_levels"] = [float(line.split()[0]) for line in f if line.strip()]
     with open(os.path.join(root, "Working_tests", "MPI_tests", "12D_propagation_S0", "benchmark")) as f:
         out["pyr12d_autocorr"] = [[float(v) for v in line.split()] for line in f if line.strip()]
+    with open(os.path.join(root, "Working_tests", "MPI_tests", "24D_propagation_S0", "benchmark")) as f:
+        out["pyr24d_autocorr"] = [[float(v) for v in line.split()] for line in f if line.strip()]
+    out["pyr24d_model"] = pyrazine24_model(root)
     out["wp_inputs"] = {
         "hcn_dat_Davidson": dict(D=3, nb0=1, cplx=False, lines=packet_lines(
             os.path.join(root, "Working_tests", "exa_hcn-test", "dat_Davidson"))),

@@ -70,3 +70,23 @@ def test_term_and_packed_tables_sg4_6d_l8():
     t = op.tables()
     assert set(np.unique(t["weight"])) <= {-10.0, -5.0, -1.0, 1.0, 5.0, 10.0}
     assert t["map"].min() == 0 and t["map"].max() == op.Np - 1
+
+
+def test_pyrazine24d_autocorrelation_matches_benchmark(golden):
+    # Working_tests/MPI_tests/24D_propagation_S0/benchmark (checked at 1e-8 by MPI_test.sh):
+    # the 24-D two-state pyrazine model of that run (parameters read from its potential file
+    # into the fixture), SG4 L=2, exact propagation of |1..1> on electronic state 2.
+    m = golden["pyr24d_model"]
+    ref = np.array(golden["pyr24d_autocorr"])
+    sp = S.pyrazine_vibronic(m["w"], m["k1"], m["k2"], m["delta"], m["lam"], m["B"], m["L"])
+    op = O.OracleProblem(sp)
+    assert (op.Np, op.nterm) == (1502, 325)
+    H = op.dense()
+    assert np.abs(H - H.T).max() < 1e-12
+    w, V = np.linalg.eigh(0.5 * (H + H.T))
+    psi0 = np.zeros(op.N)
+    psi0[op.Np] = 1.0
+    c0 = V.T @ psi0
+    for t, re, im, _ in ref:
+        a = psi0 @ (V @ (np.exp(-1j * w * t) * c0))
+        assert abs(a - (re + 1j * im)) <= 1e-8
