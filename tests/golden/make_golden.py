@@ -77,7 +77,8 @@ def pyrazine24_model(root):
     with open(os.path.join(d, "shell_run")) as f:
         sh = f.read()
     b = {k: int(re.search(r"^" + k + r"=(\d+)", sh, flags=re.M).group(1)) for k in ("B1", "B2", "B3", "B4", "B")}
-    L = int(open(os.path.join(d, "run_jobs")).read().split()[2])
+    with open(os.path.join(d, "run_jobs")) as f:
+        L = int(f.read().split()[2])  # "./shell_run <cores> <L>"
     return dict(w=fortran_array(src, "w"), k1=fortran_array(src, "k1"), k2=fortran_array(src, "k2"),
                 delta=fortran_scalar(src, "delta"), lam=fortran_scalar(src, "lambda"),
                 B=[b["B1"], b["B2"], b["B3"], b["B4"]] + [b["B"]] * 20, L=L)
