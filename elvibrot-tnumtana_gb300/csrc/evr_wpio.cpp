@@ -89,6 +89,11 @@ double val(const double* psi, int64_t ld, int cplx, int j, int64_t k, int part) 
 // letter that some compilers write for three-digit exponents (1.0+100).
 bool parse_real(const std::string& t, double* out) {
   if (t.empty()) return false;
+  {  // common case: a C-style number, read in place
+    char* end = nullptr;
+    *out = strtod(t.c_str(), &end);
+    if (end && *end == '\0' && end != t.c_str()) return true;
+  }
   std::string u;
   u.reserve(t.size() + 1);
   for (size_t i = 0; i < t.size(); ++i) {
@@ -467,17 +472,23 @@ extern "C" int evr_psi_write(evr_ctx* c, const char* path, int format, const dou
     s.clear();
     return ok;
   };
-  auto tuple = [&](int64_t row, std::string& t) {
-    const int64_t k = row % P.Np;
-    const int ie = (int)(row / P.Np) + 1;
+  // the text of each row's tuple, formatted once and reused for every packet
+  std::vector<std::string> tup;
+  if (format != EVR_WP_UNFORMATTED_V1) {
+    tup.resize((size_t)N);
     char b[24];
-    for (int i = 0; i < D; ++i) {
-      snprintf(b, sizeof b, " %d", P.packed[(size_t)k * D + i]);
+    for (int64_t row = 0; row < N; ++row) {
+      const int64_t k = row % P.Np;
+      std::string& t = tup[(size_t)row];
+      for (int i = 0; i < D; ++i) {
+        snprintf(b, sizeof b, " %d", P.packed[(size_t)k * D + i]);
+        t += b;
+      }
+      snprintf(b, sizeof b, " %d %d", 1, (int)(row / P.Np) + 1);
       t += b;
     }
-    snprintf(b, sizeof b, " %d %d", 1, ie);
-    t += b;
-  };
+  }
+  auto tuple = [&](int64_t row, std::string& t) { t += tup[(size_t)row]; };
   bool ok = true;
   if (format == EVR_WP_UNFORMATTED_V1) {
     const char X = 'X';
