@@ -277,3 +277,28 @@ def test_autocorr_file(tmp_path):
     W.write_autocorr(g, t, c)
     tt, cc = E.read_autocorr(g)
     assert np.array_equal(tt, t) and np.array_equal(cc, c)
+
+
+def test_fortran_list_directed_variants(tmp_path):
+    """Forms other compilers write: the namelist on one line with spaces around '=', D
+    exponents, repeat counts r*x, an exponent without its letter (1.5-100), comma
+    separators and CRLF line ends."""
+    pg = E.Problem(S.henon_heiles(3, 2), device=-1)
+    packed = _packed(S.henon_heiles(3, 2))
+    N = pg.N
+    want = np.zeros(N)
+    want[0], want[1], want[2], want[3] = 0.5, -2.0, 1.5e-100, 3.0
+    vals = ["5.0D-01", "-2.0d0", "1.5-100", "3.0E+000"] + ([f"{N - 4}*0.0"] if N > 4 else [])
+    lines = [" &headerFile Version_File = 1, nb_psi = 1, nb_tot = %d /" % N]
+    lines += [" ".join(str(x) for x in t) for t in W.tuples(packed, 1)]
+    lines += [", ".join(vals)]
+    f = tmp_path / "variants.wp"
+    f.write_bytes(("\r\n".join(lines) + "\r\n").encode())
+    got, dropped = pg.read_psi(f)
+    assert dropped == 0 and got.shape == (N, 1)
+    assert np.array_equal(got[:, 0], want)
+    # complex values with a repeat count and blanks inside the parentheses
+    lines[-1] = "( 1.0D0 , -2.0 ) %d*(0.0,0.0)" % (N - 1)
+    f.write_text("\n".join(lines) + "\n")
+    got, _ = pg.read_psi(f, cplx=True)
+    assert got[0, 0] == 1.0 - 2.0j and not got[1:, 0].any()
