@@ -147,29 +147,7 @@ def pyrazine_12d(L: int = 1) -> ProblemSpec:
     nb = nq = 1 + B_i l with B = 3,3,2,2,2,... (shell_run), V from sub_system_pyrazine.f
     (in eV, converted with the reference's CODATA-2006 eV), analytic type-1 KEO
     F2(i,i) = -w_i/2 (calc_f2_f1Q.f90)."""
-    D = 12
-    ev = 1.0 / AU_TO_EV
-    w, k1, k2 = np.array(PYRAZINE_W), np.array(PYRAZINE_K1), np.array(PYRAZINE_K2)
-    delta, lam = 0.46165, 0.1825
-    p = Poly()
-    for e in (0, 1):
-        for i in range(D):
-            p.add(0.5 * w[i] * ev, [i, i], e, e)
-    p.add(-delta * ev, [], 0, 0)
-    p.add(delta * ev, [], 1, 1)
-    for i in range(D):
-        if k1[i] != 0.0:
-            p.add(k1[i] * ev, [i], 0, 0)
-        if k2[i] != 0.0:
-            p.add(k2[i] * ev, [i], 1, 1)
-    p.add(lam * ev, [0], 0, 1)
-    p.add(lam * ev, [0], 1, 0)
-    c, idx, el = p.arrays()
-    B = np.array([3, 3, 2, 2] + [2] * 8, dtype=np.int32)
-    one = np.ones(D, dtype=np.int32)
-    return ProblemSpec(kind="sg4", D=D, nb0=2, LG=L, LB=L, Aq=one, Bq=B, Ab=one, Bb=B,
-                       mono_coef=c, mono_idx=idx, mono_elec=el, keo_type=1, G0=np.diag(w * ev),
-                       name=f"pyrazine12D_L{L}")
+    return pyrazine_vibronic(PYRAZINE_W, PYRAZINE_K1, PYRAZINE_K2, 0.46165, 0.1825, [3, 3, 2, 2] + [2] * 8, L)
 
 
 def pyrazine_vibronic(w, k1, k2, delta, lam, B, L, name="pyrazine") -> ProblemSpec:

@@ -94,3 +94,13 @@ def test_sil_needs_a_device():
     with pytest.raises(E.EvrError) as ei:
         pg.sil(np.ones(pg.N, dtype=complex), 1.0, 1)
     assert ei.value.code == E.EVR_EDEVICE
+
+
+def test_pyrazine_builders_agree():
+    """pyrazine_12d is the general vibronic builder on the 12-D parameters: same monomials,
+    KEO and bases (the 24-D oracle pin builds its model with the same function)."""
+    a = S.pyrazine_12d(1)
+    b = S.pyrazine_vibronic(S.PYRAZINE_W, S.PYRAZINE_K1, S.PYRAZINE_K2, 0.46165, 0.1825, [3, 3, 2, 2] + [2] * 8, 1)
+    for k in ("D", "nb0", "LG", "LB", "Aq", "Bq", "Ab", "Bb", "mono_coef", "mono_idx", "mono_elec", "keo_type",
+              "G0", "g"):
+        assert np.array_equal(np.asarray(getattr(a, k)), np.asarray(getattr(b, k))), k
