@@ -181,6 +181,55 @@ int evr_set_vgrid(evr_ctx* c, const double* v, int layout) {
   return EVR_OK;
 }
 
+// Replaces (or creates) the per-point G(Q) table of a type-10 context with host values.
+// The rows follow grid_eval_kernel's layout: per device grid point one row of
+// g_table_stride(D) entries, (i, j >= i) over the term's positions in its permuted order.
+int evr_set_ggrid(evr_ctx* c, const double* G) {
+  if (!c) return EVR_EINVAL;
+  if (!G) return set_error(c, EVR_EINVAL, "evr_set_ggrid: null values");
+  if (c->batch) return set_error(c, EVR_EINVAL, "evr_set_ggrid: not for batched contexts");
+  const HostProblem& P = c->hp;
+  if (P.keo_type != 10) return set_error(c, EVR_EINVAL, "evr_set_ggrid: the KEO of the context is not type 10");
+  if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
+  EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
+  const int D = P.D, stride = g_table_stride(D);
+  const size_t ng = (size_t)P.sum_nq * stride;
+  std::vector<double> dev(ng, 0.0);
+  std::vector<float> dev32(ng, 0.0f);
+  for (const TermDesc& T : P.terms)
+    for (int64_t qp = 0; qp < T.NQ; ++qp) {
+      const int64_t iq = P.grid_perm[(size_t)T.off_nq + qp];  // the reference's point
+      const double* Gq = G + (size_t)iq * D * D;
+      const size_t row = (size_t)(T.off_nq + qp) * stride;
+      int e = 0;
+      for (int i = 0; i < T.D; ++i)
+        for (int j = i; j < T.D; ++j, ++e) {
+          dev[row + e] = Gq[T.perm[i] + (size_t)D * T.perm[j]];
+          dev32[row + e] = (float)dev[row + e];
+        }
+    }
+  // an H.psi still reading the old table may run on a caller's stream: wait for the device
+  EVR_CU(cudaDeviceSynchronize(), "sync before G table update");
+  if (!c->dp_ggrid || !c->dp_ggrid32) {  // a context made with constant G gets its table now
+    cudaError_t e = cudaSuccess;
+    if (!c->dp_ggrid) e = cudaMalloc((void**)&c->dp_ggrid, ng * sizeof(double));
+    if (e == cudaSuccess && !c->dp_ggrid32) e = cudaMalloc((void**)&c->dp_ggrid32, ng * sizeof(float));
+    if (e != cudaSuccess) {
+      if (c->dp_ggrid) cudaFree(c->dp_ggrid);
+      if (c->dp_ggrid32) cudaFree(c->dp_ggrid32);
+      c->dp_ggrid = nullptr;
+      c->dp_ggrid32 = nullptr;
+      EVR_CU(e, "cudaMalloc G table");
+    }
+  }
+  EVR_CU(cudaMemcpyAsync(c->dp_ggrid, dev.data(), ng * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+         "copy G table");
+  EVR_CU(cudaMemcpyAsync(c->dp_ggrid32, dev32.data(), ng * sizeof(float), cudaMemcpyHostToDevice, c->stream),
+         "copy G table (FP32)");
+  EVR_CU(cudaStreamSynchronize(c->stream), "sync");
+  return EVR_OK;
+}
+
 int evr_set_kernel_path(evr_ctx* c, int path) {
   if (!c) return EVR_EINVAL;
   if (path < 0 || path > 2) return set_error(c, EVR_EINVAL, "evr_set_kernel_path: 0, 1 or 2");

@@ -64,7 +64,7 @@ EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_
            "evr_davidson",
            "evr_cheby_propagate", "evr_fma_peak", "evr_hpsi_noalloc", "evr_set_dipole", "evr_set_field",
            "evr_oc_forward", "evr_oc_backward", "evr_create_batch", "evr_batch_offsets", "evr_batch_davidson", "evr_autotune",
-           "evr_psi_write", "evr_psi_read", "evr_set_vgrid", "evr_set_dipole_grid",
+           "evr_psi_write", "evr_psi_read", "evr_set_vgrid", "evr_set_dipole_grid", "evr_set_ggrid",
            "evr_sil_propagate", "evr_restart_write", "evr_restart_read", "evr_autocorr_write",
            "evr_autocorr_read"]
 VGRID_LAYOUT = {"terms": 0, "ref": 1}
@@ -98,6 +98,7 @@ def load(build: bool = True):
     L.evr_get_vgrid.argtypes = [vp, _dp]
     L.evr_set_vgrid.argtypes = [vp, _dp, C.c_int]
     L.evr_set_dipole_grid.argtypes = [vp, _dp, C.c_int]
+    L.evr_set_ggrid.argtypes = [vp, _dp]
     L.evr_hpsi_host.argtypes = [vp, _dp, C.c_int64, _dp, C.c_int64, C.c_int, C.c_int, C.c_int]
     L.evr_hpsi_device.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.c_int, C.c_int, C.c_int, vp]
     L.evr_last_launch_count.argtypes = [vp, _lp, _lp]
@@ -399,6 +400,13 @@ class Problem:
         idx = _iarr(np.asarray(idx).reshape(-1, 4))
         elec = _iarr(np.zeros((len(coef), 2)) if elec is None else np.asarray(elec).reshape(-1, 2))
         self._check(load().evr_set_dipole(self.h, len(coef), _p(coef, _dp), _p(idx, _ip), _p(elec, _ip)))
+
+    def set_ggrid(self, G):
+        """Kinetic metric G(Q) per grid point (sum_nq x D x D, the reference's point order) in
+        place of G0 + g.Q (type-10 contexts)."""
+        D = self.spec.D
+        G = np.ascontiguousarray(np.asarray(G, dtype=np.float64).reshape(self.sum_nq, D, D).transpose(0, 2, 1))
+        self._check(load().evr_set_ggrid(self.h, _p(G, _dp)))
 
     def set_dipole_grid(self, mu, layout="terms"):
         """Dipole mu(Q) as grid values (layouts of set_vgrid) instead of monomials."""

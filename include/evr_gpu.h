@@ -127,6 +127,14 @@ int evr_get_vgrid(const evr_ctx *ctx, double *v);
 #define EVR_VGRID_TERMS 0
 #define EVR_VGRID_REF   1
 int evr_set_vgrid(evr_ctx *ctx, const double *v, int layout);
+/* The kinetic metric G(Q) as grid values, for a type-10 context: what Tnum's get_d0GG gives
+ * at each grid point (Source_ElVibRot/sub_Operator/sub_OpPsi_SG4.f90:2717-2728, where the
+ * reference recomputes it on every H.psi), in place of G0 + sum_k g_ijk Q_k.  G: sum_nq
+ * symmetric D x D matrices, point iq (the reference's whole-grid order, as EVR_VGRID_REF)
+ * at G + iq*D*D, column-major; only i <= j is read.  The operator stays
+ * -1/2 sum_ij d_i G_ij(Q) d_j (Jacobian and rho constant).  A context created with a
+ * constant G gets its per-point table here.  Synchronous; a set-up call; not for batches. */
+int evr_set_ggrid(evr_ctx *ctx, const double *G);
 
 /* H.psi on a block of vectors.
  * Replaces sub_TabOpPsi (Source_ElVibRot/sub_Operator/sub_OpPsi.f90:701-795) on SG4,

@@ -100,3 +100,26 @@ def test_set_dipole_grid_matches_monomial_dipole():
     Ja = pa.oc_forward(field, psi0, target, 10.0, w[0] - 1e-3, w[-1] + 1e-3)[0]
     Jb = pb.oc_forward(field, psi0, target, 10.0, w[0] - 1e-3, w[-1] + 1e-3)[0]
     assert abs(Ja - Jb) <= 1e-12
+
+
+def _g_linear(spec, Q):
+    """G(Q) = G0 + sum_k g[:, :, k] Q_k at the points Q (npoints x D)."""
+    return np.asarray(spec.G0)[None] + np.einsum("ijk,qk->qij", np.asarray(spec.g), Q)
+
+
+@pytest.mark.parametrize("mk", [lambda: S.config_sg4(4, 5, seed=5), lambda: S.config_dp3(nb=6, nq=8)],
+                         ids=["sg4_term_kernels", "dp_stage_kernels"])
+def test_set_ggrid_matches_the_linear_model(mk):
+    """evr_set_ggrid: a context made with constant G, given G(Q) = G0 + g.Q as grid values,
+    applies the same H as the context that evaluated that model itself."""
+    from test_host_tables import grid_points
+    spec = mk()
+    pa = E.Problem(spec)
+    pb = E.Problem(dataclasses.replace(spec, g=np.zeros_like(np.asarray(spec.g))))  # no G table yet
+    G = _g_linear(spec, grid_points(pb, spec))
+    psi = np.random.default_rng(8).standard_normal((pa.N, 5))
+    ref64, ref32 = pa.hpsi(psi), pa.hpsi(psi, prec="fp32")
+    assert rel(pb.hpsi(psi), ref64) > 1e-6  # constant G differs before the update
+    pb.set_ggrid(G)
+    assert rel(pb.hpsi(psi), ref64) <= FP64_TOL
+    assert rel(pb.hpsi(psi, prec="fp32"), ref32) <= FP32_TOL

@@ -104,3 +104,43 @@ def test_pyrazine_builders_agree():
     for k in ("D", "nb0", "LG", "LB", "Aq", "Bq", "Ab", "Bb", "mono_coef", "mono_idx", "mono_elec", "keo_type",
               "G0", "g"):
         assert np.array_equal(np.asarray(getattr(a, k)), np.asarray(getattr(b, k))), k
+
+
+def test_set_ggrid_argument_checks():
+    pt = E.Problem(S.config_sg4(3, 2, seed=1), device=-1)  # type 10
+    with pytest.raises(E.EvrError) as ei:
+        pt.set_ggrid(np.zeros((pt.sum_nq, 3, 3)))
+    assert ei.value.code == E.EVR_EDEVICE
+    p1 = E.Problem(S.henon_heiles(3, 2), device=-1)  # type 1: no G table to set
+    with pytest.raises(E.EvrError) as ei:
+        p1.set_ggrid(np.zeros((p1.sum_nq, 3, 3)))
+    assert ei.value.code == E.EVR_EINVAL
+
+
+def grid_points(pg, spec):
+    """Coordinates Q (sum_nq x D) of every grid point in the reference's order: terms in
+    order, first mode fastest inside a term, at the scaled nodes of each (mode, level)."""
+    term_l = pg.tables()["term_l"]
+    out = []
+    for t in range(pg.nterm):
+        xs = [pg.basis(d, int(term_l[t, d]))["x"] for d in range(spec.D)]
+        idx = np.indices([len(x) for x in xs]).reshape(spec.D, -1, order="F")
+        out.append(np.stack([xs[d][idx[d]] for d in range(spec.D)], axis=1))
+    return np.concatenate(out)
+
+
+def test_grid_points_reproduce_the_oracle_potential_grid():
+    """The coordinates the G-table GPU test evaluates G(Q) at are the grid's: the potential's
+    monomials at them give the oracle's V grid."""
+    for spec in (S.config_sg4(4, 5, seed=5), S.config_dp3(nb=6, nq=8)):
+        pg = E.Problem(spec, device=-1)
+        Q = grid_points(pg, spec)
+        v = np.zeros(len(Q))
+        for c, ix in zip(spec.mono_coef, np.asarray(spec.mono_idx).reshape(-1, 4)):
+            term = np.full(len(Q), c)
+            for i in ix:
+                if i >= 0:
+                    term = term * Q[:, i]
+            v += term
+        ref = O.OracleProblem(spec).vgrid()
+        assert np.abs(v - ref).max() <= 1e-13 * np.abs(ref).max()
