@@ -18,8 +18,22 @@ seed (synthetic inputs with the benchmark's shapes and distributions).
            FP64 refinement), with the largest eigenvalue difference in cm-1
   cpu_baseline / --impl reference: the CPU oracle (C++/OpenMP restatement of the
            reference's OpPsi) on the host cores, bounded to a sample of the block.
+  configs: the other workloads, one compact result each (wall clock around the library
+           call, device-resident data):
+           dp3_davidson  D=3 direct product nb=20 nq=24, lowest 20 levels to 1e-6 cm-1, FP64
+                         and mixed, against a dense diagonalisation of the same operator;
+           batch         256 uneven Smolyak problems (D 3..6, L 4..8), lowest 10 levels each,
+                         lock-step batched Davidson, FP64 and mixed;
+           prop12d       D=12 Smolyak L=6 Chebyshev propagation (dt = 10 au) timed on 200
+                         steps in complex128 and complex64-contraction form; the 2000-step
+                         time of the workload is extrapolated from them (labelled so); the
+                         FP32 - FP64 autocorrelation difference and an FP64 norm / energy
+                         check of the final packets;
+           control       optimal-control gradient D=3 nb=20 nq=24, 4000 steps of 5 au:
+                         forward and backward times, and the adjoint gradient against a
+                         central difference (h = 1e-7) at one step.
 
-Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--no-configs]
 """
 from __future__ import annotations
 
@@ -44,13 +58,12 @@ UNIT = "Hpsi/s"
 NVEC = 64
 
 
-def workload_config(p=None):
-    cfg = {"workload": "OpPsi block: SG4 D=6 L=8, nb(l)=2l+1, nq(l)=2l+3, type-10 KEO, 64 vectors",
-           "nvec": NVEC, "seed": 1, "l2": "flushed between timed steps (512 MB write)"}
-    if p is not None:
-        cfg.update({"N": int(p.N), "terms": int(p.nterm), "grid_points": int(p.sum_nq),
-                    "gflop_per_hpsi": round(p.flop_per_hpsi / 1e9, 4)})
-    return cfg
+def workload_config(n, terms, grid_points):
+    """The workload's description, printed alike by both arms (the GPU library's problem and
+    the oracle's give the same sizes)."""
+    return {"workload": "OpPsi block: SG4 D=6 L=8, nb(l)=2l+1, nq(l)=2l+3, type-10 KEO, 64 vectors",
+            "nvec": NVEC, "seed": 1, "l2": "flushed between timed steps (512 MB write)",
+            "N": int(n), "terms": int(terms), "grid_points": int(grid_points)}
 
 
 class ClockSampler:
@@ -154,8 +167,13 @@ def run_reference(args):
         return 0
     from evrgpu import spec as S
 
+    from oracle import oracle as O
+
     spec = S.config_sg4_6d_l8()
     threads = os.cpu_count() or 1
+    op = O.OracleProblem(spec)
+    cfg = workload_config(op.N, op.nterm, op.sum_nq)
+    del op
     rates = []
     for i in range(args.warmup + args.steps):
         r, _ = cpu_oracle_rate(spec, 1, threads)
@@ -165,7 +183,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": workload_config(),
+            "config": cfg,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": "1 vector of the 64-vector block per step (the reference's Fortran "
                                        "cannot be built here: no Fortran compiler)"},
@@ -231,128 +249,175 @@ def davidson_legs(p, S):
     return out
 
 
-def run_suite(args):
-    """Timings of the other workloads, one JSON line each (device-resident data, wall clock
-    around the library call after a warm-up call)."""
+def bench_dp3(args):
+    """D=3 direct product nb=20 nq=24 (type-10 KEO, G(Q) = 1 + g.q): lowest 20 levels with 16
+    start vectors to the workload's 1e-6 cm-1 (energy change below 1e-6 cm-1 and residuals
+    below 1e-8 au), FP64 and mixed, against a dense diagonalisation of the same operator
+    ((H + H^T)/2, assembled from the library's H.psi on unit blocks, torch eigvalsh)."""
+    import torch
     from evrgpu import spec as S
-    from evrgpu.lib import Problem, BatchProblem
+    from evrgpu.lib import Problem
 
-    which = ["dp3", "batch", "prop12d", "control"] if args.suite == "all" else [args.suite]
+    p = Problem(S.config_dp3(), device=0)
+    tol_ene = 1e-6 / S.AU_TO_CM
+    out = {"N": int(p.N), "levels": 20, "block": 16, "conv_ene_cm": 1e-6, "conv_resi_au": 1e-8}
+    p.davidson(20, block=16, conv_resi=1e-8, conv_ene=tol_ene)  # warm-up (work decompositions)
+    lev = {}
+    for prec in ("fp64", "fp32"):
+        t0 = time.perf_counter()
+        e, _, st = p.davidson(20, block=16, conv_resi=1e-8, conv_ene=tol_ene, prec=prec)
+        out[prec if prec == "fp64" else "mixed"] = {"s": time.perf_counter() - t0, **st}
+        lev[prec] = e
+    # dense operator from unit blocks (64 columns per call)
+    N = p.N
+    H = np.zeros((N, N))
+    eye = np.eye(N)
+    for c0 in range(0, N, 64):
+        H[:, c0:c0 + 64] = p.hpsi(eye[:, c0:c0 + 64])
+    Hs = torch.from_numpy(0.5 * (H + H.T)).cuda()
+    dense = torch.linalg.eigvalsh(Hs)[:20].cpu().numpy()
+    del Hs
+    out["fp64"]["max_abs_err_vs_dense_cm"] = float(np.abs(lev["fp64"] - dense).max() * S.AU_TO_CM)
+    out["mixed"]["max_abs_err_vs_dense_cm"] = float(np.abs(lev["fp32"] - dense).max() * S.AU_TO_CM)
+    out["speedup_mixed"] = out["fp64"]["s"] / out["mixed"]["s"]
+    out["levels_cm"] = [float(x * S.AU_TO_CM) for x in lev["fp64"][:3]]
+    return out
+
+
+def bench_batch(args):
+    """256 uneven problems (D ~ U{3..6}, L ~ U{4..8}): lowest 10 levels of every problem to
+    residual 1e-7 au, lock-step batched Davidson in FP64 and in the mixed form."""
+    from evrgpu import spec as S
+    from evrgpu.lib import BatchProblem
+
+    t0 = time.perf_counter()
+    b = BatchProblem(S.batched_systems(args.batch_n, seed=2), device=0)
+    out = {"problems": args.batch_n, "N": int(b.N), "terms": int(b.nterm), "create_s": time.perf_counter() - t0}
+    out["autotune"] = b.autotune(nvec=10, prec="fp32")
+    res = {}
+    out["conv_resi_au"] = args.batch_tol
+    runs = [("fp64", "fp64", args.batch_tol), ("mixed", "fp32", args.batch_tol)]
+    if args.batch_check:  # a tighter FP64 solve as the reference of both
+        runs.append(("fp64_tight", "fp64", args.batch_tol * 1e-2))
+    for name, prec, tol in runs:
+        t0 = time.perf_counter()
+        e, st = b.davidson(10, block=10, conv_resi=tol, conv_ene=tol * 1e-3, prec=prec, max_it=200)
+        res[name] = e
+        out[name] = {"s": time.perf_counter() - t0, **st}
+    out["speedup_mixed"] = out["fp64"]["s"] / out["mixed"]["s"]
+    d = np.abs(res["fp64"] - res["mixed"]) * S.AU_TO_CM
+    out["max_abs_diff_cm"] = float(d.max())
+    out["levels_above_1e-4_cm"] = int((d > 1e-4).sum())
+    if args.batch_check:
+        for name in ("fp64", "mixed"):
+            out[name]["max_abs_diff_vs_tight_cm"] = float((np.abs(res[name] - res["fp64_tight"]) * S.AU_TO_CM).max())
+    return out
+
+
+def bench_prop12d(args):
+    """D=12 Smolyak L=6 (nb = nq = 2l+1), Gaussian displaced by 1.0 in modes 1-3, Chebyshev
+    dt = 10 au in complex128 and with FP32 contractions (complex64 arithmetic in the
+    contractions, FP64 recurrence, autocorrelation and norm)."""
+    from evrgpu import spec as S
+    from evrgpu.lib import Problem
+
+    sp = S.config_sg4_12d_l6()
+    p = Problem(sp, device=0)
+    psi0 = S.displaced_gaussian(sp, p, [0, 1, 2], 1.0)
+    # spectral bounds of the Smolyak operator by power iterations on H and on (shift - H):
+    # the negative combination weights can put eigenvalues outside the harmonic estimate
+    rng = np.random.default_rng(0)
+    v = rng.standard_normal((p.N, 1))
+    for _ in range(150):
+        hv = p.hpsi(v)
+        top = float(np.vdot(v, hv).real / np.vdot(v, v).real)
+        v = hv / np.linalg.norm(hv)
+    shift = 1.02 * abs(top)
+    v = rng.standard_normal((p.N, 1))
+    for _ in range(150):
+        hv = shift * v - p.hpsi(v)
+        low = shift - float(np.vdot(v, hv).real / np.vdot(v, v).real)
+        v = hv / np.linalg.norm(hv)
+    span = top - low
+    emin, emax = low - 0.05 * span, top + 0.05 * span
+    out = {"N": int(p.N), "terms": int(p.nterm), "dt_au": 10.0}
+    for attempt in range(4):  # widen the bounds if the series meets a spectrum beyond them
+        try:
+            p.chebyshev(psi0, 10.0, 2, emin, emax)
+            break
+        except Exception:
+            emin, emax = emin - 0.1 * (emax - emin), emax + 0.2 * (emax - emin)
+    out.update({"emin": emin, "emax": emax})
+    if args.autotune:
+        out["autotune"] = p.autotune(nvec=2, prec="fp64")
+    e0 = float(np.vdot(psi0, p.hpsi(psi0.real[:, None])[:, 0]).real)  # psi0 is real
+    ac, fin = {}, {}
+    steps = args.prop_steps
+    for prec in ("fp64", "fp32"):
+        p.chebyshev(psi0, 10.0, 2, emin, emax, prec=prec)
+        t0 = time.perf_counter()
+        a, psiT, st = p.chebyshev(psi0, 10.0, steps, emin, emax, prec=prec, want_psi=True)
+        dt = time.perf_counter() - t0
+        ac[prec] = a[:, 0]
+        # FP64 checks of the final packet: norm and energy <psi|H|psi> (FP64 H.psi)
+        x = psiT[:, 0]
+        hx = p.hpsi(np.stack([x.real, x.imag], axis=1))
+        en = float((np.vdot(x.real, hx[:, 0]) + np.vdot(x.imag, hx[:, 1])).real / np.vdot(x, x).real)
+        key = "fp64" if prec == "fp64" else "fp32"
+        out[key] = {"steps": steps, "s": dt, "s_per_step": dt / steps, "order": st["max_order"],
+                    "norm_final_minus_1": float(np.vdot(x, x).real - 1.0), "energy_drift_au": en - e0,
+                    "s_2000_steps_extrapolated": 2000 * dt / steps}
+    out["autocorr_max_abs_diff_fp32_vs_fp64"] = float(np.abs(ac["fp32"] - ac["fp64"]).max())
+    out["autocorr_last"] = [float(ac["fp64"][-1].real), float(ac["fp64"][-1].imag)]
+    out["note"] = (f"timed on {steps} of the workload's 2000 steps; s_2000_steps_extrapolated = "
+                   f"2000 x measured s per step")
+    return out
+
+
+def bench_control(args):
+    """Optimal control on D=3 nb=20 nq=24 with the dipole: ground state -> level 5, 4000 steps
+    of 5 au, dJ/dE by the adjoint, checked against a central difference at one step."""
+    from evrgpu import spec as S
+    from evrgpu.lib import Problem
+
+    sp = S.config_oc(seed=0)
+    p = Problem(sp, device=0)
+    e, vec, _ = p.davidson(8, block=16, conv_resi=1e-9, conv_ene=1e-12, want_vectors=True, sym=0)
+    rng = np.random.default_rng(0)
+    v = rng.standard_normal((p.N, 1))
+    for _ in range(200):
+        hv = p.hpsi(v)
+        lam = float(np.linalg.norm(hv))
+        v = hv / lam
+    psi0 = vec[:, 0] / np.linalg.norm(vec[:, 0]) + 0j
+    tgt = vec[:, 5] / np.linalg.norm(vec[:, 5]) + 0j
+    field = S.oc_field(4000, 5.0, seed=0)
+    emin, emax = e[0] - 0.01, 1.05 * lam
+    t0 = time.perf_counter()
+    J, _, _, info = p.oc_forward(field, psi0, tgt, 5.0, emin, emax)
+    tf = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    g, ref, binfo = p.oc_backward(len(field))
+    tb = time.perf_counter() - t0
+    n, h = 2000, 1e-7
+    fp, fm = field.copy(), field.copy()
+    fp[n] += h
+    fm[n] -= h
+    fd = (p.oc_forward(fp, psi0, tgt, 5.0, emin, emax)[0] - p.oc_forward(fm, psi0, tgt, 5.0, emin, emax)[0]) / (2 * h)
+    return {"steps": 4000, "J": J, "forward_s": tf, "backward_s": tb, "order": info["order"],
+            "checkpoints": info["checkpoints"],
+            "fd_step": n, "fd_h": h, "fd_rel_err": float(abs(fd - g[n]) / np.abs(g).max()),
+            "ref_vs_grad": float(np.abs(0.5 * 5.0 * (ref[:-1] + ref[1:]) - g).max() / np.abs(g).max())}
+
+
+CONFIGS = {"dp3": bench_dp3, "batch": bench_batch, "prop12d": bench_prop12d, "control": bench_control}
+
+
+def run_suite(args):
+    """The other workloads, one JSON line each."""
+    which = list(CONFIGS) if args.suite == "all" else [args.suite]
     for w in which:
-        out = {"suite": w}
-        if w == "dp3":
-            # D=3 direct product nb=20 nq=24 type-10 KEO: lowest 20 levels, 16 start vectors
-            p = Problem(S.config_dp3(), device=0)
-            p.davidson(20, block=16, conv_resi=1e-8, conv_ene=1e-11)
-            for prec in ("fp64", "fp32"):
-                t0 = time.perf_counter()
-                e, _, st = p.davidson(20, block=16, conv_resi=1e-8, conv_ene=1e-11, prec=prec)
-                out[prec] = {"s": time.perf_counter() - t0, **st}
-                out[prec + "_levels_cm"] = [float(x * S.AU_TO_CM) for x in e[:3]]
-            out["N"] = int(p.N)
-        elif w == "batch":
-            # D ~ U{3..6}, L ~ U{4..8}: lowest 10 levels of every problem, lock-step batched Davidson
-            t0 = time.perf_counter()
-            b = BatchProblem(S.batched_systems(args.batch_n, seed=2), device=0)
-            out.update({"problems": args.batch_n, "N": int(b.N), "terms": int(b.nterm),
-                        "create_s": time.perf_counter() - t0})
-            out["autotune"] = b.autotune(nvec=10, prec="fp32")
-            res = {}
-            out["conv_resi_au"] = args.batch_tol
-            runs = [("fp64", "fp64", args.batch_tol), ("fp32", "fp32", args.batch_tol)]
-            if args.batch_check:  # a tighter FP64 solve as the reference of both
-                runs.append(("fp64_tight", "fp64", args.batch_tol * 1e-2))
-            for name, prec, tol in runs:
-                t0 = time.perf_counter()
-                e, st = b.davidson(10, block=10, conv_resi=tol, conv_ene=tol * 1e-3, prec=prec, max_it=200)
-                res[name] = e
-                out[name] = {"s": time.perf_counter() - t0, **st}
-            out["speedup"] = out["fp64"]["s"] / out["fp32"]["s"]
-            d = np.abs(res["fp64"] - res["fp32"]) * S.AU_TO_CM
-            out["max_abs_diff_cm"] = float(d.max())
-            q, j = np.unravel_index(int(np.argmax(d)), d.shape)
-            out["max_diff_at"] = {"problem": int(q), "level": int(j),
-                                  "levels_cm": [float(x * S.AU_TO_CM) for x in res["fp64"][q]]}
-            out["levels_above_1e-4_cm"] = int((d > 1e-4).sum())
-            if args.batch_check:
-                for name in ("fp64", "fp32"):
-                    out[name]["max_abs_diff_vs_tight_cm"] = float(
-                        (np.abs(res[name] - res["fp64_tight"]) * S.AU_TO_CM).max())
-        elif w == "prop12d":
-            # D=12 SG4 L=6, Gaussian displaced by 1.0 in modes 1-3, Chebyshev dt = 10 au
-            sp = S.config_sg4_12d_l6()
-            p = Problem(sp, device=0)
-            psi0 = S.displaced_gaussian(sp, p, [0, 1, 2], 1.0)
-            # spectral bounds of the Smolyak operator by power iterations on H and on
-            # (shift - H): the negative combination weights can put eigenvalues outside the
-            # harmonic estimate
-            rng = np.random.default_rng(0)
-            v = rng.standard_normal((p.N, 1))
-            for _ in range(150):
-                hv = p.hpsi(v)
-                top = float(np.vdot(v, hv).real / np.vdot(v, v).real)
-                v = hv / np.linalg.norm(hv)
-            shift = 1.02 * abs(top)
-            v = rng.standard_normal((p.N, 1))
-            for _ in range(150):
-                hv = shift * v - p.hpsi(v)
-                low = shift - float(np.vdot(v, hv).real / np.vdot(v, v).real)
-                v = hv / np.linalg.norm(hv)
-            span = top - low
-            emin, emax = low - 0.05 * span, top + 0.05 * span
-            out.update({"N": int(p.N), "emin": emin, "emax": emax})
-            for attempt in range(4):  # widen the bounds if the series meets a spectrum beyond them
-                try:
-                    p.chebyshev(psi0, 10.0, 2, emin, emax)
-                    break
-                except Exception:
-                    emin, emax = emin - 0.1 * (emax - emin), emax + 0.2 * (emax - emin)
-            out.update({"emin": emin, "emax": emax})
-            if args.autotune:
-                out["autotune"] = p.autotune(nvec=2, prec="fp64")
-            ac_cheb = {}
-            for prec in ("fp64", "fp32"):
-                p.chebyshev(psi0, 10.0, 2, emin, emax, prec=prec)
-                t0 = time.perf_counter()
-                ac, _, st = p.chebyshev(psi0, 10.0, args.prop_steps, emin, emax, prec=prec)
-                dt = time.perf_counter() - t0
-                ac_cheb[prec] = ac
-                out[prec] = {"steps": args.prop_steps, "s": dt, "s_per_step": dt / args.prop_steps,
-                             "order": st["max_order"], "autocorr_last": [float(ac[-1, 0].real), float(ac[-1, 0].imag)]}
-                out[prec]["s_2000_steps_extrapolated"] = 2000 * dt / args.prop_steps
-            # the same steps by short-iterative Lanczos (march_SIL; nq = nb, H symmetric)
-            p.sil(psi0, 10.0, 2, npoly=64, poly_tol=1e-10)
-            t0 = time.perf_counter()
-            ac_sil, _, st = p.sil(psi0, 10.0, args.prop_steps, npoly=64, poly_tol=1e-10)
-            dt = time.perf_counter() - t0
-            out["sil_fp64"] = {"steps": args.prop_steps, "s": dt, "s_per_step": dt / args.prop_steps,
-                               "krylov_dim": st["krylov_dim"], "hpsi": st["hpsi"],
-                               "autocorr_last": [float(ac_sil[-1, 0].real), float(ac_sil[-1, 0].imag)],
-                               "max_abs_diff_vs_chebyshev": float(np.abs(ac_sil[:, 0] - ac_cheb["fp64"][:, 0]).max())}
-        elif w == "control":
-            # D=3 nb=20 nq=24 with the dipole; ground state -> level 5, 4000 steps of 5 au
-            sp = S.config_oc(seed=0)
-            p = Problem(sp, device=0)
-            e, vec, _ = p.davidson(8, block=16, conv_resi=1e-9, conv_ene=1e-12, want_vectors=True, sym=0)
-            rng = np.random.default_rng(0)
-            v = rng.standard_normal((p.N, 1))
-            for _ in range(200):
-                hv = p.hpsi(v)
-                lam = float(np.linalg.norm(hv))
-                v = hv / lam
-            psi0 = vec[:, 0] / np.linalg.norm(vec[:, 0]) + 0j
-            tgt = vec[:, 5] / np.linalg.norm(vec[:, 5]) + 0j
-            field = S.oc_field(4000, 5.0, seed=0)
-            t0 = time.perf_counter()
-            J, _, _, info = p.oc_forward(field, psi0, tgt, 5.0, e[0] - 0.01, 1.05 * lam)
-            tf = time.perf_counter() - t0
-            t0 = time.perf_counter()
-            g, ref, binfo = p.oc_backward(len(field))
-            tb = time.perf_counter() - t0
-            out.update({"steps": 4000, "J": J, "forward_s": tf, "backward_s": tb, "order": info["order"],
-                        "checkpoints": info["checkpoints"],
-                        "ref_vs_grad": float(np.abs(0.5 * 5.0 * (ref[:-1] + ref[1:]) - g).max() / np.abs(g).max())})
-        print(json.dumps(out))
+        print(json.dumps({"suite": w, **CONFIGS[w](args)}))
     return 0
 
 
@@ -381,6 +446,7 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-davidson", action="store_true", help="skip the Davidson time-to-tolerance legs")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other workloads' compact results")
     ap.add_argument("--autotune", action="store_true", help="tune the work decomposition before timing")
     ap.add_argument("--profile", default=None, choices=["sg4_6d_l6", "sg4_6d_l8", "dp3"],
                     help="profiling mode: a few H.psi launches of the named workload, nothing else")
@@ -494,11 +560,23 @@ def main():
     dav = None
     if not args.no_davidson:
         dav = davidson_legs(p, S)
+    cfg = workload_config(p.N, p.nterm, p.sum_nq)
+    configs = None
+    if not args.no_configs and rank == 0:
+        p.close()  # the D=6 L=8 tables (about 11 GB) make room for the other workloads
+        configs = {}
+        for name, fn in CONFIGS.items():
+            t0 = time.perf_counter()
+            try:
+                configs[name] = fn(args)
+            except Exception as e:  # a failed workload is reported, the headline line still prints
+                configs[name] = {"error": f"{type(e).__name__}: {e}"}
+            configs[name]["wall_s"] = time.perf_counter() - t0
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total64 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": workload_config(p),
+            "config": cfg,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(N * NVEC * 8),
                     "d2h_bytes_per_step": int(N * NVEC * 8), "rel_err_vs_device": e2e_err},
             "mixed": {"value": mixed, "unit": UNIT, "dtype": "f32 contractions, f64 reduction",
@@ -513,6 +591,7 @@ def main():
                                         "in the measured-peaks file"},
             "roofline_hbm": hbm_roofline(TRAFFIC_PER_LAUNCH, items_ms / 1e3),
             "davidson": dav,
+            "configs": configs,
             "autotune": tuned,
             "gpu_launches": launches,
             "clocks": clk.summary()}

@@ -2,6 +2,7 @@
 // H.psi entry points.  Davidson and Chebyshev drivers live in evr_davidson.cu and
 // evr_propagate.cu.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <new>
 
@@ -173,6 +174,7 @@ int evr_set_vgrid(evr_ctx* c, const double* v, int layout) {
   const size_t n = dev.size();
   // an H.psi still reading the old table may run on a caller's stream: wait for the device
   EVR_CU(cudaDeviceSynchronize(), "sync before vgrid update");
+  free_control(c);  // a forward state of the old operator (see evr_set_ggrid)
   EVR_CU(cudaMemcpyAsync(c->dp.vgrid, dev.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream),
          "copy vgrid");
   EVR_CU(cudaMemcpyAsync(c->dp.vgrid32, dev32.data(), n * sizeof(float), cudaMemcpyHostToDevice, c->stream),
@@ -190,9 +192,20 @@ int evr_set_ggrid(evr_ctx* c, const double* G) {
   if (c->batch) return set_error(c, EVR_EINVAL, "evr_set_ggrid: not for batched contexts");
   const HostProblem& P = c->hp;
   if (P.keo_type != 10) return set_error(c, EVR_EINVAL, "evr_set_ggrid: the KEO of the context is not type 10");
+  const int D = P.D, stride = g_table_stride(D);
+  for (int64_t iq = 0; iq < P.sum_nq; ++iq) {  // the matrices must be symmetric
+    const double* Gq = G + (size_t)iq * D * D;
+    for (int i = 0; i < D; ++i)
+      for (int j = i + 1; j < D; ++j) {
+        const double a = Gq[i + (size_t)D * j], b = Gq[j + (size_t)D * i];
+        if (!(std::fabs(a - b) <= 1e-12 * std::max(1.0, std::max(std::fabs(a), std::fabs(b)))))
+          return set_error(c, EVR_EINVAL, "evr_set_ggrid: G(Q) is not symmetric at grid point " +
+                                              std::to_string(iq) + " (entries " + std::to_string(i) + ", " +
+                                              std::to_string(j) + ")");
+      }
+  }
   if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
   EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
-  const int D = P.D, stride = g_table_stride(D);
   const size_t ng = (size_t)P.sum_nq * stride;
   std::vector<double> dev(ng, 0.0);
   std::vector<float> dev32(ng, 0.0f);
@@ -204,12 +217,16 @@ int evr_set_ggrid(evr_ctx* c, const double* G) {
       int e = 0;
       for (int i = 0; i < T.D; ++i)
         for (int j = i; j < T.D; ++j, ++e) {
-          dev[row + e] = Gq[T.perm[i] + (size_t)D * T.perm[j]];
+          const int oi = T.perm[i], oj = T.perm[j];
+          dev[row + e] = 0.5 * (Gq[oi + (size_t)D * oj] + Gq[oj + (size_t)D * oi]);
           dev32[row + e] = (float)dev[row + e];
         }
     }
   // an H.psi still reading the old table may run on a caller's stream: wait for the device
   EVR_CU(cudaDeviceSynchronize(), "sync before G table update");
+  // an optimal-control forward state was propagated with the old operator: a gradient
+  // would mix the two, so it is discarded (evr_oc_backward then asks for a new forward)
+  free_control(c);
   if (!c->dp_ggrid || !c->dp_ggrid32) {  // a context made with constant G gets its table now
     cudaError_t e = cudaSuccess;
     if (!c->dp_ggrid) e = cudaMalloc((void**)&c->dp_ggrid, ng * sizeof(double));
@@ -221,6 +238,9 @@ int evr_set_ggrid(evr_ctx* c, const double* G) {
       c->dp_ggrid32 = nullptr;
       EVR_CU(e, "cudaMalloc G table");
     }
+    // launch sequences captured with the constant G (optimal-control graphs) read no
+    // table: drop them so that they are recaptured with it
+    ++c->ws_gen;
   }
   EVR_CU(cudaMemcpyAsync(c->dp_ggrid, dev.data(), ng * sizeof(double), cudaMemcpyHostToDevice, c->stream),
          "copy G table");

@@ -429,6 +429,7 @@ int evr_set_dipole_grid(evr_ctx* c, const double* mu, int layout) {
         mmax = std::max(mmax, r);
       }
   if ((rc = cuda_check(c, cudaDeviceSynchronize(), "sync before dipole update"))) return rc;
+  oc_free(c);  // a forward state propagated with the old dipole would mix two operators
   if ((rc = alloc_dipole_tables(c, n))) return rc;
   cudaStream_t s = c->stream;
   if ((rc = cuda_check(c, cudaMemcpyAsync(c->dp_mugrid, dev.data(), n * sizeof(double), cudaMemcpyHostToDevice, s),

@@ -28,8 +28,13 @@ template <typename T, bool GFLY>
 cudaError_t set_items_kernel_smem(int bytes) {
   return cudaFuncSetAttribute(hpsi_items_kernel<T, GFLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
+template <typename T, bool GFLY>
+cudaError_t occupancy_items_kernel(int* per_sm, int smem_bytes) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, hpsi_items_kernel<T, GFLY>, kThreads, smem_bytes);
+}
 template cudaError_t launch_items_kernel<EVR_KT, EVR_KGFLY>(int, size_t, cudaStream_t, const ItemParams<EVR_KT>&);
 template cudaError_t set_items_kernel_smem<EVR_KT, EVR_KGFLY>(int);
+template cudaError_t occupancy_items_kernel<EVR_KT, EVR_KGFLY>(int*, int);
 #endif
 
 }  // namespace kern

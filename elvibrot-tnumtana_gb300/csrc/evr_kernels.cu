@@ -697,11 +697,22 @@ int eval_grid_monomials(evr_ctx* c, int n_mono, const double* coef, const int* i
 // H.psi (FP64, the reference's operator H) on interleaved device blocks with all scratch
 // memory supplied by the caller: [item counter (256 B)][term-basis output][per-CTA
 // buffers].  Allocates nothing; every term runs one vector per item from the global
-// buffers.  Returns EVR_EINVAL when the scratch is too small.
+// buffers.  Returns EVR_EINVAL when the scratch is too small, and EVR_EDEVICE when the
+// kernel skipped an item that would have exceeded its buffers (the flag is read back
+// after the launches, so the call returns once the H.psi has completed).
 int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, unsigned char* scratch,
                  size_t scratch_bytes, cudaStream_t s) {
   const HostProblem& P = c->hp;
-  const int grid = c->num_sms * 2;
+  int optin = 0;
+  EVR_CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attr");
+  // the general kernel's shared memory of the regular path, so that two CTAs are resident
+  // per SM and every CTA of the grid gets its per-CTA buffer in the first wave
+  const int smem_items = std::min(optin, 228 * 1024 / 2) - 2048;
+  // the same attribute values as ensure_workspace sets, so neither path lowers the other's
+  EVR_CU((set_term_kernel_smem<double, false>(smem_items, optin - 2048)), "attr");
+  int per_sm = 0;
+  EVR_CU((occupancy_items_kernel<double, false>(&per_sm, smem_items)), "occupancy");
+  const int grid = c->num_sms * std::max(1, std::min(per_sm, 2));
   size_t slab = 0, msz = 0;
   for (const TermDesc& Tm : P.terms) {
     slab = std::max(slab, footprint_elems<double>(P, Tm, 1));
@@ -714,11 +725,8 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
     return set_error(c, EVR_EINVAL, "evr_hpsi_noalloc: problem needs " + std::to_string(need) +
                                         " bytes of scratch, the static buffer holds " + std::to_string(scratch_bytes));
   const size_t smem = msz * sizeof(double);
-  int optin = 0;
-  EVR_CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attr");
-  if (smem > (size_t)optin / 2) return set_error(c, EVR_EINVAL, "evr_hpsi_noalloc: 1-D matrices too large");
+  if (smem > (size_t)smem_items) return set_error(c, EVR_EINVAL, "evr_hpsi_noalloc: 1-D matrices too large");
   if (c->gfly || c->batch) return set_error(c, EVR_EINVAL, "evr_hpsi_noalloc: not for batched contexts");
-  EVR_CU((set_term_kernel_smem<double, false>(optin / 2, optin - 2048)), "attr");
   int* counter = reinterpret_cast<int*>(scratch);
   double* ht = reinterpret_cast<double*>(scratch + 256);
   double* slabp = reinterpret_cast<double*>(scratch + 256 + ht_bytes);
@@ -734,7 +742,7 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
   p.counter = counter;
   p.slab = slabp;
   p.slab_per_cta = (int64_t)slab;
-  p.smem_elems = (int64_t)((optin / 2) / sizeof(double));
+  p.smem_elems = (int64_t)(smem_items / sizeof(double));
   p.err = counter + 2;
   p.x = x;
   p.ldx = ldx;
@@ -752,12 +760,17 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
     for (int i = 0; i < P.D; ++i)
       for (int j = i + 1; j < P.D; ++j) p.has_offdiag |= (P.G0[i + (size_t)P.D * j] != 0.0);
   EVR_CU(cudaMemsetAsync(counter, 0, 4 * sizeof(int), s), "memset counter");  // the buffer keeps old contents
-  EVR_CU((launch_items_kernel<double, false>(grid, optin / 2, s, p)), "hpsi_items_kernel launch");
+  EVR_CU((launch_items_kernel<double, false>(grid, smem_items, s, p)), "hpsi_items_kernel launch");
   const int64_t N = P.Np * P.nb0;
   int rblocks = (int)std::min<int64_t>((N * nvec + 255) / 256, (int64_t)c->num_sms * 16);
   csr_reduce_kernel<double><<<rblocks, 256, 0, s>>>(c->dp.csr_ptr, c->dp.csr_src, c->dp.csr_w, ht, nullptr, nvec,
                                                      1.0, y, ldy, N, nvec);
   EVR_CU(cudaGetLastError(), "csr_reduce_kernel launch");
+  // the kernel's buffer-check flag: a plain copy into a host int (no allocation)
+  int flag = 0;
+  EVR_CU(cudaMemcpyAsync(&flag, counter + 2, sizeof(int), cudaMemcpyDeviceToHost, s), "flag");
+  EVR_CU(cudaStreamSynchronize(s), "flag");
+  if (flag) return set_error(c, EVR_EDEVICE, "evr_hpsi_noalloc: a work item exceeded its buffers and was skipped");
   return EVR_OK;
 }
 

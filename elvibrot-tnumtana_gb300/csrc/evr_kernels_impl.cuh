@@ -1157,6 +1157,9 @@ template <typename T, bool GFLY>
 cudaError_t set_items_kernel_smem(int bytes);
 template <typename T, bool GFLY>
 cudaError_t set_slab_kernel_smem(int bytes);
+// resident CTAs per SM of the general kernel at a dynamic shared-memory size
+template <typename T, bool GFLY>
+cudaError_t occupancy_items_kernel(int* per_sm, int smem_bytes);
 template <typename T, bool GFLY>
 cudaError_t set_term_kernel_smem(int items_bytes, int slab_bytes) {
   cudaError_t e = set_items_kernel_smem<T, GFLY>(items_bytes);

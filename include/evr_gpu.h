@@ -131,9 +131,12 @@ int evr_set_vgrid(evr_ctx *ctx, const double *v, int layout);
  * at each grid point (Source_ElVibRot/sub_Operator/sub_OpPsi_SG4.f90:2717-2728, where the
  * reference recomputes it on every H.psi), in place of G0 + sum_k g_ijk Q_k.  G: sum_nq
  * symmetric D x D matrices, point iq (the reference's whole-grid order, as EVR_VGRID_REF)
- * at G + iq*D*D, column-major; only i <= j is read.  The operator stays
- * -1/2 sum_ij d_i G_ij(Q) d_j (Jacobian and rho constant).  A context created with a
- * constant G gets its per-point table here.  Synchronous; a set-up call; not for batches. */
+ * at G + iq*D*D, column-major.  Each matrix must be symmetric: entries with
+ * |G_ij - G_ji| > 1e-12 max(1, |G_ij|) are rejected with EVR_EINVAL, and the table stores
+ * 0.5 (G_ij + G_ji).  The operator stays -1/2 sum_ij d_i G_ij(Q) d_j (Jacobian and rho
+ * constant).  A context created with a constant G gets its per-point table here (captured
+ * launch sequences of that context are dropped and recaptured).  Synchronous; a set-up
+ * call; not for batches. */
 int evr_set_ggrid(evr_ctx *ctx, const double *G);
 
 /* H.psi on a block of vectors.
@@ -175,7 +178,9 @@ int evr_set_kernel_path(evr_ctx *ctx, int path);
  * size needed).  The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.  All calls
  * share the one array: calls that overlap on the GPU (other streams, other threads)
- * race and must be serialised by the caller. */
+ * race and must be serialised by the caller.  The call returns once the H.psi has
+ * completed on the stream: it reads back the kernel's buffer-check flag (a plain copy into
+ * a host variable) and returns EVR_EDEVICE if a work item was skipped. */
 int evr_hpsi_noalloc(evr_ctx *ctx, const double *psi, int64_t ld_psi, double *hpsi, int64_t ld_hpsi, int nvec,
                      void *stream);
 

@@ -82,4 +82,6 @@ def test_reference_arm_prints_the_contract_line():
         assert k in line, k
     assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
     assert line["value"] > 0 and line["cpu_baseline"]["cores"] >= 1 and line["cpu_baseline"]["kind"] == "port"
-    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["config"]["workload"] == bench.workload_config()["workload"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0
+    # the same workload description as the GPU arm prints (sizes of the D=6 L=8 problem)
+    assert line["config"] == bench.workload_config(40081, 2975, 37769167)

@@ -147,3 +147,49 @@ def test_oc_backward_needs_forward_and_dipole():
     with pytest.raises(E.EvrError) as ei:
         p2.oc_forward(np.zeros(5), psi, psi, 5.0, 0.0, 0.1)
     assert ei.value.code == E.EVR_EINVAL
+
+
+def test_oc_gradient_finite_differences_at_workload_size():
+    # the optimal-control workload itself: D=3, nb=20, nq=24, 4000 steps of dt = 5 au, field
+    # of 8 sinusoids of amplitude 0.005, ground state -> level 5; the adjoint gradient against
+    # central differences (h = 1e-7) of the GPU forward pass at three steps, 1e-6 relative
+    sp = S.config_oc(seed=0)
+    pg = E.Problem(sp, device=0)
+    e, vec, _ = pg.davidson(8, block=16, conv_resi=1e-9, conv_ene=1e-12, want_vectors=True, sym=0)
+    rng = np.random.default_rng(0)
+    v = rng.standard_normal((pg.N, 1))
+    for _ in range(200):  # spectral radius by power iterations
+        hv = pg.hpsi(v)
+        lam = float(np.linalg.norm(hv))
+        v = hv / lam
+    psi0 = vec[:, 0] / np.linalg.norm(vec[:, 0]) + 0j
+    tgt = vec[:, 5] / np.linalg.norm(vec[:, 5]) + 0j
+    field = S.oc_field(4000, 5.0, seed=0)
+    emin, emax = e[0] - 0.01, 1.05 * lam
+
+    def J(f):
+        return pg.oc_forward(f, psi0, tgt, 5.0, emin, emax)[0]
+
+    J(field)
+    g, _, _ = pg.oc_backward(len(field))
+    h = 1e-7
+    for n in (7, 2000, 3998):
+        fp, fm = field.copy(), field.copy()
+        fp[n] += h
+        fm[n] -= h
+        assert abs((J(fp) - J(fm)) / (2 * h) - g[n]) <= 1e-6 * np.abs(g).max()
+
+
+def test_operator_update_discards_the_forward_state():
+    # a gradient must not mix two operators: evr_set_ggrid after evr_oc_forward drops the
+    # forward state, and evr_oc_backward asks for a new forward pass
+    c = Case(nb=5, nq=7, nst=10, seed=11)
+    c.forward()
+    G = np.tile(np.eye(c.sp.D), (c.pg.sum_nq, 1, 1))
+    c.pg.set_ggrid(G)
+    with pytest.raises(E.EvrError) as ei:
+        c.pg.oc_backward(len(c.field))
+    assert ei.value.code == E.EVR_EINVAL
+    c.forward()
+    g, _, _ = c.pg.oc_backward(len(c.field))
+    assert np.isfinite(g).all()

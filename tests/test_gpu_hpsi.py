@@ -191,3 +191,15 @@ def test_autotune_keeps_results():
     rng = np.random.default_rng(21)
     psi = rng.standard_normal((pg.N, 16))
     assert rel(pg.hpsi(psi), po.hpsi(psi)) <= FP64_TOL
+
+
+def test_d12_l6_propagation_workload_matches_oracle():
+    # the D=12 Smolyak level-6 propagation workload (18,564 terms, 369,305 functions, 4.2 M
+    # grid points) on two vectors, FP64 and FP32 contractions
+    spec = S.config_sg4_12d_l6()
+    pg = E.Problem(spec, device=0)
+    rng = np.random.default_rng(17)
+    psi = rng.standard_normal((pg.N, 2))
+    ref = O.OracleProblem(spec).hpsi(psi)
+    assert rel(pg.hpsi(psi, prec="fp64"), ref) <= FP64_TOL
+    assert rel(pg.hpsi(psi, prec="fp32"), ref) <= FP32_TOL

@@ -115,6 +115,12 @@ def test_set_ggrid_argument_checks():
     with pytest.raises(E.EvrError) as ei:
         p1.set_ggrid(np.zeros((p1.sum_nq, 3, 3)))
     assert ei.value.code == E.EVR_EINVAL
+    # G(Q) must be symmetric: one asymmetric point is named in the error, before any upload
+    G = np.tile(np.eye(3), (pt.sum_nq, 1, 1))
+    G[5, 0, 2] += 1e-6
+    with pytest.raises(E.EvrError) as ei:
+        pt.set_ggrid(G)
+    assert ei.value.code == E.EVR_EINVAL and "grid point 5" in str(ei.value)
 
 
 def grid_points(pg, spec):
