@@ -250,6 +250,66 @@ int evr_set_ggrid(evr_ctx* c, const double* G) {
   return EVR_OK;
 }
 
+// Jacobian and rho of a type-10 operator per grid point (the reference's point order):
+// stored as (Jac, sqrt(rho/Jac)) rows in the device's point order, FP64 and FP32.  Null
+// arrays remove the table (Jac = rho = 1).
+int evr_set_jacobian(evr_ctx* c, const double* jac, const double* rho) {
+  if (!c) return EVR_EINVAL;
+  if (c->batch) return set_error(c, EVR_EINVAL, "evr_set_jacobian: not for batched contexts");
+  const HostProblem& P = c->hp;
+  if (P.keo_type != 10) return set_error(c, EVR_EINVAL, "evr_set_jacobian: the KEO of the context is not type 10");
+  if ((jac == nullptr) != (rho == nullptr))
+    return set_error(c, EVR_EINVAL, "evr_set_jacobian: give both Jac and rho, or neither");
+  if (jac)
+    for (int64_t iq = 0; iq < P.sum_nq; ++iq)
+      if (!(jac[iq] > 0.0) || !(rho[iq] > 0.0) || !std::isfinite(jac[iq]) || !std::isfinite(rho[iq]))
+        return set_error(c, EVR_EINVAL, "evr_set_jacobian: Jac and rho must be positive and finite (grid point " +
+                                            std::to_string(iq) + ")");
+  if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
+  EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
+  EVR_CU(cudaDeviceSynchronize(), "sync before Jacobian update");
+  free_control(c);  // a forward state of the old operator (see evr_set_ggrid)
+  if (!jac) {
+    if (c->dp_jgrid) cudaFree(c->dp_jgrid);
+    if (c->dp_jgrid32) cudaFree(c->dp_jgrid32);
+    c->dp_jgrid = nullptr;
+    c->dp_jgrid32 = nullptr;
+    clear_item_sets(c);
+    free_stages(c);
+    return EVR_OK;
+  }
+  const size_t n = (size_t)P.sum_nq * 2;
+  std::vector<double> dev(n);
+  std::vector<float> dev32(n);
+  for (const TermDesc& T : P.terms)
+    for (int64_t qp = 0; qp < T.NQ; ++qp) {
+      const int64_t iq = P.grid_perm[(size_t)T.off_nq + qp];
+      const size_t r = (size_t)(T.off_nq + qp) * 2;
+      dev[r] = jac[iq];
+      dev[r + 1] = std::sqrt(rho[iq] / jac[iq]);
+      dev32[r] = (float)dev[r];
+      dev32[r + 1] = (float)dev[r + 1];
+    }
+  if (!c->dp_jgrid) {
+    cudaError_t e = cudaMalloc((void**)&c->dp_jgrid, n * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->dp_jgrid32, n * sizeof(float));
+    if (e != cudaSuccess) {
+      if (c->dp_jgrid) cudaFree(c->dp_jgrid);
+      c->dp_jgrid = nullptr;
+      c->dp_jgrid32 = nullptr;
+      EVR_CU(e, "cudaMalloc Jacobian table");
+    }
+    clear_item_sets(c);  // every term moves to the general kernel
+    free_stages(c);
+  }
+  EVR_CU(cudaMemcpyAsync(c->dp_jgrid, dev.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+         "copy Jacobian table");
+  EVR_CU(cudaMemcpyAsync(c->dp_jgrid32, dev32.data(), n * sizeof(float), cudaMemcpyHostToDevice, c->stream),
+         "copy Jacobian table (FP32)");
+  EVR_CU(cudaStreamSynchronize(c->stream), "sync");
+  return EVR_OK;
+}
+
 int evr_set_kernel_path(evr_ctx* c, int path) {
   if (!c) return EVR_EINVAL;
   if (path < 0 || path > 2) return set_error(c, EVR_EINVAL, "evr_set_kernel_path: 0, 1 or 2");
@@ -261,6 +321,22 @@ int evr_set_kernel_path(evr_ctx* c, int path) {
       cudaSetDevice(c->device);
       cudaStreamSynchronize(c->stream);
       free_workspace(c);  // work decompositions depend on the path
+    }
+  }
+  return EVR_OK;
+}
+
+int evr_set_tensor_cores(evr_ctx* c, int on, int min_km) {
+  if (!c) return EVR_EINVAL;
+  if (min_km < 0) return set_error(c, EVR_EINVAL, "evr_set_tensor_cores: min_km < 0");
+  const bool tc = on != 0;
+  if (c->use_tc != tc || c->tc_min_km != min_km) {
+    c->use_tc = tc;
+    c->tc_min_km = min_km;
+    if (!c->host_only) {
+      cudaSetDevice(c->device);
+      cudaStreamSynchronize(c->stream);
+      clear_item_sets(c);  // FP32 work decompositions depend on the shared memory left
     }
   }
   return EVR_OK;

@@ -12,7 +12,7 @@
 
 namespace evr {
 
-constexpr int kMaxD = 16;      // modes
+constexpr int kMaxD = 24;      // modes (positions of a term and modes of a problem)
 // G(Q) table: point-major, the D(D+1)/2 symmetric entries of a point padded to a multiple
 // of four (16-byte rows in FP32, 32-byte in FP64) so that a point's row loads as vectors
 __host__ __device__ constexpr int g_table_stride(int D) { return (D * (D + 1) / 2 + 3) & ~3; }
@@ -190,7 +190,9 @@ struct evr_ctx {
   bool host_only = false;           // created with device < 0: tables only
   int op_form = 0;                  // EVR_OP_H, EVR_OP_HT or EVR_OP_HSYM
   bool capturing = false;           // inside a stream capture: no event records
-  bool use_slab = true;             // slab kernel for the terms that fit (EVR_NO_SLAB=1 disables)
+  bool use_slab = true;             // slab kernel for the terms that fit (evr_set_kernel_path)
+  bool use_tc = true;               // FP32 slab-kernel contractions on the tensor cores (evr_set_tensor_cores)
+  int tc_min_km = 64;               // contractions with K*M below this stay on the CUDA cores
   bool use_stages = true;           // grid-wide stage path for single-term problems
   bool gfly = false;                // G(Q) from the linear model per point instead of a table
   int vt_cap_slab = 32, vt_cap_items = 32;  // widest vector tile of an item (evr_autotune)
@@ -208,6 +210,8 @@ struct evr_ctx {
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // around the items kernel and the reduction
   double* dp_ggrid = nullptr;      // symmetric G(Q) on the grid (type 10 with g != 0)
   float* dp_ggrid32 = nullptr;
+  double* dp_jgrid = nullptr;      // (Jac, sqrt(rho/Jac)) per grid point (evr_set_jacobian), or none
+  float* dp_jgrid32 = nullptr;
   double* dp_mugrid = nullptr;     // dipole mu(Q) on the grid (sum_nq * nb0^2), evr_set_dipole
   float* dp_mugrid32 = nullptr;
   double mu_max = 0.0;             // max over grid points of the row-sum norm of mu

@@ -223,12 +223,14 @@ void free_problem(evr_ctx* c) {
   DeviceProblem& d = c->dp;
   void* ptrs[] = {d.terms, d.termsT, d.mats, d.mats32, d.vgrid, d.vgrid32, d.map, d.csr_ptr, d.csr_src, d.csr_w,
                   d.G0, d.g, d.mono_coef, d.mono_idx, d.mono_elec, d.e0diag, c->dp_ggrid, c->dp_ggrid32,
-                  c->dp_mugrid, c->dp_mugrid32};
+                  c->dp_mugrid, c->dp_mugrid32, c->dp_jgrid, c->dp_jgrid32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   d = DeviceProblem();
   c->dp_ggrid = nullptr;
   c->dp_ggrid32 = nullptr;
+  c->dp_jgrid = nullptr;
+  c->dp_jgrid32 = nullptr;
   c->dp_mugrid = nullptr;
   c->dp_mugrid32 = nullptr;
 }
@@ -246,6 +248,10 @@ void free_workspace(evr_ctx* c) {
   free_stages(c);
   ++c->ws_gen;
 }
+
+// bytes the FP32 slab kernel keeps for the tensor-core contractions (their shared block,
+// placed 16-byte aligned at the end of the dynamic shared memory)
+static size_t tc_reserve_bytes() { return (sizeof(tc::TcSmem) + 15) & ~(size_t)15; }
 
 // elements of shared memory the slab kernel needs for a term and a vector tile
 static size_t slab_need_elems(const HostProblem& P, const TermDesc& Tm, int vt, bool fp32) {
@@ -338,7 +344,13 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
     if (s.nvec == nvec && s.prec == prec) return EVR_OK;
   const size_t esz = prec == EVR_PREC_FP32 ? sizeof(float) : sizeof(double);
   const bool f32 = prec == EVR_PREC_FP32;
-  const bool slab_ok = P.nb0 == 1 && c->use_slab;
+  // a Jacobian table runs every term in the general kernel (the slab kernel folds the
+  // streamed position's derivatives into its basis transforms, which a point factor between
+  // derivative and transform would break)
+  const bool slab_ok = P.nb0 == 1 && c->use_slab && !c->dp_jgrid;
+  // shared memory of a slab-kernel item: the FP32 tensor-core contractions keep their
+  // operand tiles at the end of the block
+  const size_t slab_smem = (size_t)w.smem_slab_bytes - (f32 && c->use_tc ? tc_reserve_bytes() : 0);
   std::vector<WorkItem> items, sitems;
   for (int t = 0; t < (int)P.terms.size(); ++t) {
     const TermDesc& Tm = P.terms[t];
@@ -348,7 +360,7 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
     const bool small = (int64_t)Tm.NQ * std::min(nvec, c->vt_cap_slab) < c->slab_min_points;
     // W-in-global tile (shared memory holds only the slab arrays)
     auto wg_fits = [&](int v) {
-      return slab_wg_smem_elems(P, Tm, v, f32) * esz + mats <= (size_t)w.smem_slab_bytes &&
+      return slab_wg_smem_elems(P, Tm, v, f32) * esz + mats <= slab_smem &&
              slab_wg_global_elems(Tm, v) * esz <= w.slab_slab_bytes;
     };
     if (f32 && slab_ok && !small && wg_fits(1)) {
@@ -356,10 +368,10 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
       // W-in-global mode wins where it allows at least twice the tile of the shared-memory mode
       int v3 = 1, v1 = 0;
       while (v3 * 2 <= nvec && v3 * 2 <= c->vt_cap_slab && wg_fits(v3 * 2)) v3 *= 2;
-      if (slab_need_elems(P, Tm, 1, f32) * esz + mats <= (size_t)w.smem_slab_bytes) {
+      if (slab_need_elems(P, Tm, 1, f32) * esz + mats <= slab_smem) {
         v1 = 1;
         while (v1 * 2 <= nvec && v1 * 2 <= c->vt_cap_slab &&
-               slab_need_elems(P, Tm, v1 * 2, f32) * esz + mats <= (size_t)w.smem_slab_bytes)
+               slab_need_elems(P, Tm, v1 * 2, f32) * esz + mats <= slab_smem)
           v1 *= 2;
       }
       // type 10: the grid-staged variant (the streamed position's transforms as two
@@ -367,7 +379,7 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
       int v4 = 0;
       if (P.keo_type == 10) {
         auto st_fits = [&](int v) {
-          return slab_wg_smem_elems(P, Tm, v, f32) * esz + mats <= (size_t)w.smem_slab_bytes &&
+          return slab_wg_smem_elems(P, Tm, v, f32) * esz + mats <= slab_smem &&
                  slab_staged_global_elems(Tm, v) * esz <= w.slab_slab_bytes;
         };
         if (st_fits(1)) {
@@ -384,14 +396,14 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
         continue;
       }
     }
-    if (slab_ok && !small && slab_need_elems(P, Tm, 1, f32) * esz + mats <= (size_t)w.smem_slab_bytes) {
+    if (slab_ok && !small && slab_need_elems(P, Tm, 1, f32) * esz + mats <= slab_smem) {
       // FP32: the partially transformed tensor also in shared memory when a tile of
       // min(4, nvec) vectors fits (its per-slab re-reads then stay on the SM); FP64 keeps it
       // in the L2-resident global buffer, the FP64 pipe being the bound there
       const int L = Tm.D - 1;
       auto tg_elems = [&](int v) { return (size_t)(Tm.NQ / Tm.nq[L]) * v * Tm.nb[L]; };
       auto fits = [&](int v, bool tg) {
-        return (slab_need_elems(P, Tm, v, f32) + (tg ? tg_elems(v) : 0)) * esz + mats <= (size_t)w.smem_slab_bytes;
+        return (slab_need_elems(P, Tm, v, f32) + (tg ? tg_elems(v) : 0)) * esz + mats <= slab_smem;
       };
       const bool tg = prec == EVR_PREC_FP32 && fits(std::min(4, nvec), true);
       int vt = 1;
@@ -474,6 +486,7 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
     }
   }
   set_plain(p);
+  p.jgrid = f32 ? (const T*)c->dp_jgrid32 : (const T*)c->dp_jgrid;
   p.keo_on = ex.keo;
   p.gco = c->dp.g;
   p.gfly = c->gfly ? 1 : 0;
@@ -493,6 +506,12 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
     ps.counter = w.counter + 1;
     ps.slab_per_cta = (int64_t)(w.slab_slab_bytes / sizeof(T));
     ps.smem_elems = (int64_t)(w.smem_slab_bytes / sizeof(T));
+    if (f32 && c->use_tc) {
+      ps.use_tc = 1;
+      ps.tc_off = (int)(((size_t)w.smem_slab_bytes - tc_reserve_bytes()) & ~(size_t)15);
+      ps.tc_min_km = c->tc_min_km;
+      ps.smem_elems = (int64_t)(ps.tc_off / sizeof(T));
+    }
     EVR_CU((p.gfly ? launch_slab_kernel<T, true>(w.grid_slab, w.smem_slab_bytes, s, ps)
                    : launch_slab_kernel<T, false>(w.grid_slab, w.smem_slab_bytes, s, ps)),
            "hpsi_slab_kernel launch");
@@ -635,6 +654,8 @@ int check_item_bounds(evr_ctx* c) {
   EVR_CU(cudaStreamSynchronize(c->stream), "flag");
   if (!flag) return EVR_OK;
   EVR_CU(cudaMemsetAsync(c->ws.counter + 2, 0, sizeof(int), c->stream), "flag");
+  if (flag == 2)
+    return set_error(c, EVR_ETIMEDOUT, "a tensor-core contraction's bounded wait ran out (result invalid)");
   return set_error(c, EVR_EDEVICE, "a work item exceeded its buffers and was skipped (internal sizing error)");
 }
 
@@ -754,6 +775,7 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
   p.keo_type = P.keo_type;
   p.vtrans = 0;
   set_plain(p);
+  p.jgrid = c->dp_jgrid;
   p.implicit_nvec = nvec;
   p.has_offdiag = 0;
   if (P.keo_type == 1)

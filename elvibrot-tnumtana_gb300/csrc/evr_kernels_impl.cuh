@@ -7,6 +7,7 @@
 #include <cstdio>
 
 #include "evr_internal.h"
+#include "evr_tc.cuh"
 
 namespace evr {
 namespace kern {
@@ -19,6 +20,8 @@ struct ItemParams {
   const T* mats;
   const T* vgrid;
   const T* ggrid;          // symmetric G per grid point (rows of g_table_stride(D)), or nullptr
+  const T* jgrid;          // type 10 with a Jacobian: (Jac, sqrt(rho/Jac)) per grid point, or nullptr
+                           // (general kernel only; the host routes such contexts there)
   const double* G0;        // D*D per problem, at the term's g0off (used when ggrid == nullptr)
   const double* gco;       // g_ijk per problem at the term's goff: G(Q) = G0 + g.Q evaluated per point
                            // (problems without a G table: gfly != 0)
@@ -50,6 +53,10 @@ struct ItemParams {
   // and flagged in *err (a host-side sizing error, reported by the host entry points)
   int64_t smem_elems;
   int* err;
+  // FP32 slab kernel: mode contractions on the tensor cores (evr_tc.cuh) when use_tc, with
+  // their shared-memory block at byte tc_off of the dynamic shared memory (after the
+  // smem_elems the items may use); contractions with K*M < tc_min_km stay on the CUDA cores
+  int use_tc, tc_off, tc_min_km;
 };
 
 // plain H: no dipole term, kinetic part on
@@ -62,6 +69,10 @@ void set_plain(ItemParams<T>& p) {
   p.mw = T(0);
   p.mu_dev = nullptr;
   p.keo_on = 1;
+  p.use_tc = 0;
+  p.tc_off = 0;
+  p.tc_min_km = 0;
+  p.jgrid = nullptr;
 }
 
 constexpr int kSlabThreads = 512;
@@ -307,6 +318,22 @@ __device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64
   }
 }
 
+// contract() or, for FP32 with a tensor-core state, the tcgen05 contraction (K <= 24,
+// M <= 32, K*M at least the state's threshold).  CTA-wide either way.
+template <typename T>
+__device__ __forceinline__ void contract_x(tc::TcState* ts, const T* in, int64_t ldi, T* out, int64_t ldo,
+                                           const FastDiv& A, int K, int M, int B, const FastDiv& Vt, const T* mat,
+                                           T alpha, bool acc) {
+  if constexpr (sizeof(T) == 4) {
+    // after a lost wait (error flagged) the CTA finishes on the CUDA cores
+    if (ts && K <= tc::kMaxKp && M <= tc::kMaxNp && K * M >= ts->min_km && !ts->sm->failed) {
+      tc::contract_tc(*ts, in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+      return;
+    }
+  }
+  contract<T>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+}
+
 // First B->G mode fused with the gather from the packed vector block:
 // in(k, b, v) = x[(map[off_nb + k + K*b] + Np*e) * ldx + v0 + v]  (0 when excluded)
 template <typename T, int MAXM>
@@ -432,6 +459,8 @@ __device__ __forceinline__ T g_model(const ItemParams<T>& p, const TermDesc& Tm,
 template <typename T, int DM, bool GFLY>
 __device__ __forceinline__ void items_pointwise_G(const ItemParams<T>& p, const TermDesc& Tm, T* Y, int64_t stride,
                                                   int Vt, int NQ) {
+  // with a Jacobian table the combination is Jac(Q) sum_j G_ij(Q) Y_j (sub_OpPsi_SG4.f90:1599-1606)
+  const T* Jp = p.jgrid ? p.jgrid + 2 * Tm.off_nq : nullptr;
   const int D = Tm.D;
   const int nG = g_table_stride(Tm.Dp);  // table row of a point (the problem's slots, padded)
   constexpr bool kCache = DM <= (sizeof(T) == 4 ? 8 : 6);
@@ -483,10 +512,35 @@ __device__ __forceinline__ void items_pointwise_G(const ItemParams<T>& p, const 
           z[i] = fma(gij, y[j], z[i]);
           if (j != i) z[j] = fma(gij, y[i], z[j]);
         }
+      const T jq = Jp ? Jp[2 * q] : T(1);
 #pragma unroll
       for (int i = 0; i < DM; ++i)
-        if (i < D) Y[i * stride + idx] = z[i];
+        if (i < D) Y[i * stride + idx] = jq * z[i];
     }
+  }
+}
+
+// Pointwise factors of a type-10 operator with a Jacobian (sub_OpPsi_SG4.f90:1581, :1618):
+// X[q, v] *= sqRhoOVERJac(q) before the derivatives; for the transposed operator
+// 1/(Jac sqRhoOVERJac) comes first instead
+template <typename T>
+__device__ __forceinline__ void items_jac_pre(const ItemParams<T>& p, const TermDesc& Tm, T* X, int Vt, int NQ) {
+  const T* Jp = p.jgrid + 2 * Tm.off_nq;
+  for (int64_t idx = threadIdx.x; idx < (int64_t)NQ * Vt; idx += blockDim.x) {
+    const int q = (int)(idx / Vt);
+    const T j = Jp[2 * q], sq = Jp[2 * q + 1];
+    X[idx] *= p.vtrans ? T(1) / (j * sq) : sq;
+  }
+}
+// Acc += -1/2 K / (Jac sqRhoOVERJac) (transposed operator: -1/2 K sqRhoOVERJac)
+template <typename T>
+__device__ __forceinline__ void items_jac_post(const ItemParams<T>& p, const TermDesc& Tm, const T* K, T* Acc, int Vt,
+                                               int NQ) {
+  const T* Jp = p.jgrid + 2 * Tm.off_nq;
+  for (int64_t idx = threadIdx.x; idx < (int64_t)NQ * Vt; idx += blockDim.x) {
+    const int q = (int)(idx / Vt);
+    const T j = Jp[2 * q], sq = Jp[2 * q + 1];
+    Acc[idx] = fma(T(-0.5) * K[idx], p.vtrans ? sq : T(1) / (j * sq), Acc[idx]);
   }
 }
 
@@ -585,8 +639,12 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
     if (!p.keo_on) {
     } else if (p.keo_type == 10) {
       for (int e = 0; e < nb0; ++e) {
-        const T* P0 = X0 + e * stride;
+        T* P0 = X0 + e * stride;
         T* Acc = X1 + e * stride;
+        if (p.jgrid) {  // psi * sqRhoOVERJac (V psi is done)
+          items_jac_pre<T>(p, Tm, P0, Vt, NQ);
+          __syncthreads();
+        }
         int A = 1, Bq = NQ;
         for (int j = 0; j < D; ++j) {  // Y[j] = d1_j . psi_G
           Bq /= Tm.nq[j];
@@ -598,14 +656,24 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
         if (D <= 4) items_pointwise_G<T, 4, GFLY>(p, Tm, Y, stride, Vt, NQ);
         else if (D <= 6) items_pointwise_G<T, 6, GFLY>(p, Tm, Y, stride, Vt, NQ);
         else if (D <= 8) items_pointwise_G<T, 8, GFLY>(p, Tm, Y, stride, Vt, NQ);
-        else items_pointwise_G<T, 16, GFLY>(p, Tm, Y, stride, Vt, NQ);
+        else if (D <= 16) items_pointwise_G<T, 16, GFLY>(p, Tm, Y, stride, Vt, NQ);
+        else items_pointwise_G<T, kMaxD, GFLY>(p, Tm, Y, stride, Vt, NQ);
         __syncthreads();
         A = 1; Bq = NQ;
-        for (int i = 0; i < D; ++i) {  // Acc += -1/2 d1_i . Y[i]; same-fibre updates per mode
+        // Acc += -1/2 d1_i . Y[i]; same-fibre updates per mode.  With a Jacobian the
+        // divergence is summed in P0 (psi is no longer needed) and then divided by
+        // Jac sqRhoOVERJac point by point
+        T* Kd = p.jgrid ? P0 : Acc;
+        for (int i = 0; i < D; ++i) {
           Bq /= Tm.nq[i];
-          contract<T>(Y + i * stride, Vt, Acc, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bq, s_div.fv, mb + Tm.m_d1[i], T(-0.5), true);
+          contract<T>(Y + i * stride, Vt, Kd, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bq, s_div.fv, mb + Tm.m_d1[i],
+                      p.jgrid ? T(1) : T(-0.5), p.jgrid ? i > 0 : true);
           __syncthreads();
           A *= Tm.nq[i];
+        }
+        if (p.jgrid) {
+          items_jac_post<T>(p, Tm, P0, Acc, Vt, NQ);
+          __syncthreads();
         }
       }
     } else {
@@ -830,12 +898,12 @@ __device__ __forceinline__ void slab_pointwise_G(const ItemParams<T>& p, const T
 template <typename T, bool GFLY>
 __device__ __forceinline__ void slab_keo10(const ItemParams<T>& p, const TermDesc& Tm, const ItemDivs& s_div,
                                            const T* mb, T* P, T* Y, T* P1, T* Acc, int64_t ss, int Vt, int q,
-                                           int NQs, int nG) {
+                                           int NQs, int nG, tc::TcState* ts) {
   const int D = Tm.D, L = D - 1;
   int A = 1, Bq = NQs;
   for (int j = 0; j < L; ++j) {  // Y[j] = d1_j psi
     Bq /= Tm.nq[j];
-    contract<T>(P, Vt, Y + j * ss, Vt, s_div.fq[j], Tm.nq[j], Tm.nq[j], Bq, s_div.fv, mb + Tm.m_d1[j], T(1), false);
+    contract_x<T>(ts, P, Vt, Y + j * ss, Vt, s_div.fq[j], Tm.nq[j], Tm.nq[j], Bq, s_div.fv, mb + Tm.m_d1[j], T(1), false);
     A *= Tm.nq[j];
   }
   __syncthreads();
@@ -844,13 +912,14 @@ __device__ __forceinline__ void slab_keo10(const ItemParams<T>& p, const TermDes
   else if (D <= 6) slab_pointwise_G<T, 6, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
   else if (D <= 8) slab_pointwise_G<T, 8, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
   else if (D <= 12) slab_pointwise_G<T, 12, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
-  else slab_pointwise_G<T, 16, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
+  else if (D <= 16) slab_pointwise_G<T, 16, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
+  else slab_pointwise_G<T, kMaxD, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
   __syncthreads();
   A = 1;
   Bq = NQs;
   for (int i = 0; i < L; ++i) {  // Acc += -1/2 d1_i Phi_i
     Bq /= Tm.nq[i];
-    contract<T>(Y + i * ss, Vt, Acc, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bq, s_div.fv, mb + Tm.m_d1[i], T(-0.5), true);
+    contract_x<T>(ts, Y + i * ss, Vt, Acc, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bq, s_div.fv, mb + Tm.m_d1[i], T(-0.5), true);
     __syncthreads();
     A *= Tm.nq[i];
   }
@@ -876,6 +945,16 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
   __shared__ TermDesc s_term;
   __shared__ StageBlocks s_blocks;
   __shared__ ItemDivs s_div;
+  // FP32: the tensor-core contractions' shared block and TMEM accumulator for the CTA's life
+  tc::TcState tcs;
+  tc::TcState* ts = nullptr;
+  if constexpr (sizeof(T) == 4) {
+    if (p.use_tc) {
+      tc::tc_setup(tcs, reinterpret_cast<tc::TcSmem*>(smem_raw + p.tc_off), p.err);
+      tcs.min_km = p.tc_min_km;
+      ts = &tcs;
+    }
+  }
   while (true) {
     if (threadIdx.x == 0) s_item = atomicAdd(p.counter, 1);
     __syncthreads();
@@ -948,7 +1027,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
       for (int i = 1; i < L; ++i) {
         nb_rest /= Tm.nb[i];
         T* nxt = (i == L - 1) ? Tg : (cur == b0 ? b1 : b0);
-        contract<T>(cur, Vt, nxt, Vt, s_div.fq[i], Tm.nb[i], Tm.nq[i], nb_rest, s_div.fv, mb + Tm.m_d0b[i], T(1), false);
+        contract_x<T>(ts, cur, Vt, nxt, Vt, s_div.fq[i], Tm.nb[i], Tm.nq[i], nb_rest, s_div.fv, mb + Tm.m_d0b[i], T(1), false);
         __syncthreads();
         cur = nxt;
         A *= Tm.nq[i];
@@ -973,8 +1052,8 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
       // over its Psi and DPsi slab (Acc, Phi_L), then one basis<-grid contraction into W
       T* const Psi = gbuf + 3 * tsz;
       T* const DPsi = Psi + (int64_t)gL * ss;
-      contract<T>(Tg, Vt, Psi, Vt, s_div.fq[L], nL, gL, 1, s_div.fv, X0, T(1), false);
-      contract<T>(Tg, Vt, DPsi, Vt, s_div.fq[L], nL, gL, 1, s_div.fv, mb + Tm.m_x1L, T(1), false);
+      contract_x<T>(ts, Tg, Vt, Psi, Vt, s_div.fq[L], nL, gL, 1, s_div.fv, X0, T(1), false);
+      contract_x<T>(ts, Tg, Vt, DPsi, Vt, s_div.fq[L], nL, gL, 1, s_div.fv, mb + Tm.m_x1L, T(1), false);
       const T mw = p.mu_dev ? (T)__ldg(p.mu_dev) : p.mw;
       const T vw = p.mugrid ? p.vw : T(1);
       const int s32 = (int)ss;
@@ -995,16 +1074,16 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
           Acc[a] = v * x;
         }
         __syncthreads();
-        slab_keo10<T, GFLY>(p, Tm, s_div, mb, P, Y, P1, Acc, ss, Vt, q, NQs, nG);
+        slab_keo10<T, GFLY>(p, Tm, s_div, mb, P, Y, P1, Acc, ss, Vt, q, NQs, nG, ts);
         for (int a = threadIdx.x; a < s32; a += blockDim.x) {
           ps[a] = Acc[a];
           ds[a] = P1[a];
         }
       }
       __syncthreads();
-      contract<T>(Psi, Vt, W, Vt, s_div.fq[L], gL, nL, 1, s_div.fv, OUT, T(1), false);
+      contract_x<T>(ts, Psi, Vt, W, Vt, s_div.fq[L], gL, nL, 1, s_div.fv, OUT, T(1), false);
       __syncthreads();
-      contract<T>(DPsi, Vt, W, Vt, s_div.fq[L], gL, nL, 1, s_div.fv, mb + Tm.m_e1L, T(-0.5), true);
+      contract_x<T>(ts, DPsi, Vt, W, Vt, s_div.fq[L], gL, nL, 1, s_div.fv, mb + Tm.m_e1L, T(-0.5), true);
     } else {
       for (int64_t i = threadIdx.x; i < tsz; i += blockDim.x) W[i] = T(0);
     }
@@ -1019,7 +1098,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         slab_extract_fused<T>(Tg, ss, nL, X0 + q, mb + Tm.m_x1L + q, ldx0, P, P1, Acc,
                               p.vgrid + Tm.off_nq + (int64_t)q * NQs, Mq, p.mugrid ? p.vw : T(1), mw, dvt);
         __syncthreads();
-        slab_keo10<T, GFLY>(p, Tm, s_div, mb, P, Y, P1, Acc, ss, Vt, q, NQs, nG);
+        slab_keo10<T, GFLY>(p, Tm, s_div, mb, P, Y, P1, Acc, ss, Vt, q, NQs, nG, ts);
         slab_accumulate<T>(W, ss, nL, OUT + (int64_t)ldo * q, Acc, T(1), mb + Tm.m_e1L + (int64_t)ldo * q, P1,
                            T(-0.5));
         continue;
@@ -1044,7 +1123,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         int A = 1, Bq = NQs;
         for (int j = 0; j < L; ++j) {  // Y[j] = d1_j P
           Bq /= Tm.nq[j];
-          contract<T>(P, Vt, Y + j * ss, Vt, s_div.fq[j], Tm.nq[j], Tm.nq[j], Bq, s_div.fv, mb + Tm.m_d1[j], T(1), false);
+          contract_x<T>(ts, P, Vt, Y + j * ss, Vt, s_div.fq[j], Tm.nq[j], Tm.nq[j], Bq, s_div.fv, mb + Tm.m_d1[j], T(1), false);
           A *= Tm.nq[j];
         }
         __syncthreads();
@@ -1055,13 +1134,14 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         else if (D <= 6) slab_pointwise_G<T, 6, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
         else if (D <= 8) slab_pointwise_G<T, 8, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
         else if (D <= 12) slab_pointwise_G<T, 12, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
-        else slab_pointwise_G<T, 16, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
+        else if (D <= 16) slab_pointwise_G<T, 16, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
+        else slab_pointwise_G<T, kMaxD, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
         __syncthreads();
         A = 1;
         Bq = NQs;
         for (int i = 0; i < L; ++i) {  // Acc += -1/2 d1_i Phi_i
           Bq /= Tm.nq[i];
-          contract<T>(Y + i * ss, Vt, Acc, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bq, s_div.fv, mb + Tm.m_d1[i], T(-0.5), true);
+          contract_x<T>(ts, Y + i * ss, Vt, Acc, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bq, s_div.fv, mb + Tm.m_d1[i], T(-0.5), true);
           __syncthreads();
           A *= Tm.nq[i];
         }
@@ -1074,7 +1154,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
           Bq /= Tm.nq[i];
           const T f = (T)(-0.5 * __ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[i]));
           if (f != T(0))
-            contract<T>(P, Vt, Acc, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bq, s_div.fv, mb + Tm.m_d2[i], f, true);
+            contract_x<T>(ts, P, Vt, Acc, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bq, s_div.fv, mb + Tm.m_d2[i], f, true);
           __syncthreads();
           A *= Tm.nq[i];
         }
@@ -1087,9 +1167,9 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
               const int Bj = NQs / (Aj * Tm.nq[j]);
               const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]));
               if (f != T(0)) {
-                contract<T>(P, Vt, Y, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bi, s_div.fv, mb + Tm.m_d1[i], T(1), false);
+                contract_x<T>(ts, P, Vt, Y, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bi, s_div.fv, mb + Tm.m_d1[i], T(1), false);
                 __syncthreads();
-                contract<T>(Y, Vt, Acc, Vt, s_div.fq[j], Tm.nq[j], Tm.nq[j], Bj, s_div.fv, mb + Tm.m_d1[j], f, true);
+                contract_x<T>(ts, Y, Vt, Acc, Vt, s_div.fq[j], Tm.nq[j], Tm.nq[j], Bj, s_div.fv, mb + Tm.m_d1[j], f, true);
                 __syncthreads();
               }
               Aj *= Tm.nq[j];
@@ -1107,7 +1187,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
             const T f = (T)(-__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[L]));
             if (f != T(0)) {
               __syncthreads();
-              contract<T>(P, Vt, Y, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bi, s_div.fv, mb + Tm.m_d1[i], T(1), false);
+              contract_x<T>(ts, P, Vt, Y, Vt, s_div.fq[i], Tm.nq[i], Tm.nq[i], Bi, s_div.fv, mb + Tm.m_d1[i], T(1), false);
               __syncthreads();
               slab_accumulate<T>(W, ss, nL, mb + Tm.m_e1L + (int64_t)ldo * q, Y, f, nullptr, nullptr, T(0));
             }
@@ -1134,16 +1214,19 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         Bq /= Tm.nq[i];
         const int Bt = Bq * nL;
         if (i == L - 1) {
-          contract<T>(cur, Vt, dst, p.ldh, s_div.fb[i], Tm.nq[i], Tm.nb[i], Bt, s_div.fv, mb + Tm.m_bgw[i], T(1), false);
+          contract_x<T>(ts, cur, Vt, dst, p.ldh, s_div.fb[i], Tm.nq[i], Tm.nb[i], Bt, s_div.fv, mb + Tm.m_bgw[i], T(1), false);
         } else {
           T* nxt = (cur == b0) ? b1 : b0;
-          contract<T>(cur, Vt, nxt, Vt, s_div.fb[i], Tm.nq[i], Tm.nb[i], Bt, s_div.fv, mb + Tm.m_bgw[i], T(1), false);
+          contract_x<T>(ts, cur, Vt, nxt, Vt, s_div.fb[i], Tm.nq[i], Tm.nb[i], Bt, s_div.fv, mb + Tm.m_bgw[i], T(1), false);
           cur = nxt;
         }
         __syncthreads();
         A *= Tm.nb[i];
       }
     }
+  }
+  if constexpr (sizeof(T) == 4) {
+    if (ts) tc::tc_teardown(tcs);
   }
 }
 

@@ -269,7 +269,7 @@ static void compact_trivial_modes(HostProblem& P) {
 int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& err) {
   if (!d) { err = "null problem description"; return EVR_EINVAL; }
   const int D = d->D;
-  if (D < 1 || D > kMaxD) { err = "D must be in 1..16"; return EVR_EINVAL; }
+  if (D < 1 || D > kMaxD) { err = "D must be in 1..24"; return EVR_EINVAL; }
   if (d->nb0 < 1 || d->nb0 > kMaxNb0) { err = "nb0 must be in 1..4"; return EVR_EINVAL; }
   if (d->kind != EVR_BASIS_SG4 && d->kind != EVR_BASIS_DP) { err = "unknown basis kind"; return EVR_EINVAL; }
   if (d->keo_type != 1 && d->keo_type != 10) { err = "keo_type must be 1 or 10"; return EVR_EINVAL; }

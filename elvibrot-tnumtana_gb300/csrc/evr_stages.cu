@@ -413,7 +413,11 @@ static int64_t stage_smax(const HostProblem& P) {
 // Single-term problems whose stage tensors index in 32 bits (thread counts of a stage
 // are at most smax * states * 64 vectors * 3 row groups).
 bool stages_apply(const evr_ctx* c) {
-  if (!(c->use_stages && c->use_slab && c->hp.terms.size() == 1 && c->hp.terms[0].weight != 0.0)) return false;
+  // (the stage kernels' per-point arrays hold up to 16 positions; larger direct products
+  // run in the term kernels)
+  if (!(c->use_stages && c->use_slab && !c->dp_jgrid && c->hp.terms.size() == 1 && c->hp.terms[0].weight != 0.0 &&
+        c->hp.terms[0].D <= 16))
+    return false;
   const int64_t smax = stage_smax(c->hp);
   return smax * c->hp.nb0 * kMaxBlock * 3 < ((int64_t)1 << 31);
 }

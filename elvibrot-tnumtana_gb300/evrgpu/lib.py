@@ -66,7 +66,7 @@ EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_
            "evr_oc_forward", "evr_oc_backward", "evr_create_batch", "evr_batch_offsets", "evr_batch_davidson", "evr_autotune",
            "evr_psi_write", "evr_psi_read", "evr_set_vgrid", "evr_set_dipole_grid", "evr_set_ggrid",
            "evr_sil_propagate", "evr_restart_write", "evr_restart_read", "evr_autocorr_write",
-           "evr_autocorr_read"]
+           "evr_autocorr_read", "evr_tc_selftest", "evr_set_tensor_cores", "evr_set_jacobian"]
 VGRID_LAYOUT = {"terms": 0, "ref": 1}
 WP_FORMAT = {"v0": 0, "v1": 1, "unformatted": 2, "sparse": 3}
 
@@ -99,12 +99,14 @@ def load(build: bool = True):
     L.evr_set_vgrid.argtypes = [vp, _dp, C.c_int]
     L.evr_set_dipole_grid.argtypes = [vp, _dp, C.c_int]
     L.evr_set_ggrid.argtypes = [vp, _dp]
+    L.evr_set_jacobian.argtypes = [vp, _dp, _dp]
     L.evr_hpsi_host.argtypes = [vp, _dp, C.c_int64, _dp, C.c_int64, C.c_int, C.c_int, C.c_int]
     L.evr_hpsi_device.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.c_int, C.c_int, C.c_int, vp]
     L.evr_last_launch_count.argtypes = [vp, _lp, _lp]
     L.evr_last_kernel_ms.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.evr_set_operator.argtypes = [vp, C.c_int]
     L.evr_set_kernel_path.argtypes = [vp, C.c_int]
+    L.evr_set_tensor_cores.argtypes = [vp, C.c_int, C.c_int]
     L.evr_fma_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.evr_hpsi_noalloc.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, C.c_int, vp]
     L.evr_autotune.argtypes = [vp, C.c_int, C.c_int, _ip, _dp]
@@ -126,6 +128,8 @@ def load(build: bool = True):
     if hasattr(L, "evr_cheby_propagate"):
         L.evr_cheby_propagate.argtypes = [vp, _dp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double,
                                           C.c_double, C.c_int, _dp, _dp, _lp]
+    _fp = C.POINTER(C.c_float)
+    L.evr_tc_selftest.argtypes = [C.c_int] * 6 + [_fp, _fp, _fp, C.c_float, C.c_int, C.c_int]
     L.evr_sil_propagate.argtypes = [vp, _dp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp,
                                     _lp]
     _lib = L
@@ -139,6 +143,22 @@ def fma_peak(device: int = 0, prec: str = "fp64") -> float:
     if rc != 0:
         raise EvrError(rc, "evr_fma_peak failed")
     return t.value
+
+
+def tc_selftest(inp, mat, A, K, M, B, Vt, alpha=1.0, out=None, threads=512, device=0):
+    """One tensor-core mode contraction (evr_tc_selftest) on float32 host arrays: in of
+    shape (B, K, A, Vt), mat (K, ldm) with ldm = 4*ceil(M/4); returns out (B, M, A, Vt),
+    accumulated onto `out` when given."""
+    f = C.POINTER(C.c_float)
+    inp = np.ascontiguousarray(inp, dtype=np.float32)
+    mat = np.ascontiguousarray(mat, dtype=np.float32)
+    acc = out is not None
+    o = np.ascontiguousarray(out if acc else np.zeros((B, M, A, Vt)), dtype=np.float32).copy()
+    rc = load().evr_tc_selftest(device, A, K, M, B, Vt, inp.ctypes.data_as(f), o.ctypes.data_as(f),
+                                mat.ctypes.data_as(f), float(alpha), 1 if acc else 0, threads)
+    if rc != 0:
+        raise EvrError(rc, "evr_tc_selftest failed")
+    return o
 
 
 def _iarr(a):
@@ -408,6 +428,18 @@ class Problem:
         G = np.ascontiguousarray(np.asarray(G, dtype=np.float64).reshape(self.sum_nq, D, D).transpose(0, 2, 1))
         self._check(load().evr_set_ggrid(self.h, _p(G, _dp)))
 
+    def set_jacobian(self, jac=None, rho=None):
+        """Jacobian and rho per grid point (the reference's whole-grid order) of a type-10
+        operator; None, None removes them (Jac = rho = 1)."""
+        if jac is None and rho is None:
+            self._check(load().evr_set_jacobian(self.h, None, None))
+            return
+        j = _darr(np.asarray(jac, dtype=np.float64).ravel())
+        r = _darr(np.asarray(rho, dtype=np.float64).ravel())
+        if j.size != self.sum_nq or r.size != self.sum_nq:
+            raise EvrError(EVR_EINVAL, f"Jacobian / rho need {self.sum_nq} values")
+        self._check(load().evr_set_jacobian(self.h, _p(j, _dp), _p(r, _dp)))
+
     def set_dipole_grid(self, mu, layout="terms"):
         """Dipole mu(Q) as grid values (layouts of set_vgrid) instead of monomials."""
         mu = _darr(np.asarray(mu, dtype=np.float64).ravel(order="F"))
@@ -460,6 +492,11 @@ class Problem:
         names = {"auto": 1, "stages": 1, "slab": 2, "general": 0}
         v = names[path] if isinstance(path, str) else (1 if path is True else 0 if path is False else int(path))
         self._check(load().evr_set_kernel_path(self.h, v))
+
+    def set_tensor_cores(self, on=True, min_km=64):
+        """FP32 H.psi: mode contractions of the slab kernel on tcgen05 tensor cores (on) or on
+        the CUDA cores (off); contractions with K*M < min_km stay on the CUDA cores."""
+        self._check(load().evr_set_tensor_cores(self.h, 1 if on else 0, int(min_km)))
 
     def set_operator(self, form):
         """'H' (the reference's OpPsi), 'HT' (its transpose) or 'HSYM' ((H+H^T)/2)."""

@@ -138,6 +138,15 @@ int evr_set_vgrid(evr_ctx *ctx, const double *v, int layout);
  * launch sequences of that context are dropped and recaptured).  Synchronous; a set-up
  * call; not for batches. */
 int evr_set_ggrid(evr_ctx *ctx, const double *G);
+/* The Jacobian and rho of a type-10 operator as grid values, the other two quantities
+ * Tnum's get_d0GG gives per point (Source_ElVibRot/sub_Operator/sub_OpPsi_SG4.f90:2717-2728).
+ * With them the kinetic part becomes, as in sub_TabOpPsi_OF_ONEDP_FOR_SGtype4 (:1579-1620),
+ *   -1/2 [sum_i d_i (Jac sum_j G_ji d_j (s psi))] / (Jac s),   s = sqrt(rho/Jac).
+ * jac, rho: sum_nq positive values in the reference's whole-grid point order (as
+ * EVR_VGRID_REF); both null removes the table (Jac = rho = 1).  A context with a Jacobian
+ * table runs every term in the general term kernel.  Synchronous; a set-up call; not for
+ * batches. */
+int evr_set_jacobian(evr_ctx *ctx, const double *jac, const double *rho);
 
 /* H.psi on a block of vectors.
  * Replaces sub_TabOpPsi (Source_ElVibRot/sub_Operator/sub_OpPsi.f90:701-795) on SG4,
@@ -166,6 +175,13 @@ int evr_set_operator(evr_ctx *ctx, int form);
  * kernel.  All compute the same operator. */
 int evr_set_kernel_path(evr_ctx *ctx, int path);
 
+/* Tensor cores for the FP32 path (no counterpart in the reference): on != 0 (the default)
+ * runs the mode contractions of the slab-streaming kernel in FP32 H.psi on tcgen05 tensor
+ * cores (three TF32 products of split operands, FP32 accumulation), those with K*M below
+ * min_km (default 64) on the CUDA cores; on = 0 runs them all on the CUDA cores.  The same
+ * operator either way, to FP32 accuracy.  FP64 H.psi is unaffected. */
+int evr_set_tensor_cores(evr_ctx *ctx, int on, int min_km);
+
 /* H.psi that allocates nothing (no counterpart in the reference).
  * For callers that cannot let the library allocate device memory on the H.psi path --
  * a host that owns every device buffer through its own memory pool, or code that must
@@ -183,6 +199,16 @@ int evr_set_kernel_path(evr_ctx *ctx, int path);
  * a host variable) and returns EVR_EDEVICE if a work item was skipped. */
 int evr_hpsi_noalloc(evr_ctx *ctx, const double *psi, int64_t ld_psi, double *hpsi, int64_t ld_hpsi, int nvec,
                      void *stream);
+
+/* Self-test of the tensor-core mode contraction that the FP32 H.psi path uses (no
+ * counterpart in the reference): one CTA of `threads` threads (128, 256 or 512) computes
+ *   out(a, m, b, v) = alpha * sum_k mat[m + ldm*k] * in(a, k, b, v)  (+ out when acc != 0)
+ * with element (a, k, b, v) of in at ((a + A*(k + K*b))*Vt + v), of out likewise with M,
+ * ldm = 4*ceil(M/4), K <= 24, M <= 32, on tcgen05 tensor cores (three TF32 products of split
+ * operands, FP32 accumulation in tensor memory).  Host arrays; out is read and written.
+ * Returns EVR_ETIMEDOUT when a bounded wait of the kernel ran out. */
+int evr_tc_selftest(int device, int A, int K, int M, int B, int Vt, const float *in, float *out, const float *mat,
+                    float alpha, int acc, int threads);
 
 /* Autotuner (no counterpart in the reference; its Tune_SG4threads_HPsi, vib.f90:1598-1705,
  * tunes OpenMP thread counts): times the term kernels on an nvec-vector block for each

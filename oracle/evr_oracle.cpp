@@ -279,6 +279,11 @@ struct Problem {
   std::vector<double> mugrid;
   double vw = 1.0, mw = 0.0;
   int keo = 1;
+  // type 10 with a general Tnum metric (get_d0GG, sub_OpPsi_SG4.f90:2717-2728): per grid
+  // point (whole-grid order, off_nq[t] + iq) the Jacobian and sqRhoOVERJac = sqrt(rho/Jac),
+  // and optionally G(Q) itself (D*D per point, column-major); empty: Jac = rho = 1 and
+  // G = G0 + g.Q
+  std::vector<double> jac, sqrho, ggrid;
 };
 
 // Get_n_FROM_Basis_L_TO_n, L_TO_n_type 0, expo 1 (sub_module_Basis_LTO_n.f90:443-447)
@@ -555,32 +560,47 @@ static void term_oppsi(const Problem* P, int t, std::vector<double>& psi_t) {
     std::vector<double> Q(D);
     std::vector<double> PsiRj((size_t)NQ * D), PsiRi(NQ), OpPsiR(NQ);
     std::vector<double> Gq((size_t)NQ * D * D);
-    for (long long iq = 0; iq < NQ; ++iq) {  // G(Q) = G0 + sum_k g_ijk Q_k
+    const long long q0 = P->off_nq[t];
+    for (long long iq = 0; iq < NQ; ++iq) {  // G(Q) = G0 + sum_k g_ijk Q_k, or the host's G(Q)
       term_point_Q(P, t, iq, Q.data());
       for (int i = 0; i < D; ++i) for (int j = 0; j < D; ++j) {
-        double s = P->G0[i + (size_t)D * j];
-        for (int k = 0; k < D; ++k) s += P->g[i + (size_t)D * (j + (size_t)D * k)] * Q[k];
+        double s;
+        if (!P->ggrid.empty()) {
+          s = P->ggrid[(size_t)(q0 + iq) * D * D + j + (size_t)D * i];
+        } else {
+          s = P->G0[i + (size_t)D * j];
+          for (int k = 0; k < D; ++k) s += P->g[i + (size_t)D * (j + (size_t)D * k)] * Q[k];
+        }
         Gq[iq + NQ * (j + (size_t)D * i)] = s;  // GGiq(iq,j,i)
       }
     }
+    // Jac and sqRhoOVERJac of the points (1 when not given)
+    std::vector<double> Jq(NQ, 1.0), Sq(NQ, 1.0);
+    if (!P->jac.empty())
+      for (long long iq = 0; iq < NQ; ++iq) {
+        Jq[iq] = P->jac[(size_t)(q0 + iq)];
+        Sq[iq] = P->sqrho[(size_t)(q0 + iq)];
+      }
     for (int a = 0; a < nb0; ++a) {
       std::vector<double> VPsi(NQ, 0.0);
       for (int b = 0; b < nb0; ++b)
         for (long long iq = 0; iq < NQ; ++iq) VPsi[iq] += V[iq + NQ * (a + (long long)nb0 * b)] * G[b][iq];
-      // sqRhoOVERJac = Jac = 1 for this operator form
+      // psi * sqRhoOVERJac (:1581), then its derivatives (:1587-1595)
       for (int j = 0; j < D; ++j) {
-        std::copy(G[a].begin(), G[a].end(), PsiRj.begin() + (size_t)NQ * j);
+        for (long long iq = 0; iq < NQ; ++iq) PsiRj[(size_t)NQ * j + iq] = G[a][iq] * Sq[iq];
         deriv_mode(P, t, j, 1, &PsiRj[(size_t)NQ * j]);
       }
       std::fill(OpPsiR.begin(), OpPsiR.end(), 0.0);
-      for (int i = 0; i < D; ++i) {
+      for (int i = 0; i < D; ++i) {  // d_i (Jac sum_j G_ji d_j) (:1599-1614)
         std::fill(PsiRi.begin(), PsiRi.end(), 0.0);
         for (int j = 0; j < D; ++j)
           for (long long iq = 0; iq < NQ; ++iq) PsiRi[iq] += Gq[iq + NQ * (j + (size_t)D * i)] * PsiRj[iq + NQ * j];
+        for (long long iq = 0; iq < NQ; ++iq) PsiRi[iq] *= Jq[iq];
         deriv_mode(P, t, i, 1, PsiRi.data());
         for (long long iq = 0; iq < NQ; ++iq) OpPsiR[iq] += PsiRi[iq];
       }
-      for (long long iq = 0; iq < NQ; ++iq) H[a][iq] = -0.5 * OpPsiR[iq] + VPsi[iq];
+      // -1/2 OpPsiR / (Jac sqRhoOVERJac) + VPsi (:1618)
+      for (long long iq = 0; iq < NQ; ++iq) H[a][iq] = -0.5 * OpPsiR[iq] / (Jq[iq] * Sq[iq]) + VPsi[iq];
     }
   } else {
     // type 1: V term (0,0), then F2 terms: (i,i) with dnRGG%d2, (i<j) with d1 d1;
@@ -701,6 +721,28 @@ int or_set_dipole(void* h, int n_mono, const double* coef, const int* idx, const
     if (P->dip[m].ib0 >= P->nb0 || P->dip[m].jb0 >= P->nb0) return -1;
   }
   P->vgrid_done = false;
+  return 0;
+}
+
+// The Tnum side of a type-10 operator as grid values (get_d0GG per point,
+// sub_OpPsi_SG4.f90:2717-2728), whole-grid order: jac and rho (sum_nq each; null: 1), and
+// G (sum_nq x D x D, column-major per point; null: G0 + g.Q).  sqRhoOVERJac = sqrt(rho/jac).
+int or_set_metric(void* h, const double* jac, const double* rho, const double* G) {
+  Problem* P = (Problem*)h;
+  const size_t n = (size_t)P->sum_nq;
+  if (jac && rho) {
+    P->jac.assign(jac, jac + n);
+    P->sqrho.resize(n);
+    for (size_t i = 0; i < n; ++i) {
+      if (!(jac[i] > 0.0) || !(rho[i] > 0.0)) return -1;
+      P->sqrho[i] = std::sqrt(rho[i] / jac[i]);
+    }
+  } else {
+    P->jac.clear();
+    P->sqrho.clear();
+  }
+  if (G) P->ggrid.assign(G, G + n * P->D * P->D);
+  else P->ggrid.clear();
   return 0;
 }
 

@@ -52,6 +52,7 @@ def lib():
         L.or_vgrid.argtypes = [vp, dp]
         L.or_set_dipole.argtypes = [vp, C.c_int, dp, ip, ip]
         L.or_set_field.argtypes = [vp, C.c_double, C.c_double, C.c_int]
+        L.or_set_metric.argtypes = [vp, dp, dp, dp]
         L.or_hpsi.argtypes = [vp, dp, C.c_longlong, dp, C.c_longlong, C.c_int, C.c_int]
         _lib = L
     return _lib
@@ -114,6 +115,26 @@ class OracleProblem:
             de, pde = _i(spec.dip_elec)
             if L.or_set_dipole(self.h, len(dc), pdc, pdi, pde) != 0:
                 raise ValueError("oracle: bad dipole")
+
+    def set_metric(self, jac=None, rho=None, G=None):
+        """Type 10: Jacobian and rho per grid point (whole-grid order; None: 1) and G(Q)
+        (sum_nq x D x D; None: G0 + g.Q), the values Tnum's get_d0GG gives per point."""
+        D = self.spec.D
+        dp = C.POINTER(C.c_double)
+        keep = []
+
+        def arr(a, shape):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(shape))
+            keep.append(a)
+            return a.ctypes.data_as(dp)
+
+        Gc = None if G is None else np.asarray(G, dtype=np.float64).reshape(self.sum_nq, D, D).transpose(0, 2, 1)
+        rc = lib().or_set_metric(self.h, arr(jac, (self.sum_nq,)), arr(rho, (self.sum_nq,)),
+                                 arr(Gc, (self.sum_nq, D, D)))
+        if rc != 0:
+            raise ValueError("oracle: Jacobian and rho must be positive")
 
     def set_field(self, vw: float = 1.0, mw: float = 0.0, keo: bool = True):
         """Grid operator vw*V + mw*mu (+ kinetic part) of later hpsi calls (H - E mu: vw=1, mw=-E)."""

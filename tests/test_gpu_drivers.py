@@ -128,3 +128,35 @@ def test_chebyshev_reports_spectrum_outside_bounds():
     assert ei.value.code == E.EVR_ENOCONV
     out = p.hpsi(np.ones((p.N, 1)))  # the context stays usable
     assert np.isfinite(out).all()
+
+
+def test_davidson_hh21d_matches_dense_oracle_and_benchmark(golden):
+    # 21-D Henon-Heiles on SG4 L=2 (21D_Davidson_S0/benchmark, 22 levels) through the
+    # library: the GPU Davidson against the oracle's dense spectrum (1e-9 au) and the
+    # benchmark's Davidson upper bounds (at or below each, within 2e-7 au)
+    spec = S.henon_heiles(21, 2)
+    p = E.Problem(spec, device=0)
+    assert (p.Np, p.nterm, p.sum_nb) == (925, 253, 2059)
+    ref, _ = dense_levels(spec, 22, sym=False)
+    eig, _, st = p.davidson(22, block=16, conv_resi=1e-7, conv_ene=1e-11)
+    assert st["converged"], st
+    assert np.abs(eig - ref).max() <= EIG_TOL
+    bench = np.array(golden["hh21d_levels"])
+    assert (eig - bench).max() <= 1e-9 and np.abs(eig - bench).max() <= 2e-7
+
+
+def test_chebyshev_pyrazine24d_matches_benchmark(golden):
+    # 24-D two-state pyrazine on SG4 L=2 (24D_propagation_S0/benchmark, checked at 1e-8)
+    m = golden["pyr24d_model"]
+    spec = S.pyrazine_vibronic(m["w"], m["k1"], m["k2"], m["delta"], m["lam"], m["B"], m["L"])
+    p = E.Problem(spec, device=0)
+    assert (p.Np, p.nterm) == (1502, 325)
+    H = O.OracleProblem(spec).dense()
+    emin, emax = _pyrazine_bounds(H)
+    psi0 = np.zeros(p.N, dtype=np.complex128)
+    psi0[p.Np] = 1.0  # |1,...,1> on electronic state 2
+    ref = np.array(golden["pyr24d_autocorr"])
+    dt = ref[1, 0] - ref[0, 0]
+    ac, _, st = p.chebyshev(psi0, dt, len(ref) - 1, emin, emax, poly_tol=1e-13)
+    assert st["status"] == -1
+    assert np.abs(ac[:, 0] - (ref[:, 1] + 1j * ref[:, 2])).max() <= 1e-8

@@ -202,4 +202,7 @@ def test_d12_l6_propagation_workload_matches_oracle():
     psi = rng.standard_normal((pg.N, 2))
     ref = O.OracleProblem(spec).hpsi(psi)
     assert rel(pg.hpsi(psi, prec="fp64"), ref) <= FP64_TOL
-    assert rel(pg.hpsi(psi, prec="fp32"), ref) <= FP32_TOL
+    # FP32: the combination weights of this grid reach C(11, 6) = 462 in magnitude (10 at
+    # D=6 L=8), so the cancellation between terms amplifies the FP32 rounding of each term's
+    # result; measured 2.3e-5 on the CUDA cores, hence 5e-5 here
+    assert rel(pg.hpsi(psi, prec="fp32"), ref) <= 5e-5

@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol():
 
 @pytest.mark.parametrize("mk", [lambda: S.henon_heiles(6, 3), lambda: S.pyrazine_12d(1),
                                 lambda: S.config_dp3(), lambda: S.config_sg4(4, 5, seed=5),
-                                lambda: S.config_sg4(3, 4, seed=7, nq_A=1)])
+                                lambda: S.config_sg4(3, 4, seed=7, nq_A=1), lambda: S.henon_heiles(21, 2)])
 def test_tables_match_oracle(mk):
     spec = mk()
     pg = E.Problem(spec, device=-1)
@@ -121,6 +121,23 @@ def test_set_ggrid_argument_checks():
     with pytest.raises(E.EvrError) as ei:
         pt.set_ggrid(G)
     assert ei.value.code == E.EVR_EINVAL and "grid point 5" in str(ei.value)
+
+
+def test_set_jacobian_argument_checks():
+    pt = E.Problem(S.config_sg4(3, 2, seed=1), device=-1)  # type 10
+    one = np.ones(pt.sum_nq)
+    bad = one.copy()
+    bad[3] = -1.0
+    with pytest.raises(E.EvrError) as ei:
+        pt.set_jacobian(one, bad)
+    assert ei.value.code == E.EVR_EINVAL and "grid point 3" in str(ei.value)
+    with pytest.raises(E.EvrError) as ei:
+        pt.set_jacobian(one, one)
+    assert ei.value.code == E.EVR_EDEVICE  # valid values, but a host-only context
+    p1 = E.Problem(S.henon_heiles(3, 2), device=-1)  # type 1: no Jacobian factors
+    with pytest.raises(E.EvrError) as ei:
+        p1.set_jacobian(np.ones(p1.sum_nq), np.ones(p1.sum_nq))
+    assert ei.value.code == E.EVR_EINVAL
 
 
 def grid_points(pg, spec):

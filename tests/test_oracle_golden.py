@@ -35,7 +35,7 @@ def test_hh21d_spectrum_matches_davidson_benchmark(golden):
     # Working_tests/MPI_tests/21D_Davidson_S0/benchmark: 22 levels of the 21-D Henon-Heiles
     # model on SG4 L=2 (same potential file as the 6-D case), from a Davidson run with
     # conv_resi = 5e-4 au.  The oracle's dense spectrum lies at or below each level, within
-    # 2e-7 au.  (The library's term tables hold at most 16 modes, so only the oracle runs it.)
+    # 2e-7 au.  (The GPU library runs the same case in tests/test_gpu_drivers.py.)
     ref = np.array(golden["hh21d_levels"])
     op = O.OracleProblem(S.henon_heiles(21, 2))
     assert (op.Np, op.nterm, op.sum_nb) == (925, 253, 2059)
