@@ -161,7 +161,7 @@ __device__ __forceinline__ void tc_teardown(TcState& st) {
 // (a, k, b, v) at ((a + A*(k + K*b))*ld + v).  A CTA-wide call (all threads, blockDim a
 // multiple of 128), K <= kMaxKp, M <= kMaxNp.  FastDiv: the divisor type of the caller.
 template <typename Div>
-__device__ void contract_tc(TcState& st, const float* __restrict__ in, int64_t ldi, float* __restrict__ out,
+__device__ __noinline__ void contract_tc(TcState& st, const float* __restrict__ in, int64_t ldi, float* __restrict__ out,
                             int64_t ldo, const Div& da, int K, int M, int B, const Div& dvt,
                             const float* __restrict__ mat, float alpha, bool acc) {
   TcSmem* sm = st.sm;
