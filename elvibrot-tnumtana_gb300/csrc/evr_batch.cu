@@ -897,8 +897,13 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
   int prec = o->prec;
   int64_t c64 = 0, c32 = 0;
   std::vector<double> Eh((size_t)nsys * M), Eold((size_t)nsys * nlev, 1e300), rn((size_t)nsys * d.nkeep);
-  double best_r = 1e300;
-  int stall = 0, it = 0;
+  // FP32 phase of the mixed form, per problem: best residual so far, iterations without
+  // halving it, and whether the problem has reached its FP32 floor (it then waits, taking
+  // no H.psi, until every problem has)
+  std::vector<double> best_q(nsys, 1e300);
+  std::vector<int> stall_q(nsys, 0);
+  std::vector<unsigned char> floor_q(nsys, 0);
+  int it = 0, it32 = 0;
   bool converged = false;
   for (it = 0; it < o->max_it; ++it) {
     if ((rc = d.hop(d.Pt.d() + n0, M, d.HPt.d() + n0, M, n1 - n0, prec, c64, c32))) return rc;
@@ -918,7 +923,7 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
       return set_error(c, EVR_EDEVICE, "evr_batch_davidson: residual norms");
     if (jerr) return set_error(c, EVR_EDEVICE, "evr_batch_davidson: inconsistent eigenvalue order in the Jacobi kernel");
     const int nt = std::min(nlev, k);
-    double rmax = 0.0;
+    std::vector<double> rq(nsys, 0.0);
     std::vector<std::vector<int>> todo(nsys);
     size_t most = 0;
     for (int q = 0; q < nsys; ++q) {
@@ -927,7 +932,7 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
         const double e = Eh[(size_t)q * M + j];
         const double de = std::fabs(e - Eold[(size_t)q * nlev + j]);
         Eold[(size_t)q * nlev + j] = e;
-        rmax = std::max(rmax, r);
+        rq[q] = std::max(rq[q], r);
         if (!(r < o->conv_resi && de < o->conv_ene)) todo[q].push_back(j);
       }
       most = std::max(most, todo[q].size());
@@ -939,17 +944,28 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
       break;
     }
     if (prec == EVR_PREC_FP32) {
-      double hscale = 0.0;
-      for (int q = 0; q < nsys; ++q)
-        hscale = std::max(hscale, std::max(std::fabs(Eh[(size_t)q * M]), std::fabs(Eh[(size_t)q * M + nt - 1])));
-      // the FP32 phase ends at a residual of 1e-4 of the level energies, when the largest
-      // residual stops halving, or when every level meets the tolerance; the solve then
-      // continues as the FP64 iteration from the Ritz vectors (in lock step a mixed
-      // refinement would recompute the Ritz vectors' H.psi in FP64 after every subspace
-      // restart, as many FP64 H.psi as the plain solve)
-      const bool floor_hit = rmax < std::max(o->conv_resi, 1e-4 * hscale);
-      if (rmax < 0.5 * best_r) { best_r = rmax; stall = 0; } else ++stall;
-      if (floor_hit || stall >= 1 || most == 0) {
+      // Each problem runs its FP32 phase until its largest residual reaches 1e-4 of its
+      // level energies, stops halving for two iterations, or meets the tolerance; it then
+      // waits (no H.psi, empty new columns) while the others go on.  When every problem has
+      // reached its floor the whole batch continues as the FP64 iteration from the Ritz
+      // vectors (in lock step a mixed refinement would recompute the Ritz vectors' H.psi
+      // in FP64 after every subspace restart, as many FP64 H.psi as the plain solve).
+      ++it32;
+      bool all_floor = nt == nlev;
+      for (int q = 0; q < nsys && nt == nlev; ++q) {
+        if (floor_q[q]) continue;
+        const double hs = std::max(std::fabs(Eh[(size_t)q * M]), std::fabs(Eh[(size_t)q * M + nt - 1]));
+        if (rq[q] < 0.5 * best_q[q]) {
+          best_q[q] = rq[q];
+          stall_q[q] = 0;
+        } else {
+          ++stall_q[q];
+        }
+        if (rq[q] < std::max(o->conv_resi, 1e-4 * hs) || stall_q[q] >= 2 || todo[q].empty()) floor_q[q] = 1;
+        all_floor = all_floor && floor_q[q];
+      }
+      // a cap on the FP32 phase: half of the iteration budget
+      if (all_floor || it32 >= std::max(2, o->max_it / 2)) {
         const int kr = std::min(k, nlev);
         if (cudaMemcpy2DAsync(d.Pt.p, sizeof(double) * M, d.X.p, sizeof(double) * d.nkeep, sizeof(double) * kr, N,
                               cudaMemcpyDeviceToDevice, s) ||
@@ -960,10 +976,10 @@ extern "C" int evr_batch_davidson(evr_ctx* c, const evr_davidson_opts* o, double
         n0 = 0;
         std::fill(Eold.begin(), Eold.end(), 1e300);
         std::fill(d.active.begin(), d.active.end(), 1);  // every problem continues in FP64
-        best_r = 1e300;
-        stall = 0;
         continue;
       }
+      for (int q = 0; q < nsys; ++q)
+        if (floor_q[q]) d.active[q] = 0;  // waits for the others at its FP32 floor
     }
     // new directions: per problem its lowest unconverged levels, filled up with its other
     // levels so that every problem adds the same number of columns

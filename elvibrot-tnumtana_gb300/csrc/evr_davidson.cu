@@ -3,15 +3,16 @@
 // Follows sub_propagation_Davidson (Source_ElVibRot/sub_propagation/sub_module_Davidson.f90:54-748):
 //   H.psi of the new vectors (sub_MakeHPsi_Davidson :880-1024) -> projected matrix
 //   (sub_MakeH_Davidson :1028-1143, symmetrised as sub_hermitic_H) -> dense eigensolve
-//   (diagonalization type 3, here cuSOLVER syevd on the device) -> residuals
+//   (diagonalization type 3, here a parallel Jacobi kernel on the device) -> residuals
 //   g_j = sum_i (H psi_i - E_j psi_i) V_ij (MakeResidual_Davidson :1214-1288) and the
 //   convergence tests on |dE| and |g| (:407-449) -> new vectors from the residuals with a
 //   diagonal preconditioner (NewVec_type 4, :1424-1445, with the separable harmonic
 //   energies as the diagonal) -> two classical Gram-Schmidt passes (:1513-1529) ->
 //   restart from the Ritz vectors when the subspace is full (:491-595).
 // Everything stays on the device in FP64; the vector blocks use the library's
-// interleaved layout (row k of the N x ld block holds component k of every vector), so
-// the projections are cuBLAS DGEMMs on the column-major transposes.
+// interleaved layout (row k of the N x ld block holds component k of every vector).  The
+// projections, combinations and the projected eigenproblem are the hand-written,
+// deterministic kernels of evr_dense.cuh (no BLAS or LAPACK library).
 //
 // Mixed precision (prec = EVR_PREC_FP32): the iteration first runs with FP32 contractions
 // in H.psi.  When the residuals reach the FP32 floor (or stop decreasing) the subspace is
@@ -29,9 +30,7 @@
 #include <numeric>
 #include <vector>
 
-#include <cublas_v2.h>
-#include <cusolverDn.h>
-
+#include "evr_dense.cuh"
 #include "evr_internal.h"
 
 using namespace evr;
@@ -45,25 +44,6 @@ struct DevBuf {
   }
   cudaError_t alloc(size_t n) { return cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(double)); }
 };
-
-// sum of squares of each column of an interleaved N x k block (ld), accumulated into out[k]
-__global__ void col_norm2_kernel(const double* __restrict__ x, int64_t ld, int64_t N, int k, double* __restrict__ out) {
-  __shared__ double red[8][33];
-  const int c = blockIdx.y * 32 + threadIdx.x;
-  double s = 0.0;
-  if (c < k)
-    for (int64_t r = blockIdx.x * 8 + threadIdx.y; r < N; r += (int64_t)gridDim.x * 8) {
-      const double v = x[r * ld + c];
-      s = fma(v, v, s);
-    }
-  red[threadIdx.y][threadIdx.x] = s;
-  __syncthreads();
-  if (threadIdx.y == 0 && c < k) {
-    double t = 0.0;
-    for (int i = 0; i < 8; ++i) t += red[i][threadIdx.x];
-    atomicAdd(out + c, t);
-  }
-}
 
 // R[k, j] = HX[k, j] - E[j] X[k, j] for j < nt (interleaved, ld = ldk)
 __global__ void residual_kernel(const double* __restrict__ X, const double* __restrict__ HX, int64_t ldk,
@@ -88,19 +68,6 @@ __global__ void precondition_kernel(const double* __restrict__ R, int64_t ldr, c
     double den = E[j] - d[r];
     if (fabs(den) < floor_) den = den < 0 ? -floor_ : floor_;
     T[r * ldt + s] = R[r * ldr + j] / den;
-  }
-}
-
-// symmetrise the leading n x n block of a column-major matrix: A = (A + A^T)/2
-__global__ void symmetrize_kernel(double* A, int lda, int n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)n * n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int r = (int)(i % n), c = (int)(i / n);
-    if (r < c) {
-      const double v = 0.5 * (A[r + (int64_t)lda * c] + A[c + (int64_t)lda * r]);
-      A[r + (int64_t)lda * c] = v;
-      A[c + (int64_t)lda * r] = v;
-    }
   }
 }
 
@@ -155,65 +122,93 @@ void small_eigh(int n, std::vector<double> a, std::vector<double>& val, std::vec
 struct Davidson {
   evr_ctx* c;
   cudaStream_t s;
-  cublasHandle_t blas = nullptr;
-  cusolverDnHandle_t solver = nullptr;
   int64_t N = 0;
   int M = 0;        // max subspace (columns of Pt/HPt)
   int nkeep = 0;    // Ritz vectors kept at a restart
   int bmax = 0;     // new vectors per iteration
   int op = OP_H;
-  DevBuf Pt, HPt, X, HX, R, T, Hs, Hw, V, E, C, W, nrm, ework, Tt;
-  int* info_d = nullptr;
+  DevBuf Pt, HPt, X, HX, R, T, Hs, Hw, V, E, C, W, nrm, Tt;
+  DevBuf part, wa, wv;   // partial sums of the row chunks; Jacobi working matrices
   int* sel_d = nullptr;
-  int lwork = 0;
+  int* word_d = nullptr;
+  int64_t rows_per_chunk = 0;
+  int nchunk = 0, jgrid = 0;
   std::string err;
 
   ~Davidson() {
-    if (blas) cublasDestroy(blas);
-    if (solver) cusolverDnDestroy(solver);
-    if (info_d) cudaFree(info_d);
     if (sel_d) cudaFree(sel_d);
+    if (word_d) cudaFree(word_d);
   }
 
   int fail(int code, const std::string& m) { return set_error(c, code, "evr_davidson: " + m); }
 
   int init() {
-    if (cublasCreate(&blas) != CUBLAS_STATUS_SUCCESS) return fail(EVR_EDEVICE, "cublasCreate");
-    if (cusolverDnCreate(&solver) != CUSOLVER_STATUS_SUCCESS) return fail(EVR_EDEVICE, "cusolverDnCreate");
-    cublasSetStream(blas, s);
-    cusolverDnSetStream(solver, s);
-    cublasSetPointerMode(blas, CUBLAS_POINTER_MODE_HOST);
+    if (M > dense::kMaxEig) return fail(EVR_EINVAL, "subspace larger than 512 vectors (max_dim)");
     const size_t nm = (size_t)N * M;
+    // row chunks of the projections: about two per SM, at least 256 rows each
+    rows_per_chunk = std::max<int64_t>(256, (N + 2 * c->num_sms - 1) / (2 * c->num_sms));
+    nchunk = (int)((N + rows_per_chunk - 1) / rows_per_chunk);
+    const int np = (M + 1) & ~1;
     if (Pt.alloc(nm) || HPt.alloc(nm) || X.alloc((size_t)N * nkeep) || HX.alloc((size_t)N * nkeep) ||
         R.alloc((size_t)N * nkeep) || T.alloc((size_t)N * bmax) || Tt.alloc((size_t)N * bmax) ||
         Hs.alloc((size_t)M * M) || Hw.alloc((size_t)M * M) || V.alloc((size_t)M * M) || E.alloc(M) ||
-        C.alloc((size_t)M * bmax) || W.alloc((size_t)bmax * bmax) || nrm.alloc(M))
+        C.alloc((size_t)M * bmax) || W.alloc((size_t)bmax * bmax) || nrm.alloc(M) ||
+        part.alloc((size_t)nchunk * std::max<int64_t>((int64_t)M * M, nkeep)) || wa.alloc((size_t)np * np) ||
+        wv.alloc((size_t)np * np))
       return fail(EVR_ENOMEM, "device allocation");
-    if (cudaMalloc(&info_d, sizeof(int)) || cudaMalloc(&sel_d, sizeof(int) * bmax))
+    if (cudaMalloc(&sel_d, sizeof(int) * bmax) || cudaMalloc(&word_d, sizeof(int) * np))
       return fail(EVR_ENOMEM, "device allocation");
-    if (cusolverDnDsyevd_bufferSize(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, M, Hw.p, M, E.p,
-                                    &lwork) != CUSOLVER_STATUS_SUCCESS)
-      return fail(EVR_EDEVICE, "syevd buffer size");
-    if (ework.alloc(lwork)) return fail(EVR_ENOMEM, "device allocation");
+    int coop = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device) != cudaSuccess || !coop)
+      return fail(EVR_EDEVICE, "cooperative launch not supported");
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dense::jacobi_coop_kernel, 256, 0) != cudaSuccess ||
+        per_sm < 1)
+      return fail(EVR_EDEVICE, "Jacobi kernel occupancy");
+    jgrid = std::min(32, c->num_sms * per_sm);
     return EVR_OK;
   }
 
-  // C(na x nb) = A_rows^T-product: sum_k A[k, a0+i] * B[k, b0+j] for interleaved blocks
+  // C(na x nb) = sum_r A[r, i] * B[r, j] over the N rows of interleaved blocks (+ beta C)
   int gram(const double* A, int lda, const double* B, int ldb, int na, int nb, double* Cm, int ldc, double beta = 0.0) {
-    const double one = 1.0;
-    if (cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_T, na, nb, (int)N, &one, A, lda, B, ldb, &beta, Cm, ldc) !=
-        CUBLAS_STATUS_SUCCESS)
-      return fail(EVR_EDEVICE, "cublasDgemm (gram)");
-    return EVR_OK;
+    if (na < 1 || nb < 1) return EVR_OK;
+    const int tiles = ((na + dense::kTile - 1) / dense::kTile) * ((nb + dense::kTile - 1) / dense::kTile);
+    dense::gram_part_kernel<<<dim3(nchunk, tiles), 256, 0, s>>>(A, lda, B, ldb, na, nb, N, rows_per_chunk, part.p);
+    dense::gram_reduce_kernel<<<std::min(1024, (na * nb + 255) / 256), 256, 0, s>>>(part.p, nchunk, na, nb, Cm, ldc,
+                                                                                   beta);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? EVR_OK : fail(EVR_EDEVICE, std::string("gram: ") + cudaGetErrorString(e));
   }
 
   // Y(:, 0:k) = alpha * X_block(:, 0:n) * Mat(n x k) + beta * Y   (interleaved blocks)
   int combine(const double* Xb, int ldx, int n, const double* Mat, int ldm, int k, double* Y, int ldy, double alpha,
               double beta) {
-    if (cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, k, (int)N, n, &alpha, Mat, ldm, Xb, ldx, &beta, Y, ldy) !=
-        CUBLAS_STATUS_SUCCESS)
-      return fail(EVR_EDEVICE, "cublasDgemm (combine)");
-    return EVR_OK;
+    if (k < 1) return EVR_OK;
+    dense::combine_kernel<<<dim3((unsigned)((N + 63) / 64), (unsigned)((k + 31) / 32)), 256, 0, s>>>(
+        Xb, ldx, n, Mat, ldm, k, Y, ldy, alpha, beta, N);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? EVR_OK : fail(EVR_EDEVICE, std::string("combine: ") + cudaGetErrorString(e));
+  }
+
+  // squared norms of the k columns of an interleaved block into out[0..k)
+  int colnorm2(const double* Xb, int ldx, int k, double* out) {
+    dense::colnorm_part_kernel<<<dim3(nchunk, (k + 31) / 32), dim3(32, 8), 0, s>>>(Xb, ldx, k, N, rows_per_chunk,
+                                                                                    part.p);
+    dense::gram_reduce_kernel<<<1, 256, 0, s>>>(part.p, nchunk, k, 1, out, k, 0.0);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? EVR_OK : fail(EVR_EDEVICE, std::string("column norms: ") + cudaGetErrorString(e));
+  }
+
+  // eigenvalues (ascending) and eigenvectors of the symmetric part of A (n x n, ld M)
+  int eigh(const double* A, int n, double* Wv, double* Vm) {
+    int nn = n, lda = M, ldv = M, sweeps = 40;
+    double tol = 1e-15;
+    double* wap = wa.p;
+    double* wvp = wv.p;
+    int* wop = word_d;
+    void* args[] = {(void*)&A, &lda, &nn, &Wv, &Vm, &ldv, &wap, &wvp, &wop, &sweeps, &tol};
+    const cudaError_t e =
+        cudaLaunchCooperativeKernel((const void*)dense::jacobi_coop_kernel, dim3(jgrid), dim3(256), args, 0, s);
+    return e == cudaSuccess ? EVR_OK : fail(EVR_EDEVICE, std::string("Jacobi launch: ") + cudaGetErrorString(e));
   }
 
   int hop(const double* x, int ldx, double* y, int ldy, int n, int prec, int64_t& cnt64, int64_t& cnt32) {
@@ -280,23 +275,12 @@ struct Davidson {
     const int kx = std::min(ke, n0);
     if (kx > 0 && (rc = gram(HPt.p, M, Pt.p + n0, M, kx, n1 - n0, Hs.p + (size_t)M * n0, M))) return rc;
     // mirror the new columns into the new rows: Hs(n0:n1, 0:n0) = Hs(0:n0, n0:n1)^T
-    const double one = 1.0, zero = 0.0;
-    if (n0 > 0 && cublasDgeam(blas, CUBLAS_OP_T, CUBLAS_OP_N, n1 - n0, n0, &one, Hs.p + (size_t)M * n0, M, &zero,
-                              Hs.p + n0, M, Hs.p + n0, M) != CUBLAS_STATUS_SUCCESS)
-      return fail(EVR_EDEVICE, "cublasDgeam");
-    if (cudaMemcpy2DAsync(Hw.p, sizeof(double) * M, Hs.p, sizeof(double) * M, sizeof(double) * n1, n1,
-                          cudaMemcpyDeviceToDevice, s))
-      return fail(EVR_EDEVICE, "copy");
-    symmetrize_kernel<<<64, 256, 0, s>>>(Hw.p, M, n1);
-    if (cusolverDnDsyevd(solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n1, Hw.p, M, E.p, ework.p, lwork,
-                         info_d) != CUSOLVER_STATUS_SUCCESS)
-      return fail(EVR_EDEVICE, "cusolverDnDsyevd");
-    int info = 0;
+    if (n0 > 0) dense::mirror_kernel<<<64, 256, 0, s>>>(Hs.p, M, n0, n1);
+    // eigenpairs of the symmetric part (sub_hermitic_H), eigenvectors into Hw
+    if ((rc = eigh(Hs.p, n1, E.p, Hw.p))) return rc;
     Eh.resize(n1);
-    if (cudaMemcpyAsync(Eh.data(), E.p, sizeof(double) * n1, cudaMemcpyDeviceToHost, s) ||
-        cudaMemcpyAsync(&info, info_d, sizeof(int), cudaMemcpyDeviceToHost, s) || cudaStreamSynchronize(s))
+    if (cudaMemcpyAsync(Eh.data(), E.p, sizeof(double) * n1, cudaMemcpyDeviceToHost, s) || cudaStreamSynchronize(s))
       return fail(EVR_EDEVICE, "copy eigenvalues");
-    if (info != 0) return fail(EVR_EDEVICE, "syevd info " + std::to_string(info));
     return EVR_OK;
   }
 };
@@ -386,11 +370,7 @@ extern "C" int evr_davidson(evr_ctx* c, const evr_davidson_opts* o, const double
     if ((rc = d.combine(d.Pt.p, M, n1, d.Hw.p, M, k, d.X.p, d.nkeep, 1.0, 0.0))) return rc;
     if ((rc = d.combine(d.HPt.p, M, n1, d.Hw.p, M, k, d.HX.p, d.nkeep, 1.0, 0.0))) return rc;
     residual_kernel<<<c->num_sms * 8, 256, 0, s>>>(d.X.p, d.HX.p, d.nkeep, d.E.p, k, N, d.R.p, d.nkeep);
-    if (cudaMemsetAsync(d.nrm.p, 0, sizeof(double) * k, s)) return set_error(c, EVR_EDEVICE, "memset");
-    {
-      dim3 blk(32, 8), grd((unsigned)std::min<int64_t>((N + 7) / 8, 4096), (unsigned)((k + 31) / 32));
-      col_norm2_kernel<<<grd, blk, 0, s>>>(d.R.p, d.nkeep, N, k, d.nrm.p);
-    }
+    if ((rc = d.colnorm2(d.R.p, d.nkeep, k, d.nrm.p))) return rc;
     if (cudaMemcpyAsync(rnorm.data(), d.nrm.p, sizeof(double) * k, cudaMemcpyDeviceToHost, s) ||
         cudaStreamSynchronize(s))
       return set_error(c, EVR_EDEVICE, "evr_davidson: residual norms");

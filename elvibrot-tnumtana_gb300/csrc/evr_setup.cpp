@@ -126,6 +126,8 @@ bool spd_solve(int nb, std::vector<LD> A, std::vector<LD>& B, int m) {
   return true;
 }
 
+bool finish_basis(Basis1D& b);
+
 // One HO primitive basis ("HO"/"Hm", type 20) on its Gauss-Hermite grid, scaled as in
 // sub_scale_basis (sub_module_basis.f90:1540-1638); grid derivative matrices through the
 // pseudo-inverse of d0b (sub_dnGB_TO_dnGG, :2195-2460), here formed as
@@ -150,7 +152,34 @@ bool build_basis(Basis1D& b, int nb, int nq, double scaleQ, double Q0) {
     }
   }
   for (int q = 0; q < nq; ++q) { b.x[q] = Q0 + b.x[q] / scaleQ; b.w[q] = b.w[q] * (1.0 / scaleQ); }
-  // P = (d0b^T d0b)^-1 d0b^T
+  return finish_basis(b);
+}
+
+// A primitive basis given by the host as tables on its grid (the reference's tables after
+// construct_primitive_basis and sub_scale_basis, sub_module_basis.f90:391-782, 1540-1638):
+// x, w (nq), d0b, d1b, d2b (nq x nb, column-major); the grid derivative matrices and the
+// weighted transpose follow as for the built bases.
+bool basis_from_tables(Basis1D& b, const evr_basis1d& t) {
+  const int nq = t.nq, nb = t.nb;
+  if (nb < 1 || nq < nb || nq > kMaxN1 || !t.x || !t.w || !t.d0b || !t.d1b || !t.d2b) return false;
+  b.nb = nb; b.nq = nq;
+  b.x.assign(t.x, t.x + nq);
+  b.w.assign(t.w, t.w + nq);
+  const size_t n = (size_t)nq * nb;
+  b.d0b.assign(t.d0b, t.d0b + n);
+  b.d1b.assign(t.d1b, t.d1b + n);
+  b.d2b.assign(t.d2b, t.d2b + n);
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(b.d0b[i]) || !std::isfinite(b.d1b[i]) || !std::isfinite(b.d2b[i])) return false;
+  for (int q = 0; q < nq; ++q)
+    if (!std::isfinite(b.x[q]) || !(b.w[q] > 0.0)) return false;
+  return finish_basis(b);
+}
+
+// Grid derivative matrices through the pseudo-inverse of d0b (sub_dnGB_TO_dnGG,
+// sub_module_basis.f90:2195-2460), P = (d0b^T d0b)^-1 d0b^T, and bgw = d0b^T diag(w).
+bool finish_basis(Basis1D& b) {
+  const int nb = b.nb, nq = b.nq;
   std::vector<LD> A((size_t)nb * nb), P((size_t)nb * nq);
   for (int i = 0; i < nb; ++i) for (int j = 0; j < nb; ++j) {
     LD t = 0.0L;
@@ -286,8 +315,23 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
       for (int L = 0; L <= P.LG; ++L) {
         int nq = d->Aq[i] + d->Bq[i] * L, nb = d->Ab[i] + d->Bb[i] * L;
         double s = d->scaleQ ? d->scaleQ[i] : 1.0, q0 = d->Q0 ? d->Q0[i] : 0.0;
+        if (d->bases) {  // the host's tables of (mode i, level L)
+          const evr_basis1d& t = d->bases[(size_t)i * (d->LG + 1) + L];
+          if (t.nq != nq || t.nb != nb) {
+            err = "host basis table of mode " + std::to_string(i) + " level " + std::to_string(L) +
+                  " has nq, nb = " + std::to_string(t.nq) + ", " + std::to_string(t.nb) + "; the level rules give " +
+                  std::to_string(nq) + ", " + std::to_string(nb);
+            return EVR_EINVAL;
+          }
+          if (!basis_from_tables(P.bas[i][L], t)) {
+            err = "invalid host basis table (null or non-finite arrays, non-positive weights, or a singular basis) "
+                  "at mode " + std::to_string(i) + " level " + std::to_string(L);
+            return EVR_EINVAL;
+          }
+          continue;
+        }
         if (!(s > 0.0) || !build_basis(P.bas[i][L], nb, nq, s, q0)) {
-          err = "invalid 1-D basis (need 1 <= nb <= nq <= 32, scaleQ > 0) at mode " + std::to_string(i);
+          err = "invalid 1-D basis (need 1 <= nb <= nq <= 24, scaleQ > 0) at mode " + std::to_string(i);
           return EVR_EINVAL;
         }
       }
@@ -306,8 +350,15 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
     for (int i = 0; i < D; ++i) {
       P.bas[i].resize(1);
       double s = d->scaleQ ? d->scaleQ[i] : 1.0, q0 = d->Q0 ? d->Q0[i] : 0.0;
-      if (!(s > 0.0) || !build_basis(P.bas[i][0], d->nb_dp[i], d->nq_dp[i], s, q0)) {
-        err = "invalid 1-D basis (need 1 <= nb <= nq <= 32, scaleQ > 0) at mode " + std::to_string(i);
+      if (d->bases) {
+        const evr_basis1d& t = d->bases[i];
+        if (t.nq != d->nq_dp[i] || t.nb != d->nb_dp[i] || !basis_from_tables(P.bas[i][0], t)) {
+          err = "invalid host basis table at mode " + std::to_string(i) +
+                " (sizes must equal nq_dp, nb_dp; finite arrays, positive weights, a regular basis)";
+          return EVR_EINVAL;
+        }
+      } else if (!(s > 0.0) || !build_basis(P.bas[i][0], d->nb_dp[i], d->nq_dp[i], s, q0)) {
+        err = "invalid 1-D basis (need 1 <= nb <= nq <= 24, scaleQ > 0) at mode " + std::to_string(i);
         return EVR_EINVAL;
       }
       nbmax[i] = d->nb_dp[i];
@@ -602,11 +653,47 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
   std::vector<double> vconst(nb0, 0.0);
   for (int m = 0; m < d->n_mono; ++m)
     if (P.mono_idx[4 * m] < 0 && P.mono_elec[2 * m] == P.mono_elec[2 * m + 1]) vconst[P.mono_elec[2 * m]] += P.mono_coef[m];
+  // With host tables (any primitive basis) the diagonal is that of the separable part of H
+  // on the largest basis of each mode: -1/2 G0_ii <n|d2|n> plus <n|V_i|n> for the monomials
+  // of mode i alone, both by the mode's own quadrature.
+  std::vector<std::vector<double>> e1(D);
+  if (d->bases)
+    for (int i = 0; i < D; ++i) {
+      const Basis1D& b = P.bas[i].back();
+      e1[i].assign(b.nb + 1, 0.0);
+      for (int n = 0; n < b.nb; ++n) {
+        double t = 0.0, v = 0.0;
+        for (int q = 0; q < b.nq; ++q) {
+          const double f = b.d0b[q + (size_t)b.nq * n];
+          t += b.w[q] * f * b.d2b[q + (size_t)b.nq * n];
+          double vq = 0.0;
+          for (int m = 0; m < d->n_mono; ++m) {
+            if (P.mono_elec[2 * m] != 0 || P.mono_elec[2 * m + 1] != 0) continue;
+            bool alone = P.mono_idx[4 * m] >= 0;
+            double term = P.mono_coef[m];
+            for (int r = 0; r < 4 && alone; ++r) {
+              const int ix = P.mono_idx[4 * m + r];
+              if (ix < 0) continue;
+              if (ix != i) alone = false;
+              else term *= b.x[q];
+            }
+            if (alone) vq += term;
+          }
+          v += b.w[q] * f * f * vq;
+        }
+        e1[i][n + 1] = -0.5 * P.G0[i + (size_t)D * i] * t + v;
+      }
+    }
   for (int64_t k = 0; k < P.Np; ++k) {
     double e = 0.0;
     for (int i = 0; i < D; ++i) {
-      double s = d->scaleQ ? d->scaleQ[i] : 1.0;
-      e += P.G0[i + (size_t)D * i] * s * s * (P.packed[(size_t)k * D + i] - 0.5);
+      const int n = P.packed[(size_t)k * D + i];
+      if (d->bases) {
+        e += e1[i][n];
+      } else {
+        double s = d->scaleQ ? d->scaleQ[i] : 1.0;
+        e += P.G0[i + (size_t)D * i] * s * s * (n - 0.5);
+      }
     }
     for (int a = 0; a < nb0; ++a) P.e0diag[k + P.Np * a] = e + vconst[a];
   }

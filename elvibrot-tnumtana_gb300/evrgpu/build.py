@@ -1,7 +1,7 @@
 """Builds libevrgpu.so (the sm_103a H.psi library) in-tree with nvcc.
 
 The translation units are compiled in parallel and linked against the CUDA runtime,
-cuBLAS and cuSOLVER.  Output: elvibrot-tnumtana_gb300/_build/libevrgpu.so.
+the CUDA runtime only (no BLAS or LAPACK library).  Output: elvibrot-tnumtana_gb300/_build/libevrgpu.so.
 """
 from __future__ import annotations
 
@@ -60,7 +60,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
         objs = list(ex.map(comp, srcs))
     tmp = LIB + ".tmp"
-    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcublas", "-lcusolver", "-lcudart", "-lpthread"]
+    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

@@ -34,11 +34,17 @@ class EvrError(RuntimeError):
         self.code = code
 
 
+class Basis1D(C.Structure):
+    _fields_ = [("nq", C.c_int), ("nb", C.c_int), ("x", _dp), ("w", _dp), ("d0b", _dp), ("d1b", _dp),
+                ("d2b", _dp)]
+
+
 class ProblemDesc(C.Structure):
     _fields_ = [("kind", C.c_int), ("D", C.c_int), ("nb0", C.c_int), ("LG", C.c_int), ("LB", C.c_int),
                 ("Aq", _ip), ("Bq", _ip), ("Ab", _ip), ("Bb", _ip), ("nq_dp", _ip), ("nb_dp", _ip),
                 ("scaleQ", _dp), ("Q0", _dp), ("n_mono", C.c_int), ("mono_coef", _dp), ("mono_idx", _ip),
-                ("mono_elec", _ip), ("keo_type", C.c_int), ("G0", _dp), ("g", _dp)]
+                ("mono_elec", _ip), ("keo_type", C.c_int), ("G0", _dp), ("g", _dp),
+                ("bases", C.POINTER(Basis1D))]
 
 
 class Sizes(C.Structure):
@@ -200,6 +206,19 @@ def _describe(spec, keep):
     d.keo_type = spec.keo_type
     d.G0 = F(np.asarray(spec.G0).ravel(order="F"))
     d.g = F(np.asarray(spec.g).ravel(order="F"))
+    if getattr(spec, "bases", None) is not None:
+        # host tables of the primitive bases, (mode, level) order: dicts with x, w and the
+        # nq x nb arrays d0b, d1b, d2b
+        arr = (Basis1D * len(spec.bases))()
+        for k, t in enumerate(spec.bases):
+            d0 = np.asarray(t["d0b"])
+            arr[k].nq, arr[k].nb = int(d0.shape[0]), int(d0.shape[1])
+            arr[k].x, arr[k].w = F(t["x"]), F(t["w"])
+            arr[k].d0b = F(np.asarray(t["d0b"]).ravel(order="F"))
+            arr[k].d1b = F(np.asarray(t["d1b"]).ravel(order="F"))
+            arr[k].d2b = F(np.asarray(t["d2b"]).ravel(order="F"))
+        keep.append(arr)
+        d.bases = C.cast(arr, C.POINTER(Basis1D))
     return d
 
 

@@ -75,6 +75,9 @@ class ProblemSpec:
     dip_coef: np.ndarray = None    # optional dipole mu(Q), monomials like the potential
     dip_idx: np.ndarray = None
     dip_elec: np.ndarray = None
+    # optional host tables of the primitive bases ((mode, level) order: dicts with x, w,
+    # d0b, d1b, d2b on the grid); None: HO bases on Gauss-Hermite grids
+    bases: list = None
     name: str = ""
     extra: dict = field(default_factory=dict)
 

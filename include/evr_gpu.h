@@ -57,9 +57,23 @@ typedef struct evr_ctx evr_ctx;
  *   (Source_ElVibRot/sub_Operator/sub_OpPsi_SG4.f90:1354-1668).
  * The library builds all tables itself from these few numbers.
  */
+/* A primitive basis of one (mode, level) given as tables on its grid, as the reference holds
+ * them after construct_primitive_basis and sub_scale_basis
+ * (Source_ElVibRot/sub_Basis/sub_module_basis.f90:391-782, 1540-1638): any primitive
+ * basis and any grid (for instance non-HO bases, or the Nested=1 Hermite grids of
+ * grid_HermiteNested1, :734-822).  x, w: nq grid points and weights (wrho); d0b, d1b, d2b:
+ * the basis functions and their first and second derivatives on the grid, nq x nb,
+ * column-major.  The library forms d0b^T w and the grid derivatives d1b pinv(d0b),
+ * d2b pinv(d0b) (sub_dnGB_TO_dnGG, :2195-2460) itself. */
+typedef struct evr_basis1d {
+  int nq, nb;
+  const double *x, *w;
+  const double *d0b, *d1b, *d2b;
+} evr_basis1d;
+
 typedef struct evr_problem_desc {
   int kind;              /* EVR_BASIS_SG4 or EVR_BASIS_DP                          */
-  int D;                 /* number of modes, 1..16                                  */
+  int D;                 /* number of modes, 1..24                                  */
   int nb0;               /* electronic states (nb_elec), >= 1                       */
   int LG, LB;            /* SG4: L_SparseGrid, L_SparseBasis (LB <= LG)             */
   const int *Aq, *Bq;    /* SG4: nq(l) = Aq[i] + Bq[i]*l   (L_TO_nq_A/B)            */
@@ -79,6 +93,11 @@ typedef struct evr_problem_desc {
   int keo_type;
   const double *G0;      /* D*D column-major, NULL = identity                       */
   const double *g;       /* D*D*D, NULL = 0                                          */
+  /* optional host tables of the primitive bases: SG4 D*(LG+1) entries, (mode i, level L)
+   * at bases[i*(LG+1) + L], sizes equal to the level rules Aq/Bq/Ab/Bb; DP D entries with
+   * sizes nq_dp, nb_dp.  NULL: harmonic-oscillator bases on Gauss-Hermite grids scaled by
+   * scaleQ and Q0, which are then unused. */
+  const evr_basis1d *bases;
 } evr_problem_desc;
 
 /* sizes reported by evr_sizes(): */

@@ -96,3 +96,24 @@ def test_batch_davidson_equals_single_problems():
     assert st32["hpsi_fp32"] > 0
     # mixed form: within 1e-4 cm-1 of the FP64 levels
     assert np.abs(e32 - e64).max() * S.AU_TO_CM <= 1e-4
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_batch_davidson_matches_oracle_dense_spectra(prec):
+    # every problem of a batch against the oracle's dense spectrum of the same operator (its
+    # symmetric part, the operator the Davidson uses when nq > nb), 1e-9 au, in FP64 and in
+    # the mixed form (per-problem FP32 phase, FP64 continuation)
+    from oracle import oracle as O
+
+    sp = specs()[:4]
+    b = E.BatchProblem(sp, device=0)
+    nlev = 6
+    e, st = b.davidson(nlev, block=8, conv_resi=1e-8, conv_ene=1e-11, prec=prec)
+    assert st["converged"], st
+    if prec == "fp32":
+        assert st["hpsi_fp32"] > 0 and st["hpsi_fp64"] > 0
+    for q, s1 in enumerate(sp):
+        H = O.OracleProblem(s1).dense()
+        ref = np.linalg.eigvalsh(0.5 * (H + H.T))[:nlev]
+        assert np.abs(e[q] - ref).max() <= 1e-9, q
