@@ -318,6 +318,14 @@ __device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64
   }
 }
 
+// contract() as one out-of-line function: the FP32 slab kernel calls it from many sites,
+// which would otherwise each carry their own copy of every size bucket
+__device__ __noinline__ void contract_cc32(const float* in, int64_t ldi, float* out, int64_t ldo, const FastDiv& A,
+                                           int K, int M, int B, const FastDiv& Vt, const float* mat, float alpha,
+                                           bool acc) {
+  contract<float>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+}
+
 // contract() or, for FP32 with a tensor-core state, the tcgen05 contraction (K <= 24,
 // M <= 32, K*M at least the state's threshold).  CTA-wide either way.
 template <typename T>
@@ -330,8 +338,10 @@ __device__ __forceinline__ void contract_x(tc::TcState* ts, const T* in, int64_t
       tc::contract_tc(*ts, in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
       return;
     }
+    contract_cc32(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  } else {
+    contract<T>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
   }
-  contract<T>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
 }
 
 // First B->G mode fused with the gather from the packed vector block:
