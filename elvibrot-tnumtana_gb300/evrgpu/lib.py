@@ -77,6 +77,7 @@ VGRID_LAYOUT = {"terms": 0, "ref": 1}
 WP_FORMAT = {"v0": 0, "v1": 1, "unformatted": 2, "sparse": 3}
 
 _lib = None
+_build_error = None  # a failed build is reported once per process, not retried by every call
 
 
 def library_path() -> str:
@@ -85,11 +86,17 @@ def library_path() -> str:
 
 def load(build: bool = True):
     """Load (building first if needed) libevrgpu.so and declare its signatures."""
-    global _lib
+    global _lib, _build_error
     if _lib is not None:
         return _lib
+    if _build_error is not None:
+        raise EvrError(EVR_EDEVICE, f"libevrgpu.so failed to build earlier in this process: {_build_error}")
     if build:
-        _build.build()
+        try:
+            _build.build()
+        except Exception as e:
+            _build_error = str(e)[-2000:]
+            raise
     if not os.path.exists(_build.LIB):
         raise EvrError(EVR_EDEVICE, f"{_build.LIB} is missing: build the CUDA library first")
     L = C.CDLL(_build.LIB)
