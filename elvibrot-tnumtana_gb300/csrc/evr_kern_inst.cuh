@@ -16,8 +16,16 @@ template <typename T, bool GFLY>
 cudaError_t set_slab_kernel_smem(int bytes) {
   return cudaFuncSetAttribute(hpsi_slab_kernel<T, GFLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
+template <typename T, bool GFLY>
+cudaError_t slab_kernel_static_smem(int* bytes) {
+  cudaFuncAttributes a;
+  const cudaError_t e = cudaFuncGetAttributes(&a, hpsi_slab_kernel<T, GFLY>);
+  *bytes = e == cudaSuccess ? (int)a.sharedSizeBytes : 0;
+  return e;
+}
 template cudaError_t launch_slab_kernel<EVR_KT, EVR_KGFLY>(int, size_t, cudaStream_t, const ItemParams<EVR_KT>&);
 template cudaError_t set_slab_kernel_smem<EVR_KT, EVR_KGFLY>(int);
+template cudaError_t slab_kernel_static_smem<EVR_KT, EVR_KGFLY>(int*);
 #else
 template <typename T, bool GFLY>
 cudaError_t launch_items_kernel(int grid, size_t smem, cudaStream_t s, const ItemParams<T>& p) {
@@ -32,8 +40,16 @@ template <typename T, bool GFLY>
 cudaError_t occupancy_items_kernel(int* per_sm, int smem_bytes) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, hpsi_items_kernel<T, GFLY>, kThreads, smem_bytes);
 }
+template <typename T, bool GFLY>
+cudaError_t items_kernel_static_smem(int* bytes) {
+  cudaFuncAttributes a;
+  const cudaError_t e = cudaFuncGetAttributes(&a, hpsi_items_kernel<T, GFLY>);
+  *bytes = e == cudaSuccess ? (int)a.sharedSizeBytes : 0;
+  return e;
+}
 template cudaError_t launch_items_kernel<EVR_KT, EVR_KGFLY>(int, size_t, cudaStream_t, const ItemParams<EVR_KT>&);
 template cudaError_t set_items_kernel_smem<EVR_KT, EVR_KGFLY>(int);
+template cudaError_t items_kernel_static_smem<EVR_KT, EVR_KGFLY>(int*);
 template cudaError_t occupancy_items_kernel<EVR_KT, EVR_KGFLY>(int*, int);
 #endif
 

@@ -253,6 +253,32 @@ void free_workspace(evr_ctx* c) {
 // placed 16-byte aligned at the end of the dynamic shared memory)
 static size_t tc_reserve_bytes() { return (sizeof(tc::TcSmem) + 15) & ~(size_t)15; }
 
+// Dynamic shared memory of the term kernels: the slab kernel takes what one CTA may have
+// (the opt-in maximum less its static block), the general kernel what leaves room for two
+// CTAs per SM (each also holds its static block and the per-block reservation).
+int term_kernel_smem(evr_ctx* c, int* items_bytes, int* slab_bytes) {
+  int optin = 0, per_sm = 0, reserved = 0;
+  EVR_CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attr");
+  EVR_CU(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device), "attr");
+  if (cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, c->device) != cudaSuccess) {
+    (void)cudaGetLastError();
+    reserved = 1024;
+  }
+  int st_slab = 0, st_items = 0, v = 0;
+  EVR_CU((slab_kernel_static_smem<float, false>(&v)), "attr"); st_slab = std::max(st_slab, v);
+  EVR_CU((slab_kernel_static_smem<float, true>(&v)), "attr"); st_slab = std::max(st_slab, v);
+  EVR_CU((slab_kernel_static_smem<double, false>(&v)), "attr"); st_slab = std::max(st_slab, v);
+  EVR_CU((slab_kernel_static_smem<double, true>(&v)), "attr"); st_slab = std::max(st_slab, v);
+  EVR_CU((items_kernel_static_smem<float, false>(&v)), "attr"); st_items = std::max(st_items, v);
+  EVR_CU((items_kernel_static_smem<float, true>(&v)), "attr"); st_items = std::max(st_items, v);
+  EVR_CU((items_kernel_static_smem<double, false>(&v)), "attr"); st_items = std::max(st_items, v);
+  EVR_CU((items_kernel_static_smem<double, true>(&v)), "attr"); st_items = std::max(st_items, v);
+  // multiples of 256 bytes below the limits
+  *slab_bytes = (optin - st_slab) & ~255;
+  *items_bytes = (std::min(optin - st_items, per_sm / 2 - reserved - st_items)) & ~255;
+  return EVR_OK;
+}
+
 // elements of shared memory the slab kernel needs for a term and a vector tile
 static size_t slab_need_elems(const HostProblem& P, const TermDesc& Tm, int vt, bool fp32) {
   const int L = Tm.D - 1;  // the term's own mode count (stacked problems differ)
@@ -290,10 +316,8 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
   const HostProblem& P = c->hp;
   int rc = EVR_OK;
   if (!w.counter) {
-    int optin = 0;
-    EVR_CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attr");
-    w.smem_bytes = std::min(optin, 228 * 1024 / 2) - 2048;   // general kernel: 2 CTAs per SM
-    w.smem_slab_bytes = optin - 2048;                         // slab kernel: 1 CTA per SM
+    // general kernel: 2 CTAs per SM; slab kernel: 1 CTA per SM
+    if ((rc = term_kernel_smem(c, &w.smem_bytes, &w.smem_slab_bytes))) return rc;
     w.grid = c->num_sms * 2;
     w.grid_slab = c->num_sms;
     size_t slab = 0;  // general kernel: FP64 buffers of the terms that run from global memory
@@ -724,13 +748,13 @@ int eval_grid_monomials(evr_ctx* c, int n_mono, const double* coef, const int* i
 int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ldy, int nvec, unsigned char* scratch,
                  size_t scratch_bytes, cudaStream_t s) {
   const HostProblem& P = c->hp;
-  int optin = 0;
-  EVR_CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attr");
   // the general kernel's shared memory of the regular path, so that two CTAs are resident
   // per SM and every CTA of the grid gets its per-CTA buffer in the first wave
-  const int smem_items = std::min(optin, 228 * 1024 / 2) - 2048;
+  int smem_items = 0, smem_slab = 0;
+  int rc0 = term_kernel_smem(c, &smem_items, &smem_slab);
+  if (rc0) return rc0;
   // the same attribute values as ensure_workspace sets, so neither path lowers the other's
-  EVR_CU((set_term_kernel_smem<double, false>(smem_items, optin - 2048)), "attr");
+  EVR_CU((set_term_kernel_smem<double, false>(smem_items, smem_slab)), "attr");
   int per_sm = 0;
   EVR_CU((occupancy_items_kernel<double, false>(&per_sm, smem_items)), "occupancy");
   const int grid = c->num_sms * std::max(1, std::min(per_sm, 2));

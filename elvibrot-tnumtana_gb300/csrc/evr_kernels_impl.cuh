@@ -1264,6 +1264,11 @@ template <typename T, bool GFLY>
 cudaError_t set_items_kernel_smem(int bytes);
 template <typename T, bool GFLY>
 cudaError_t set_slab_kernel_smem(int bytes);
+// static shared memory of the kernels (the dynamic budget is what the SM has left)
+template <typename T, bool GFLY>
+cudaError_t slab_kernel_static_smem(int* bytes);
+template <typename T, bool GFLY>
+cudaError_t items_kernel_static_smem(int* bytes);
 // resident CTAs per SM of the general kernel at a dynamic shared-memory size
 template <typename T, bool GFLY>
 cudaError_t occupancy_items_kernel(int* per_sm, int smem_bytes);
