@@ -206,6 +206,8 @@ def run_profile(args):
     else:
         spec = S.config_sg4(6, 6, seed=1) if args.profile == "sg4_6d_l6" else S.config_sg4_6d_l8()
     p = Problem(spec, device=0)
+    if args.tc:
+        p.set_tensor_cores(True, 64)
     x = torch.randn((p.N, nvec), dtype=torch.float64, device="cuda")
     y = torch.empty_like(x)
     st = torch.cuda.Stream()
@@ -451,6 +453,7 @@ def main():
     ap.add_argument("--profile", default=None, choices=["sg4_6d_l6", "sg4_6d_l8", "dp3"],
                     help="profiling mode: a few H.psi launches of the named workload, nothing else")
     ap.add_argument("--prec", default="both", choices=["both", "fp64", "fp32"], help="precision(s) in profiling mode")
+    ap.add_argument("--tc", action="store_true", help="profiling mode: FP32 contractions on the tensor cores")
     ap.add_argument("--suite", default=None, choices=["dp3", "batch", "prop12d", "control", "all"],
                     help="the other workloads (one JSON line each): direct-product Davidson, 256 batched "
                          "problems, D=12 Chebyshev propagation, optimal-control gradient")
@@ -524,10 +527,19 @@ def main():
         launches = p.last_launch_count()[0] * args.steps
         t32, k32 = timed("fp32", y32)
         launches += p.last_launch_count()[0] * args.steps
+    # the FP32 contractions of the slab kernel on the tcgen05 tensor cores (3xTF32), same block
+    ytc = torch.empty_like(x)
+    p.set_tensor_cores(True, 64)
+    for _ in range(args.warmup):
+        step("fp32", ytc)
+    ttc, ktc = timed("fp32", ytc)
+    p.set_tensor_cores(False)
     total64 = max_over_ranks(sum(t64), "cuda")
     value = job_rate(NVEC * args.steps, total64, world)
     mixed = NVEC * args.steps / sum(t32)
     err32 = float((y32 - y).abs().max() / y.abs().max())
+    errtc = float((ytc - y).abs().max() / y.abs().max())
+    itc = statistics.mean(k[0] for k in ktc)
 
     # end to end through the host entry point with pinned buffers (column-major, as the
     # Fortran host passes TabPsi(:)%RvecB)
@@ -582,7 +594,12 @@ def main():
             "mixed": {"value": mixed, "unit": UNIT, "dtype": "f32 contractions, f64 reduction",
                       "rel_err_vs_fp64": err32, "items_kernel_ms": items32,
                       "achieved_tflops": flop_launch / (items32 / 1e3) / 1e12, "fp32_fma_peak_tflops": fma32,
-                      "frac_of_fp32_fma": flop_launch / (items32 / 1e3) / 1e12 / fma32},
+                      "frac_of_fp32_fma": flop_launch / (items32 / 1e3) / 1e12 / fma32,
+                      "contractions": "CUDA cores (default; the autotuner's choice on this workload)",
+                      "tensor_cores": {"value": NVEC * args.steps / sum(ttc), "unit": UNIT,
+                                       "contractions": "tcgen05 kind::tf32, 3 products of split operands, "
+                                                       "FP32 accumulation in TMEM, K*M >= 64",
+                                       "rel_err_vs_fp64": errtc, "items_kernel_ms": itc}},
             "roofline": {"bound": "fp64-fma", "achieved": achieved, "peak": fma64, "unit": "TFLOP/s",
                          "frac": achieved / fma64, "traffic": TRAFFIC_PER_LAUNCH,
                          "kernel": "hpsi_slab_kernel<double> + hpsi_items_kernel<double>", "items_kernel_ms": items_ms,

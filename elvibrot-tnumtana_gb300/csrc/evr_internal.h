@@ -191,7 +191,8 @@ struct evr_ctx {
   int op_form = 0;                  // EVR_OP_H, EVR_OP_HT or EVR_OP_HSYM
   bool capturing = false;           // inside a stream capture: no event records
   bool use_slab = true;             // slab kernel for the terms that fit (evr_set_kernel_path)
-  bool use_tc = true;               // FP32 slab-kernel contractions on the tensor cores (evr_set_tensor_cores)
+  bool use_tc = false;              // FP32 slab-kernel contractions on the tensor cores (evr_set_tensor_cores;
+                                    // off by default: slower than the CUDA cores at these sizes, see evr_autotune)
   int tc_min_km = 64;               // contractions with K*M below this stay on the CUDA cores
   bool use_stages = true;           // grid-wide stage path for single-term problems
   bool gfly = false;                // G(Q) from the linear model per point instead of a table

@@ -900,6 +900,28 @@ extern "C" int evr_autotune(evr_ctx* c, int nvec, int prec, int* caps, double* b
   c->vt_cap_slab = bs;
   c->vt_cap_items = bi;
   c->slab_min_points = bm;
+  // FP32: the slab kernel's contractions on the CUDA cores or on the tensor cores (above a
+  // size K*M); the decomposition changes with the shared memory the tensor-core block takes
+  if (!rc && prec == EVR_PREC_FP32) {
+    bool btc = c->use_tc;
+    int bkm = c->tc_min_km;
+    const int kms[] = {64, 160, 288};
+    for (int on = 0; on < 2 && !rc; ++on)
+      for (int km : kms) {
+        c->use_tc = on != 0;
+        c->tc_min_km = km;
+        double ms;
+        if ((rc = time_it(ms))) break;
+        if (ms < best) {
+          best = ms;
+          btc = c->use_tc;
+          bkm = km;
+        }
+        if (!on) break;  // the threshold does not matter with the tensor cores off
+      }
+    c->use_tc = btc;
+    c->tc_min_km = bkm;
+  }
   clear_item_sets(c);
   cudaFree(x);
   cudaFree(y);
@@ -908,6 +930,7 @@ extern "C" int evr_autotune(evr_ctx* c, int nvec, int prec, int* caps, double* b
     caps[0] = bs;
     caps[1] = bi;
     caps[2] = bm;
+    caps[3] = c->use_tc ? c->tc_min_km : -1;
   }
   if (best_ms) *best_ms = best;
   return EVR_OK;

@@ -298,24 +298,6 @@ __device__ __forceinline__ void contract_m(const T* __restrict__ in, int64_t ldi
   }
 }
 
-// FP64 contraction with the contraction length K (1..24) as a compile-time constant, so
-// that the FP64 pipe issues exactly K FMAs per output (register budget MG*K <= 24 doubles):
-// one out-of-line function holding all lengths
-#define EVR_MS_CASE(KK, MG) \
-  case KK: contract_ms<double, KK, MG>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
-static __device__ __noinline__ void contract_f64(const double* in, int64_t ldi, double* out, int64_t ldo, const FastDiv& A,
-                                          int K, int M, int B, const FastDiv& Vt, const double* mat, double alpha,
-                                          bool acc) {
-  switch (K) {
-    EVR_MS_CASE(1, 4) EVR_MS_CASE(2, 4) EVR_MS_CASE(3, 4) EVR_MS_CASE(4, 4) EVR_MS_CASE(5, 2) EVR_MS_CASE(6, 2)
-    EVR_MS_CASE(7, 2) EVR_MS_CASE(8, 2) EVR_MS_CASE(9, 2) EVR_MS_CASE(10, 2) EVR_MS_CASE(11, 2) EVR_MS_CASE(12, 2)
-    EVR_MS_CASE(13, 1) EVR_MS_CASE(14, 1) EVR_MS_CASE(15, 1) EVR_MS_CASE(16, 1) EVR_MS_CASE(17, 1)
-    EVR_MS_CASE(18, 1) EVR_MS_CASE(19, 1) EVR_MS_CASE(20, 1) EVR_MS_CASE(21, 1) EVR_MS_CASE(22, 1)
-    EVR_MS_CASE(23, 1) EVR_MS_CASE(24, 1)
-    default: break;  // K <= kMaxN1 = 24 by construction of the tables
-  }
-}
-#undef EVR_MS_CASE
 
 template <typename T>
 __device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64_t ldo, const FastDiv& A, int K, int M,
@@ -327,8 +309,13 @@ __device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64
     else if (M <= 16) contract_m<T, 16, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else if (M <= 20) contract_m<T, 20, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else contract_m<T, 24, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
-  } else {  // FP64: matrix strip in registers, the contraction length exact (no padded FMAs)
-    contract_f64(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+  } else {  // FP64: matrix strip in registers (register budget MG*MAXK <= 24 doubles)
+    if (K <= 4) contract_ms<T, 4, 4>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (K <= 8) contract_ms<T, 8, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (K <= 12) contract_ms<T, 12, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (K <= 16) contract_ms<T, 16, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else if (K <= 20) contract_ms<T, 20, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    else contract_ms<T, 24, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
   }
 }
 

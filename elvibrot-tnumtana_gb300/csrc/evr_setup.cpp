@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <string>
 #include <unordered_map>
 
 #include "evr_internal.h"
@@ -497,15 +498,13 @@ int build_host_problem(const evr_problem_desc* d, HostProblem& P, std::string& e
   // packed basis: SG4 -> all n with sum l(n_i) <= LB, last index fastest
   // (nDindB type 5, ADD_ONE_TO_nDindex_type5p, Source_Lib/sub_nDindex/sub_module_nDindex.f90:2396);
   // DP -> full product, first index fastest.
-  long double radix_prod = 1.0L;
-  for (int i = 0; i < D; ++i) radix_prod *= (long double)(nbmax[i] + 1);
-  if (radix_prod > 9.0e18L) { err = "basis too large for 64-bit tuple keys"; return EVR_EINVAL; }
+  // tuple keys: one byte per mode (n_i <= nb <= 24), exact for any number of modes
   auto key_of = [&](const int* n) {
-    uint64_t k = 0;
-    for (int i = 0; i < D; ++i) k = k * (uint64_t)(nbmax[i] + 1) + (uint64_t)n[i];
+    std::string k((size_t)D, '\0');
+    for (int i = 0; i < D; ++i) k[(size_t)i] = (char)(unsigned char)n[i];
     return k;
   };
-  std::unordered_map<uint64_t, int> rank;
+  std::unordered_map<std::string, int> rank;
   std::vector<int> n(D, 1);
   if (P.kind == EVR_BASIS_SG4) {
     struct Rec {

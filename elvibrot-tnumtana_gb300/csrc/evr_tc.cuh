@@ -11,13 +11,13 @@
 // contraction runs in chunks of 8 (K padded to 8, 16 or 24):
 //   * the CTA stages the fibre tile into shared memory in the canonical K-major layout
 //     without swizzle (8-row x 16-byte core matrices; LBO = 128 B between core matrices
-//     along K, SBO = 32*Kp B between 8-row groups), split x = hi + lo with hi the TF32 value
-//     (mantissa cut to 10 bits) and lo = x - hi, both written by the staging threads;
+//     along K, SBO = 32*Kp B between 8-row groups), split x = hi + lo with hi the nearest
+//     TF32 value and lo the nearest TF32 value of x - hi, both written by the staging threads;
 //   * one thread issues hi*Bhi + lo*Bhi + hi*Blo (3*Kp/8 MMAs, kind::tf32, M=128) into a
 //     TMEM accumulator and commits them to an mbarrier;
 //   * every warp reads its lane quarter of the accumulator (tcgen05.ld 32x32b) and writes
 //     its fibres' outputs (coalesced: consecutive lanes are consecutive fibres).
-// The dropped lo*lo term and the TF32 rounding of lo leave a relative error near 2^-21 per
+// The dropped lo*lo term and the rounding of lo leave a relative error near 2^-23 per
 // product, FP32 level.  Waits on the mbarrier are bounded: on expiry the CTA records an
 // error code and leaves the contraction.
 #pragma once
@@ -73,7 +73,18 @@ __device__ __forceinline__ uint32_t idesc_tf32(int M, int N) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-__device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+// x rounded to the nearest TF32 value (10-bit mantissa), low 13 bits cleared
+__device__ __forceinline__ float tf32_rna(float x) {
+  uint32_t u;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(x));
+  return __uint_as_float(u & 0xFFFFE000u);
+}
+// x = hi + lo with hi, lo TF32 values: |x - hi - lo| <= 2^-24 |x| (each rounded to nearest),
+// so that the MMA reads both exactly, whatever it does with low mantissa bits
+__device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
+  hi = tf32_rna(x);
+  lo = tf32_rna(x - hi);
+}
 
 __device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -178,10 +189,11 @@ __device__ __noinline__ void contract_tc(TcState& st, const float* __restrict__ 
   for (int i = threadIdx.x; i < Np * Kp; i += nthr) {
     const int n = i / Kp, k = i - n * Kp;
     const float x = (n < M && k < K) ? mat[n + ldm * k] : 0.0f;
-    const float h = tf32_hi(x);
+    float h, l;
+    tf32_split(x, h, l);
     const int o = kmajor_index(n, k, Kp);
     sm->b_hi[o] = h;
-    sm->b_lo[o] = x - h;
+    sm->b_lo[o] = l;
   }
   const uint32_t idesc = idesc_tf32(kRows, Np);
   const uint32_t sbo_a = 32u * Kp, sbo_b = 32u * Kp;
@@ -208,10 +220,10 @@ __device__ __noinline__ void contract_tc(TcState& st, const float* __restrict__ 
           if (4 * c + j < K) x[j] = ip[(4 * c + j) * istr];
       }
       float4 h, l;
-      h.x = tf32_hi(x[0]); l.x = x[0] - h.x;
-      h.y = tf32_hi(x[1]); l.y = x[1] - h.y;
-      h.z = tf32_hi(x[2]); l.z = x[2] - h.z;
-      h.w = tf32_hi(x[3]); l.w = x[3] - h.w;
+      tf32_split(x[0], h.x, l.x);
+      tf32_split(x[1], h.y, l.y);
+      tf32_split(x[2], h.z, l.z);
+      tf32_split(x[3], h.w, l.w);
       const int o = ((r >> 3) * kgroups + c) * 32 + (r & 7) * 4;
       *reinterpret_cast<float4*>(sm->a_hi + o) = h;
       *reinterpret_cast<float4*>(sm->a_lo + o) = l;

@@ -505,10 +505,13 @@ class Problem:
 
     def autotune(self, nvec=64, prec="fp64"):
         """Choose the work decomposition by timing; returns (slab cap, general cap,
-        small-term threshold, ms)."""
-        caps = np.zeros(3, dtype=np.int32)
+        small-term threshold, ms), and for FP32 the tensor-core threshold (-1: CUDA cores)
+        before the time."""
+        caps = np.zeros(4, dtype=np.int32)
         ms = np.zeros(1)
         self._check(load().evr_autotune(self.h, nvec, PREC[prec], _p(caps, _ip), _p(ms, _dp)))
+        if prec == "fp32":
+            return int(caps[0]), int(caps[1]), int(caps[2]), int(caps[3]), float(ms[0])
         return int(caps[0]), int(caps[1]), int(caps[2]), float(ms[0])
 
     def set_kernel_path(self, path):

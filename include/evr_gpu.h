@@ -194,11 +194,12 @@ int evr_set_operator(evr_ctx *ctx, int form);
  * kernel.  All compute the same operator. */
 int evr_set_kernel_path(evr_ctx *ctx, int path);
 
-/* Tensor cores for the FP32 path (no counterpart in the reference): on != 0 (the default)
- * runs the mode contractions of the slab-streaming kernel in FP32 H.psi on tcgen05 tensor
- * cores (three TF32 products of split operands, FP32 accumulation), those with K*M below
- * min_km (default 64) on the CUDA cores; on = 0 runs them all on the CUDA cores.  The same
- * operator either way, to FP32 accuracy.  FP64 H.psi is unaffected. */
+/* Tensor cores for the FP32 path (no counterpart in the reference): on != 0 runs the mode
+ * contractions of the slab-streaming kernel in FP32 H.psi on tcgen05 tensor cores (three
+ * TF32 products of split operands, FP32 accumulation in tensor memory), those with K*M
+ * below min_km on the CUDA cores; on = 0 (the default) runs them all on the CUDA cores.
+ * The same operator either way, to FP32 accuracy.  FP64 H.psi is unaffected.
+ * evr_autotune with EVR_PREC_FP32 also times this choice and keeps the faster. */
 int evr_set_tensor_cores(evr_ctx *ctx, int on, int min_km);
 
 /* H.psi that allocates nothing (no counterpart in the reference).
@@ -233,7 +234,9 @@ int evr_tc_selftest(int device, int A, int K, int M, int B, int Vt, const float 
  * tunes OpenMP thread counts): times the term kernels on an nvec-vector block for each
  * cap of the vector tile of a work item (2..32, slab kernel then general kernel) and for
  * the size below which a term runs in the general kernel, and keeps the fastest for later
- * calls.  caps[3] (optional): slab cap, general cap, size threshold; best_ms: the time. */
+ * calls; with EVR_PREC_FP32 also whether the slab kernel's contractions run on the tensor
+ * cores and from which size K*M (evr_set_tensor_cores).  caps[4] (optional): slab cap,
+ * general cap, size threshold, tensor-core threshold (-1: CUDA cores); best_ms: the time. */
 int evr_autotune(evr_ctx *ctx, int nvec, int prec, int *caps, double *best_ms);
 
 /* Launch statistics of the last evr_hpsi_* call (kernels launched, work items). */

@@ -72,3 +72,19 @@ def test_fp32_hpsi_tensor_cores_on_and_off_match_oracle():
         outs[name] = pg.hpsi(psi, prec="fp32")
         assert np.abs(outs[name] - ref).max() <= 2e-5 * np.abs(ref).max(), name
     pg.set_tensor_cores(True, 64)
+
+
+def test_fp32_autotune_keeps_results():
+    # the autotuner also chooses between CUDA-core and tensor-core contractions in FP32;
+    # whatever it keeps computes the same operator
+    from evrgpu import spec as S
+    from oracle import oracle as O
+
+    spec = S.config_sg4(5, 5, seed=3)
+    pg = E.Problem(spec, device=0)
+    cs, ci, thr, km, ms = pg.autotune(nvec=16, prec="fp32")
+    assert km == -1 or km in (64, 160, 288)
+    assert ms > 0
+    psi = np.random.default_rng(8).standard_normal((pg.N, 16))
+    ref = O.OracleProblem(spec).hpsi(psi)
+    assert np.abs(pg.hpsi(psi, prec="fp32") - ref).max() <= 2e-5 * np.abs(ref).max()
