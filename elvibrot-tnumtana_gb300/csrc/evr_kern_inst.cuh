@@ -1,5 +1,6 @@
 // evr_kern_inst.cuh -- instantiation of one term kernel (EVR_KSLAB: slab-streaming or
-// general) for one (type, G source) pair; included by the evr_kern_*.cu units, which are
+// general) for one (type, G source) pair, and for the FP32 slab kernel with or without the
+// tensor-core contractions (EVR_KTC); included by the evr_kern_*.cu units, which are
 // compiled in parallel.
 #include "evr_kernels_impl.cuh"
 
@@ -7,25 +8,29 @@ namespace evr {
 namespace kern {
 
 #if EVR_KSLAB
-template <typename T, bool GFLY>
+#ifndef EVR_KTC
+#define EVR_KTC false
+#endif
+template <typename T, bool GFLY, bool TC>
 cudaError_t launch_slab_kernel(int grid, size_t smem, cudaStream_t s, const ItemParams<T>& p) {
-  hpsi_slab_kernel<T, GFLY><<<grid, kSlabThreads, smem, s>>>(p);
+  hpsi_slab_kernel<T, GFLY, TC><<<grid, kSlabThreads, smem, s>>>(p);
   return cudaGetLastError();
 }
-template <typename T, bool GFLY>
+template <typename T, bool GFLY, bool TC>
 cudaError_t set_slab_kernel_smem(int bytes) {
-  return cudaFuncSetAttribute(hpsi_slab_kernel<T, GFLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  return cudaFuncSetAttribute(hpsi_slab_kernel<T, GFLY, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
-template <typename T, bool GFLY>
+template <typename T, bool GFLY, bool TC>
 cudaError_t slab_kernel_static_smem(int* bytes) {
   cudaFuncAttributes a;
-  const cudaError_t e = cudaFuncGetAttributes(&a, hpsi_slab_kernel<T, GFLY>);
+  const cudaError_t e = cudaFuncGetAttributes(&a, hpsi_slab_kernel<T, GFLY, TC>);
   *bytes = e == cudaSuccess ? (int)a.sharedSizeBytes : 0;
   return e;
 }
-template cudaError_t launch_slab_kernel<EVR_KT, EVR_KGFLY>(int, size_t, cudaStream_t, const ItemParams<EVR_KT>&);
-template cudaError_t set_slab_kernel_smem<EVR_KT, EVR_KGFLY>(int);
-template cudaError_t slab_kernel_static_smem<EVR_KT, EVR_KGFLY>(int*);
+template cudaError_t launch_slab_kernel<EVR_KT, EVR_KGFLY, EVR_KTC>(int, size_t, cudaStream_t,
+                                                                   const ItemParams<EVR_KT>&);
+template cudaError_t set_slab_kernel_smem<EVR_KT, EVR_KGFLY, EVR_KTC>(int);
+template cudaError_t slab_kernel_static_smem<EVR_KT, EVR_KGFLY, EVR_KTC>(int*);
 #else
 template <typename T, bool GFLY>
 cudaError_t launch_items_kernel(int grid, size_t smem, cudaStream_t s, const ItemParams<T>& p) {

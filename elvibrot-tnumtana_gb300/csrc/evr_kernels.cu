@@ -265,10 +265,12 @@ int term_kernel_smem(evr_ctx* c, int* items_bytes, int* slab_bytes) {
     reserved = 1024;
   }
   int st_slab = 0, st_items = 0, v = 0;
-  EVR_CU((slab_kernel_static_smem<float, false>(&v)), "attr"); st_slab = std::max(st_slab, v);
-  EVR_CU((slab_kernel_static_smem<float, true>(&v)), "attr"); st_slab = std::max(st_slab, v);
-  EVR_CU((slab_kernel_static_smem<double, false>(&v)), "attr"); st_slab = std::max(st_slab, v);
-  EVR_CU((slab_kernel_static_smem<double, true>(&v)), "attr"); st_slab = std::max(st_slab, v);
+  EVR_CU((slab_kernel_static_smem<float, false, false>(&v)), "attr"); st_slab = std::max(st_slab, v);
+  EVR_CU((slab_kernel_static_smem<float, true, false>(&v)), "attr"); st_slab = std::max(st_slab, v);
+  EVR_CU((slab_kernel_static_smem<float, false, true>(&v)), "attr"); st_slab = std::max(st_slab, v);
+  EVR_CU((slab_kernel_static_smem<float, true, true>(&v)), "attr"); st_slab = std::max(st_slab, v);
+  EVR_CU((slab_kernel_static_smem<double, false, false>(&v)), "attr"); st_slab = std::max(st_slab, v);
+  EVR_CU((slab_kernel_static_smem<double, true, false>(&v)), "attr"); st_slab = std::max(st_slab, v);
   EVR_CU((items_kernel_static_smem<float, false>(&v)), "attr"); st_items = std::max(st_items, v);
   EVR_CU((items_kernel_static_smem<float, true>(&v)), "attr"); st_items = std::max(st_items, v);
   EVR_CU((items_kernel_static_smem<double, false>(&v)), "attr"); st_items = std::max(st_items, v);
@@ -536,9 +538,19 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
       ps.tc_min_km = c->tc_min_km;
       ps.smem_elems = (int64_t)(ps.tc_off / sizeof(T));
     }
-    EVR_CU((p.gfly ? launch_slab_kernel<T, true>(w.grid_slab, w.smem_slab_bytes, s, ps)
-                   : launch_slab_kernel<T, false>(w.grid_slab, w.smem_slab_bytes, s, ps)),
-           "hpsi_slab_kernel launch");
+    cudaError_t le;
+    if constexpr (sizeof(T) == 4) {
+      if (ps.use_tc)
+        le = p.gfly ? launch_slab_kernel<T, true, true>(w.grid_slab, w.smem_slab_bytes, s, ps)
+                    : launch_slab_kernel<T, false, true>(w.grid_slab, w.smem_slab_bytes, s, ps);
+      else
+        le = p.gfly ? launch_slab_kernel<T, true, false>(w.grid_slab, w.smem_slab_bytes, s, ps)
+                    : launch_slab_kernel<T, false, false>(w.grid_slab, w.smem_slab_bytes, s, ps);
+    } else {
+      le = p.gfly ? launch_slab_kernel<T, true, false>(w.grid_slab, w.smem_slab_bytes, s, ps)
+                  : launch_slab_kernel<T, false, false>(w.grid_slab, w.smem_slab_bytes, s, ps);
+    }
+    EVR_CU(le, "hpsi_slab_kernel launch");
   }
   if (set.n_items > 0) {
     p.items = set.items;

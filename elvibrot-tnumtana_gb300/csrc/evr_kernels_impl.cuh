@@ -98,10 +98,13 @@ __device__ __forceinline__ void fma_column(T (&accv)[MAXM], const T* __restrict_
     if (m4 < M) {
       T c0, c1, c2, c3;
       load4(mk + m4, c0, c1, c2, c3);
+      // FP64: no FMA for the rows past M (the FP64 pipe is the bound); FP32 keeps the
+      // unconditional group of four (fewer predicates, the padded rows are discarded)
+      constexpr bool kExact = sizeof(T) == 8;
       accv[m4] = fma(c0, xk, accv[m4]);
-      accv[m4 + 1] = fma(c1, xk, accv[m4 + 1]);
-      accv[m4 + 2] = fma(c2, xk, accv[m4 + 2]);
-      accv[m4 + 3] = fma(c3, xk, accv[m4 + 3]);
+      if (!kExact || m4 + 1 < M) accv[m4 + 1] = fma(c1, xk, accv[m4 + 1]);
+      if (!kExact || m4 + 2 < M) accv[m4 + 2] = fma(c2, xk, accv[m4 + 2]);
+      if (!kExact || m4 + 3 < M) accv[m4 + 3] = fma(c3, xk, accv[m4 + 3]);
     }
 }
 
@@ -309,22 +312,35 @@ __device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64
     else if (M <= 16) contract_m<T, 16, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else if (M <= 20) contract_m<T, 20, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else contract_m<T, 24, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
-  } else {  // FP64: matrix strip in registers (register budget MG*MAXK <= 24 doubles)
+  } else {
+#ifndef EVR_FP64_OLD_BUCKETS
+    // FP64: one output row per thread with the row's coefficients in registers, in buckets
+    // of odd lengths (the 1-D sizes 2l+1 and 2l+3 run without padded FMAs; an even K pads
+    // one): the FP64 pipe is the bound, so padded FMAs cost time one for one
+    switch ((K >> 1) + 1) {  // bucket 2j-1 >= K: j = K/2 + 1
+      case 1: contract_ms<T, 1, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
+      case 2: contract_ms<T, 3, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
+      case 3: contract_ms<T, 5, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
+      case 4: contract_ms<T, 7, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
+      case 5: contract_ms<T, 9, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
+      case 6: contract_ms<T, 11, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
+      case 7: contract_ms<T, 13, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
+      case 8: contract_ms<T, 15, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
+      case 9: contract_ms<T, 17, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
+      case 10: contract_ms<T, 19, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
+      case 11: contract_ms<T, 21, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
+      case 12: contract_ms<T, 23, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
+      default: contract_ms<T, 24, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc); break;
+    }
+#else
     if (K <= 4) contract_ms<T, 4, 4>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else if (K <= 8) contract_ms<T, 8, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else if (K <= 12) contract_ms<T, 12, 2>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else if (K <= 16) contract_ms<T, 16, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else if (K <= 20) contract_ms<T, 20, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else contract_ms<T, 24, 1>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+#endif
   }
-}
-
-// contract() as one out-of-line function: the FP32 slab kernel calls it from many sites,
-// which would otherwise each carry their own copy of every size bucket
-static __device__ __noinline__ void contract_cc32(const float* in, int64_t ldi, float* out, int64_t ldo, const FastDiv& A,
-                                           int K, int M, int B, const FastDiv& Vt, const float* mat, float alpha,
-                                           bool acc) {
-  contract<float>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
 }
 
 // contract() or, for FP32 with a tensor-core state, the tcgen05 contraction (K <= 24,
@@ -339,7 +355,7 @@ __device__ __forceinline__ void contract_x(tc::TcState* ts, const T* in, int64_t
       tc::contract_tc(*ts, in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
       return;
     }
-    contract_cc32(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
+    contract<T>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
   } else {
     contract<T>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
   }
@@ -461,6 +477,70 @@ __device__ __forceinline__ T g_model(const ItemParams<T>& p, const TermDesc& Tm,
   for (int k = 0; k < DM; ++k)  // dropped 1-point modes sit at Q = 0
     if (k < D) s = fma(__ldg(gp + Dp * Dp * Tm.perm[k]), xq[k], s);
   return (T)s;
+}
+
+// Phi_i = sum_j G_ij(Q) y_j for terms of more than 8 active positions (rare: levels above 8
+// in more than 8 modes, or modes whose level-0 grid has several points), at points
+// r0 .. r0+npts-1 of the term grid: y_j = Y[j*ys + pt*Vt + v] for j < D-1 and last[pt*Vt + v]
+// for j = D-1, in place; with jac, Phi_i is multiplied by jac[2*(r0+pt)].  Runtime loops
+// over the positions and the point's G (table row, G0 or the linear model) in a per-thread
+// array: one out-of-line copy per kernel instead of unrolled loops of every width.
+template <typename T, bool GFLY>
+__device__ __noinline__ void pointwise_G_wide(const ItemParams<T>& p, const TermDesc& Tm, T* Y, int64_t ys, T* last,
+                                              int Vt, int npts, int64_t r0, const T* jac) {
+  const int D = Tm.D, L = D - 1;
+  const int nG = g_table_stride(Tm.Dp);
+  const int nch = max(1, min(Vt, (int)blockDim.x / max(npts, 1)));
+  for (int task = threadIdx.x; task < npts * nch; task += blockDim.x) {
+    const int pt = task / nch, ch = task - pt * nch;
+    const int64_t r = r0 + pt;
+    T G[kMaxD * (kMaxD + 1) / 2];
+    if (GFLY) {
+      double xq[kMaxD];
+      int rr = (int)r;
+      for (int k = 0; k < D; ++k) {
+        const int n = Tm.nq[k];
+        const int i = rr % n;
+        rr /= n;
+        xq[k] = (double)p.mats[Tm.m_x[k] + i];
+      }
+      int s = 0;
+      for (int i = 0; i < D; ++i)
+        for (int j = i; j < D; ++j, ++s) {
+          const int oi = Tm.perm[i], oj = Tm.perm[j];
+          double g = __ldg(p.G0 + Tm.g0off + oi + Tm.Dp * oj);
+          const double* gp = p.gco + Tm.goff + oi + Tm.Dp * oj;
+          for (int k = 0; k < D; ++k) g = fma(__ldg(gp + Tm.Dp * Tm.Dp * Tm.perm[k]), xq[k], g);
+          G[s] = (T)g;
+        }
+    } else if (p.ggrid) {
+      const T* Gp = p.ggrid + (Tm.off_nq + r) * nG;
+      for (int s = 0; s < D * (D + 1) / 2; ++s) G[s] = __ldg(Gp + s);
+    } else {
+      int s = 0;
+      for (int i = 0; i < D; ++i)
+        for (int j = i; j < D; ++j, ++s) G[s] = (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]);
+    }
+    const T jq = jac ? jac[2 * r] : T(1);
+    for (int v = ch; v < Vt; v += nch) {
+      const int64_t a = (int64_t)pt * Vt + v;
+      T y[kMaxD], z[kMaxD];
+      for (int j = 0; j < D; ++j) {
+        y[j] = j < L ? Y[j * ys + a] : last[a];
+        z[j] = T(0);
+      }
+      int s = 0;
+      for (int i = 0; i < D; ++i)
+        for (int j = i; j < D; ++j, ++s) {
+          z[i] = fma(G[s], y[j], z[i]);
+          if (j != i) z[j] = fma(G[s], y[i], z[j]);
+        }
+      for (int i = 0; i < D; ++i) {
+        if (i < L) Y[i * ys + a] = jq * z[i];
+        else last[a] = jq * z[i];
+      }
+    }
+  }
 }
 
 // Y[i] <- sum_j G_ij(Q) Y[j] on the whole term grid (general kernel).  A thread owns a grid
@@ -667,8 +747,8 @@ __global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p
         if (D <= 4) items_pointwise_G<T, 4, GFLY>(p, Tm, Y, stride, Vt, NQ);
         else if (D <= 6) items_pointwise_G<T, 6, GFLY>(p, Tm, Y, stride, Vt, NQ);
         else if (D <= 8) items_pointwise_G<T, 8, GFLY>(p, Tm, Y, stride, Vt, NQ);
-        else if (D <= 16) items_pointwise_G<T, 16, GFLY>(p, Tm, Y, stride, Vt, NQ);
-        else items_pointwise_G<T, kMaxD, GFLY>(p, Tm, Y, stride, Vt, NQ);
+        else pointwise_G_wide<T, GFLY>(p, Tm, Y, stride, Y + (D - 1) * stride, Vt, NQ, 0,
+                                       p.jgrid ? p.jgrid + 2 * Tm.off_nq : nullptr);
         __syncthreads();
         A = 1; Bq = NQ;
         // Acc += -1/2 d1_i . Y[i]; same-fibre updates per mode.  With a Jacobian the
@@ -922,9 +1002,7 @@ __device__ __forceinline__ void slab_keo10(const ItemParams<T>& p, const TermDes
   if (D <= 4) slab_pointwise_G<T, 4, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
   else if (D <= 6) slab_pointwise_G<T, 6, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
   else if (D <= 8) slab_pointwise_G<T, 8, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
-  else if (D <= 12) slab_pointwise_G<T, 12, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
-  else if (D <= 16) slab_pointwise_G<T, 16, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
-  else slab_pointwise_G<T, kMaxD, GFLY>(p, Tm, Y, P1, ss, Vt, q, NQs, nG);
+  else pointwise_G_wide<T, GFLY>(p, Tm, Y, ss, P1, Vt, NQs, (int64_t)q * NQs, nullptr);
   __syncthreads();
   A = 1;
   Bq = NQs;
@@ -949,22 +1027,23 @@ __device__ __forceinline__ void slab_keo10(const ItemParams<T>& p, const TermDes
 //      term-basis output.
 // The algebra is that of sub_TabOpPsi_OF_ONEDP_FOR_SGtype4 (sub_OpPsi_SG4.f90:1490-1650)
 // with the last mode's B->G, derivative and G->B matrices multiplied together.
-template <typename T, bool GFLY>
+// TC (FP32 only): the mode contractions with K*M >= p.tc_min_km on the tensor cores; a
+// separate instantiation, so that the CUDA-core kernel carries no call into them.
+template <typename T, bool GFLY, bool TC>
 __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T> p) {
+  static_assert(!TC || sizeof(T) == 4, "tensor-core contractions are FP32");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   __shared__ TermDesc s_term;
   __shared__ StageBlocks s_blocks;
   __shared__ ItemDivs s_div;
-  // FP32: the tensor-core contractions' shared block and TMEM accumulator for the CTA's life
+  // the tensor-core contractions' shared block and TMEM accumulator for the CTA's life
   tc::TcState tcs;
   tc::TcState* ts = nullptr;
-  if constexpr (sizeof(T) == 4) {
-    if (p.use_tc) {
-      tc::tc_setup(tcs, reinterpret_cast<tc::TcSmem*>(smem_raw + p.tc_off), p.err);
-      tcs.min_km = p.tc_min_km;
-      ts = &tcs;
-    }
+  if constexpr (TC) {
+    tc::tc_setup(tcs, reinterpret_cast<tc::TcSmem*>(smem_raw + p.tc_off), p.err);
+    tcs.min_km = p.tc_min_km;
+    ts = &tcs;
   }
   while (true) {
     if (threadIdx.x == 0) s_item = atomicAdd(p.counter, 1);
@@ -1144,9 +1223,7 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
         if (D <= 4) slab_pointwise_G<T, 4, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
         else if (D <= 6) slab_pointwise_G<T, 6, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
         else if (D <= 8) slab_pointwise_G<T, 8, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
-        else if (D <= 12) slab_pointwise_G<T, 12, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
-        else if (D <= 16) slab_pointwise_G<T, 16, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
-        else slab_pointwise_G<T, kMaxD, GFLY>(p, Tm, Y, P, ss, Vt, q, NQs, nG);
+        else pointwise_G_wide<T, GFLY>(p, Tm, Y, ss, P, Vt, NQs, (int64_t)q * NQs, nullptr);
         __syncthreads();
         A = 1;
         Bq = NQs;
@@ -1236,23 +1313,22 @@ __global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T
       }
     }
   }
-  if constexpr (sizeof(T) == 4) {
-    if (ts) tc::tc_teardown(tcs);
-  }
+  if constexpr (TC) tc::tc_teardown(tcs);
 }
 
 
 // launchers, instantiated in evr_kern_*.cu
 template <typename T, bool GFLY>
 cudaError_t launch_items_kernel(int grid, size_t smem, cudaStream_t s, const ItemParams<T>& p);
-template <typename T, bool GFLY>
+// slab kernel: TC = true only for float (the tensor-core instantiation, its own units)
+template <typename T, bool GFLY, bool TC>
 cudaError_t launch_slab_kernel(int grid, size_t smem, cudaStream_t s, const ItemParams<T>& p);
 template <typename T, bool GFLY>
 cudaError_t set_items_kernel_smem(int bytes);
-template <typename T, bool GFLY>
+template <typename T, bool GFLY, bool TC>
 cudaError_t set_slab_kernel_smem(int bytes);
 // static shared memory of the kernels (the dynamic budget is what the SM has left)
-template <typename T, bool GFLY>
+template <typename T, bool GFLY, bool TC>
 cudaError_t slab_kernel_static_smem(int* bytes);
 template <typename T, bool GFLY>
 cudaError_t items_kernel_static_smem(int* bytes);
@@ -1262,7 +1338,11 @@ cudaError_t occupancy_items_kernel(int* per_sm, int smem_bytes);
 template <typename T, bool GFLY>
 cudaError_t set_term_kernel_smem(int items_bytes, int slab_bytes) {
   cudaError_t e = set_items_kernel_smem<T, GFLY>(items_bytes);
-  return e != cudaSuccess ? e : set_slab_kernel_smem<T, GFLY>(slab_bytes);
+  if (e == cudaSuccess) e = set_slab_kernel_smem<T, GFLY, false>(slab_bytes);
+  if constexpr (sizeof(T) == 4) {
+    if (e == cudaSuccess) e = set_slab_kernel_smem<T, GFLY, true>(slab_bytes);
+  }
+  return e;
 }
 
 }  // namespace kern

@@ -171,6 +171,10 @@ __device__ __forceinline__ void tc_teardown(TcState& st) {
 // out(a, m, b, v) = alpha * sum_k mat[m + ldm*k] * in(a, k, b, v) (+ out if acc); element
 // (a, k, b, v) at ((a + A*(k + K*b))*ld + v).  A CTA-wide call (all threads, blockDim a
 // multiple of 128), K <= kMaxKp, M <= kMaxNp.  FastDiv: the divisor type of the caller.
+// Software pipeline with one barrier per 128-fibre tile: the loads of tile i+1 are issued
+// into registers right after the MMAs of tile i, so they are in flight while the MMAs run
+// and while tile i's accumulator is read back; then they are split into the (free) operand
+// tile and the barrier hands it to the MMA-issuing thread.
 template <typename Div>
 __device__ __noinline__ void contract_tc(TcState& st, const float* __restrict__ in, int64_t ldi, float* __restrict__ out,
                             int64_t ldo, const Div& da, int K, int M, int B, const Div& dvt,
@@ -200,16 +204,20 @@ __device__ __noinline__ void contract_tc(TcState& st, const float* __restrict__ 
   const uint32_t a_hi = smem_u32(sm->a_hi), a_lo = smem_u32(sm->a_lo);
   const uint32_t b_hi = smem_u32(sm->b_hi), b_lo = smem_u32(sm->b_lo);
   const int kgroups = Kp >> 2;
+  const int ntask = kRows * kgroups;  // staging tasks of a tile: (fibre row, group of 4 k)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int quarter = warp & 3, chunk = warp >> 2, nchunk = nthr >> 7;
 
-  for (int f0 = 0; f0 < nfib; f0 += kRows) {
-    // ---- stage the fibre tile (rows f0..f0+127, K columns), split into hi and lo
-    for (int i = threadIdx.x; i < kRows * kgroups; i += nthr) {
-      const int r = i & (kRows - 1), c = i >> 7;
-      const int f = f0 + r;
-      float x[4] = {0.f, 0.f, 0.f, 0.f};
-      if (f < nfib) {
+  // a thread's staging tasks of one tile: threadIdx.x + t*nthr (at most kTasks with >= 128 threads)
+  constexpr int kTasks = kMaxKp / 4;
+  float x[kTasks][4];
+  auto load_tile = [&](int f0) {
+#pragma unroll
+    for (int t = 0; t < kTasks; ++t) {
+      x[t][0] = x[t][1] = x[t][2] = x[t][3] = 0.f;
+      const int i = threadIdx.x + t * nthr;
+      const int f = f0 + (i & (kRows - 1)), c = i >> 7;
+      if (i < ntask && f < nfib) {
         const int t1 = (int)dvt.div((uint32_t)f);
         const int v = f - t1 * Vt;
         const int b = (int)da.div((uint32_t)t1);
@@ -217,22 +225,41 @@ __device__ __noinline__ void contract_tc(TcState& st, const float* __restrict__ 
         const float* ip = in + (int64_t)(a + (int64_t)A * K * b) * ldi + v;
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-          if (4 * c + j < K) x[j] = ip[(4 * c + j) * istr];
+          if (4 * c + j < K) x[t][j] = ip[(4 * c + j) * istr];
       }
-      float4 h, l;
-      tf32_split(x[0], h.x, l.x);
-      tf32_split(x[1], h.y, l.y);
-      tf32_split(x[2], h.z, l.z);
-      tf32_split(x[3], h.w, l.w);
-      const int o = ((r >> 3) * kgroups + c) * 32 + (r & 7) * 4;
-      *reinterpret_cast<float4*>(sm->a_hi + o) = h;
-      *reinterpret_cast<float4*>(sm->a_lo + o) = l;
     }
+  };
+  auto store_tile = [&]() {
+#pragma unroll
+    for (int t = 0; t < kTasks; ++t) {
+      const int i = threadIdx.x + t * nthr;
+      if (i < ntask) {
+        const int r = i & (kRows - 1), c = i >> 7;
+        float4 h, l;
+        tf32_split(x[t][0], h.x, l.x);
+        tf32_split(x[t][1], h.y, l.y);
+        tf32_split(x[t][2], h.z, l.z);
+        tf32_split(x[t][3], h.w, l.w);
+        const int o = ((r >> 3) * kgroups + c) * 32 + (r & 7) * 4;
+        *reinterpret_cast<float4*>(sm->a_hi + o) = h;
+        *reinterpret_cast<float4*>(sm->a_lo + o) = l;
+      }
+    }
+  };
+
+  bool ok = true;
+  load_tile(0);
+  for (int f0 = 0; f0 < nfib; f0 += kRows) {
+    // the operand tile is free: the previous tile's MMAs have completed (waited below)
+    store_tile();
     fence_async_smem();
     fence_before_sync();
-    __syncthreads();
+    // one barrier per tile; it also carries the outcome of the previous tile's wait (a lost
+    // wait on any thread ends the contraction for all)
+    const bool lost = __syncthreads_or(!ok) != 0;
     fence_after_sync();
-    // ---- one thread issues the MMAs: hi*Bhi + lo*Bhi + hi*Blo over the K chunks
+    if (lost) break;
+    // ---- one thread issues hi*Bhi + lo*Bhi + hi*Blo over the K chunks
     if (threadIdx.x == 0) {
       uint32_t accum = 0;
       for (int kc = 0; kc < Kp; kc += 8) {
@@ -244,14 +271,10 @@ __device__ __noinline__ void contract_tc(TcState& st, const float* __restrict__ 
       }
       mma_commit(mbar);
     }
-    // every thread waits for the commit, then the CTA agrees on the outcome (a lost
-    // wait on any thread ends the contraction for all)
-    const bool ok = __syncthreads_and(mbar_wait(mbar, st.phase)) != 0;
+    // ---- the next tile's loads go out while the MMAs run
+    if (f0 + kRows < nfib) load_tile(f0 + kRows);
+    ok = mbar_wait(mbar, st.phase);
     st.phase ^= 1u;
-    if (!ok && threadIdx.x == 0) {
-      sm->failed = 1;
-      atomicExch(st.err, 2);
-    }
     fence_after_sync();
     // ---- epilogue: warp (quarter, chunk) reads lanes 32*quarter.., columns 8*chunk..
     if (ok) {
@@ -277,11 +300,16 @@ __device__ __noinline__ void contract_tc(TcState& st, const float* __restrict__ 
         }
       }
     }
-    // the next tile's staging overwrites the operands and its MMAs the accumulator
+    // the accumulator reads are complete (wait::ld) before the next barrier releases the
+    // next tile's MMAs
     fence_before_sync();
-    __syncthreads();
-    fence_after_sync();
-    if (!ok) return;
+  }
+  // the last tile's outcome; the caller's next contraction may overwrite the operands
+  const bool lost = __syncthreads_or(!ok) != 0;
+  fence_after_sync();
+  if (lost && threadIdx.x == 0) {
+    sm->failed = 1;
+    atomicExch(st.err, 2);
   }
 }
 
