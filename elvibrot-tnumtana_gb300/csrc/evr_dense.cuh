@@ -24,7 +24,7 @@ constexpr int kMaxEig = 512;     // largest projected matrix of the Jacobi kerne
 // partial Gram of one chunk of rows: part[chunk] (na x nb, column-major) =
 // sum_{r in chunk} A[r, i] B[r, j] over the 64 x 64 output tile of blockIdx.y; a thread owns
 // a 4 x 4 block of the tile
-__global__ void __launch_bounds__(256) gram_part_kernel(const double* __restrict__ A, int lda,
+static __global__ void __launch_bounds__(256) gram_part_kernel(const double* __restrict__ A, int lda,
                                                         const double* __restrict__ B, int ldb, int na, int nb,
                                                         int64_t N, int64_t rows_per_chunk, double* __restrict__ part) {
   __shared__ double sA[kStage][kTile + 2];
@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(256) gram_part_kernel(const double* __restrict
 }
 
 // C (ld ldc) = sum over the chunks of the partial Grams, in chunk order (+ beta C)
-__global__ void gram_reduce_kernel(const double* __restrict__ part, int nchunk, int na, int nb,
+static __global__ void gram_reduce_kernel(const double* __restrict__ part, int nchunk, int na, int nb,
                                    double* __restrict__ C, int ldc, double beta) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < na * nb; e += gridDim.x * blockDim.x) {
     const int i = e % na, j = e / na;
@@ -86,7 +86,7 @@ __global__ void gram_reduce_kernel(const double* __restrict__ part, int nchunk, 
 // Y[r, j] = alpha sum_{i < n} X[r, i] Mat[i + ldm j] + beta Y[r, j]  (j < k): 64 rows x 32
 // columns per CTA, the contraction in steps of 32 through shared memory; a thread forms
 // 2 rows x 4 columns
-__global__ void __launch_bounds__(256) combine_kernel(const double* __restrict__ X, int ldx, int n,
+static __global__ void __launch_bounds__(256) combine_kernel(const double* __restrict__ X, int ldx, int n,
                                                       const double* __restrict__ Mat, int ldm, int k,
                                                       double* __restrict__ Y, int ldy, double alpha, double beta,
                                                       int64_t N) {
@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(256) combine_kernel(const double* __restrict__
 // per-chunk sums of squares of the k columns of an interleaved block: part[chunk*k + c];
 // a warp holds 32 consecutive columns, the 8 warps of a CTA take interleaved rows and are
 // summed in warp order
-__global__ void colnorm_part_kernel(const double* __restrict__ X, int ldx, int k, int64_t N, int64_t rows_per_chunk,
+static __global__ void colnorm_part_kernel(const double* __restrict__ X, int ldx, int k, int64_t N, int64_t rows_per_chunk,
                                     double* __restrict__ part) {
   __shared__ double red[8][33];
   const int c = blockIdx.y * 32 + threadIdx.x;
@@ -164,7 +164,7 @@ __global__ void colnorm_part_kernel(const double* __restrict__ X, int ldx, int k
 
 // Hs(n0 + j, i) = Hs(i, n0 + j) for i < n0, j < n1 - n0: the new columns of the projected
 // matrix mirrored into its new rows
-__global__ void mirror_kernel(double* __restrict__ Hs, int ld, int n0, int n1) {
+static __global__ void mirror_kernel(double* __restrict__ Hs, int ld, int n0, int n1) {
   const int nn = n1 - n0;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n0 * nn; e += gridDim.x * blockDim.x) {
     const int i = e % n0, j = e / n0;
@@ -182,7 +182,7 @@ __global__ void mirror_kernel(double* __restrict__ Hs, int ld, int n0, int n1) {
 // after max_sweeps.  Work arrays wa, wv: np x np each; word: np ints.  Output: eigenvalues
 // ascending in W, eigenvectors as the columns of V (ld ldv).  The working matrices are read
 // and written with L2-coherent accesses (__ldcg / __stcg).
-__global__ void __launch_bounds__(256) jacobi_coop_kernel(const double* __restrict__ A, int lda, int n,
+static __global__ void __launch_bounds__(256) jacobi_coop_kernel(const double* __restrict__ A, int lda, int n,
                                                           double* __restrict__ W, double* __restrict__ V, int ldv,
                                                           double* __restrict__ wa, double* __restrict__ wv,
                                                           int* __restrict__ word, int max_sweeps, double tol) {

@@ -58,6 +58,12 @@ class DavidsonOpts(C.Structure):
                 ("sym", C.c_int)]
 
 
+class FilterOpts(C.Structure):
+    _fields_ = [("hmin", C.c_double), ("hmax", C.c_double), ("e0", C.c_double), ("width", C.c_double),
+                ("n_filters", C.c_int), ("max_order", C.c_int), ("nstart", C.c_int), ("prec", C.c_int),
+                ("conv_resi", C.c_double), ("seed", C.c_ulonglong)]
+
+
 class OcOpts(C.Structure):
     _fields_ = [("nsteps", C.c_int), ("dt", C.c_double), ("emin", C.c_double), ("emax", C.c_double),
                 ("poly_tol", C.c_double), ("checkpoint", C.c_int), ("prec", C.c_int)]
@@ -72,7 +78,7 @@ EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_
            "evr_oc_forward", "evr_oc_backward", "evr_create_batch", "evr_batch_offsets", "evr_batch_davidson", "evr_autotune",
            "evr_psi_write", "evr_psi_read", "evr_set_vgrid", "evr_set_dipole_grid", "evr_set_ggrid",
            "evr_sil_propagate", "evr_restart_write", "evr_restart_read", "evr_autocorr_write",
-           "evr_autocorr_read", "evr_tc_selftest", "evr_set_tensor_cores", "evr_set_jacobian"]
+           "evr_autocorr_read", "evr_tc_selftest", "evr_set_tensor_cores", "evr_set_jacobian", "evr_filter_diag"]
 VGRID_LAYOUT = {"terms": 0, "ref": 1}
 WP_FORMAT = {"v0": 0, "v1": 1, "unformatted": 2, "sparse": 3}
 
@@ -145,6 +151,7 @@ def load(build: bool = True):
     L.evr_tc_selftest.argtypes = [C.c_int] * 6 + [_fp, _fp, _fp, C.c_float, C.c_int, C.c_int]
     L.evr_sil_propagate.argtypes = [vp, _dp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp,
                                     _lp]
+    L.evr_filter_diag.argtypes = [vp, C.POINTER(FilterOpts), _dp, _dp, _dp, _dp, C.POINTER(C.c_int), _dp, _lp]
     _lib = L
     return L
 
@@ -530,6 +537,34 @@ class Problem:
     def set_operator(self, form):
         """'H' (the reference's OpPsi), 'HT' (its transpose) or 'HSYM' ((H+H^T)/2)."""
         self._check(load().evr_set_operator(self.h, {"H": 0, "HT": 1, "HSYM": 2}[form]))
+
+    def filter_diag(self, hmin, hmax, e0, width, n_filters, max_order=2000, q0=None, nstart=1, prec="fp64",
+                    conv_resi=1e-6, seed=1, want_vectors=False):
+        """Gaussian filter diagonalisation (sub_GaussianFilterDiagonalization) of the levels
+        in the window of `width` au around e0; q0: optional start vectors (N x nstart).
+        Returns dict(eig, resid, vec, lambda_min, lambda_max, non_hermitic, order, hpsi,
+        kept, in_window, converged_in_window)."""
+        L = load()
+        o = FilterOpts()
+        o.hmin, o.hmax, o.e0, o.width = hmin, hmax, e0, width
+        o.n_filters, o.max_order, o.prec, o.conv_resi, o.seed = n_filters, max_order, PREC[prec], conv_resi, seed
+        q = None
+        if q0 is not None:
+            q = np.asfortranarray(np.asarray(q0, dtype=np.float64).reshape(self.N, -1))
+            nstart = q.shape[1]
+        o.nstart = nstart
+        K = n_filters * nstart
+        eig, resid = np.zeros(K), np.zeros(K)
+        vec = np.zeros((self.N, K), order="F") if want_vectors else None
+        nout = C.c_int(0)
+        win = np.zeros(3)
+        info = np.zeros(5, dtype=np.int64)
+        self._check(L.evr_filter_diag(self.h, C.byref(o), _p(q, _dp), _p(eig, _dp), _p(resid, _dp), _p(vec, _dp),
+                                      C.byref(nout), _p(win, _dp), _p(info, _lp)))
+        k = nout.value
+        return dict(eig=eig[:k], resid=resid[:k], vec=None if vec is None else vec[:, :k], lambda_min=win[0],
+                    lambda_max=win[1], non_hermitic=win[2], order=int(info[0]), hpsi=int(info[1]), kept=int(info[2]),
+                    in_window=int(info[3]), converged_in_window=int(info[4]))
 
     def sil(self, psi0, dt, nsteps, npoly=64, poly_tol=1e-10, prec="fp64", want_psi=False):
         """Short-iterative-Lanczos propagation (march_SIL) of complex packets psi0 (N x npsi);

@@ -299,6 +299,42 @@ int evr_cheby_propagate(evr_ctx *ctx, const double *psi0, int npsi, double dt, i
 int evr_sil_propagate(evr_ctx *ctx, const double *psi0, int npsi, double dt, int nsteps, int npoly,
                       double poly_tol, int prec, double *autocorr, double *psi_out, int64_t *info);
 
+/*
+ * Gaussian filter diagonalisation: the levels of H in an energy window.
+ * Replaces sub_GaussianFilterDiagonalization
+ * (Source_ElVibRot/sub_propagation/sub_module_Filter.f90:70-520): n_filters Gaussian
+ * filters exp(-((x - E_l)/sigma)^2), sigma = width/Esc/n_filters, centred at
+ * lambda_min + l*width/(n_filters-1) with lambda_min = max(hmin, e0 - width/2), are
+ * expanded in Chebyshev polynomials of Hs = (H - E0)/Esc (hmin/hmax widened by 1 % of their
+ * range; the coefficients by the reference's Gauss-Chebyshev rule and kernel damping
+ * factor, :300-345 and :2538-2579; the series length grown by 10 % until the central
+ * filter's tail is below 1e-8 or it exceeds max_order, :199-283) and applied to each start
+ * vector by the Chebyshev recursion (one H.psi per order for all start vectors,
+ * sub_chebychev_recursion :2221-2298).  The filtered vectors are orthonormalised as
+ * sub_Lowdin and sub_Schmidt do, those with an overlap eigenvalue above 1e-9 kept, and H is
+ * diagonalised in their span (symmetrised, as sub_hermitic_H), with the residual norm of
+ * every Ritz pair (:405-470).  The reference stops after this diagonalisation; the call
+ * returns its results.  The operator is the context's form (evr_set_operator).
+ * q0: optional HOST start vectors (N x nstart column-major; NULL = seeded random).
+ * eig, resid: out, up to n_filters*nstart values (eigenvalues ascending, residual norms).
+ * vec: optional HOST out (N x n_out column-major Ritz vectors).  n_out: kept vectors.
+ * window: optional out [lambda_min, lambda_max, non_hermitic].
+ * info: optional out [series length, H.psi count, kept vectors, levels in the window,
+ *   levels in the window with a residual below max(conv_resi, non_hermitic)]. */
+typedef struct evr_filter_opts {
+  double hmin, hmax;     /* spectral bounds of H (au); hmin is also the window's floor   */
+  double e0;             /* window centre (au; the reference's E0_filter + Hmin)          */
+  double width;          /* window width (au; W_filter)                                  */
+  int n_filters;         /* L_filter >= 2                                               */
+  int max_order;         /* M_filter: cap of the series length (>= 4)                     */
+  int nstart;            /* start vectors, n_filters filtered vectors each (1 = the reference) */
+  int prec;              /* EVR_PREC_FP64 or EVR_PREC_FP32 contractions in the H.psi      */
+  double conv_resi;      /* residual norm below which a level counts as converged (au)    */
+  unsigned long long seed; /* random start vectors when q0 is NULL                        */
+} evr_filter_opts;
+int evr_filter_diag(evr_ctx *ctx, const evr_filter_opts *opts, const double *q0, double *eig, double *resid,
+                    double *vec, int *n_out, double *window, int64_t *info);
+
 /* FMA issue-rate micro-benchmark of the device (independent FMA chains, no memory
  * traffic): the peak of the CUDA-core pipe the contractions run on, in TFLOP/s.
  * Utility for roofline reporting; no counterpart in the reference. */
