@@ -156,8 +156,10 @@ struct Workspace {
   double* xin = nullptr;            // interleaved copies (layout conversions)
   double* xout = nullptr;
   int grid = 0, smem_bytes = 0;             // general kernel
-  int grid_slab = 0, smem_slab_bytes = 0;   // slab kernel
-  size_t slab_slab_bytes = 0;               // slab kernel's global tensor per CTA
+  // slab kernel, per precision (index EVR_PREC_FP64 / EVR_PREC_FP32): grid, dynamic shared
+  // memory and global tensor per CTA
+  int grid_slab[2] = {0, 0}, smem_slab_bytes[2] = {0, 0};
+  size_t slab_slab_bytes[2] = {0, 0};
   WorkItem* f_items = nullptr;              // filtered item lists (terms of active problems)
   WorkItem* f_slab = nullptr;
   size_t f_cap = 0;

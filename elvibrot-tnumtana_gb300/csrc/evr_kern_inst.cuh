@@ -13,7 +13,7 @@ namespace kern {
 #endif
 template <typename T, bool GFLY, bool TC>
 cudaError_t launch_slab_kernel(int grid, size_t smem, cudaStream_t s, const ItemParams<T>& p) {
-  hpsi_slab_kernel<T, GFLY, TC><<<grid, kSlabThreads, smem, s>>>(p);
+  hpsi_slab_kernel<T, GFLY, TC><<<grid, slab_threads<T>(), smem, s>>>(p);
   return cudaGetLastError();
 }
 template <typename T, bool GFLY, bool TC>

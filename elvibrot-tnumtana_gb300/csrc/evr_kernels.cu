@@ -253,9 +253,10 @@ void free_workspace(evr_ctx* c) {
 // placed 16-byte aligned at the end of the dynamic shared memory)
 static size_t tc_reserve_bytes() { return (sizeof(tc::TcSmem) + 15) & ~(size_t)15; }
 
-// Dynamic shared memory of the term kernels: the slab kernel takes what one CTA may have
-// (the opt-in maximum less its static block), the general kernel what leaves room for two
-// CTAs per SM (each also holds its static block and the per-block reservation).
+// Dynamic shared memory of the term kernels: the slab kernel's CTAs (slab_ctas per SM, per
+// precision) and the general kernel's two CTAs per SM share the SM's shared memory, each
+// CTA also holding its static block and the per-block reservation.  slab_bytes[p] for
+// p = EVR_PREC_FP64, EVR_PREC_FP32.
 int term_kernel_smem(evr_ctx* c, int* items_bytes, int* slab_bytes) {
   int optin = 0, per_sm = 0, reserved = 0;
   EVR_CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attr");
@@ -276,7 +277,8 @@ int term_kernel_smem(evr_ctx* c, int* items_bytes, int* slab_bytes) {
   EVR_CU((items_kernel_static_smem<double, false>(&v)), "attr"); st_items = std::max(st_items, v);
   EVR_CU((items_kernel_static_smem<double, true>(&v)), "attr"); st_items = std::max(st_items, v);
   // multiples of 256 bytes below the limits
-  *slab_bytes = (optin - st_slab) & ~255;
+  slab_bytes[EVR_PREC_FP64] = (std::min(optin - st_slab, per_sm / slab_ctas<double>() - reserved - st_slab)) & ~255;
+  slab_bytes[EVR_PREC_FP32] = (std::min(optin - st_slab, per_sm / slab_ctas<float>() - reserved - st_slab)) & ~255;
   *items_bytes = (std::min(optin - st_items, per_sm / 2 - reserved - st_items)) & ~255;
   return EVR_OK;
 }
@@ -319,9 +321,10 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
   int rc = EVR_OK;
   if (!w.counter) {
     // general kernel: 2 CTAs per SM; slab kernel: 1 CTA per SM
-    if ((rc = term_kernel_smem(c, &w.smem_bytes, &w.smem_slab_bytes))) return rc;
+    if ((rc = term_kernel_smem(c, &w.smem_bytes, w.smem_slab_bytes))) return rc;
     w.grid = c->num_sms * 2;
-    w.grid_slab = c->num_sms;
+    w.grid_slab[EVR_PREC_FP64] = c->num_sms * slab_ctas<double>();
+    w.grid_slab[EVR_PREC_FP32] = c->num_sms * slab_ctas<float>();
     size_t slab = 0;  // general kernel: FP64 buffers of the terms that run from global memory
     for (const TermDesc& Tm : P.terms) {
       size_t fp1 = footprint_elems<double>(P, Tm, 1) * sizeof(double);
@@ -331,23 +334,26 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
     // the slab kernel keeps its partially transformed tensor (at most half of its shared
     // memory) in global memory; terms in the W-in-global mode (FP64 terms whose slab
     // pipeline does not fit shared memory) need three such tensors there
-    size_t sb = (size_t)(w.smem_slab_bytes / 2 + 256);
+    const int s64 = w.smem_slab_bytes[EVR_PREC_FP64], s32 = w.smem_slab_bytes[EVR_PREC_FP32];
+    size_t sb64 = (size_t)(s64 / 2 + 256), sb32 = (size_t)(s32 / 2 + 256);
     if (P.nb0 == 1)
       for (const TermDesc& Tm : P.terms) {
         if (Tm.weight == 0.0) continue;
         const size_t mats = (size_t)((Tm.msz + 3) & ~3) * sizeof(double);
-        if (slab_need_elems(P, Tm, 1, false) * sizeof(double) + mats <= (size_t)w.smem_slab_bytes) continue;
-        if (slab_wg_smem_elems(P, Tm, 1, false) * sizeof(double) + mats > (size_t)w.smem_slab_bytes) continue;
-        sb = std::max(sb, slab_wg_global_elems(Tm, 1) * sizeof(double));
+        if (slab_need_elems(P, Tm, 1, false) * sizeof(double) + mats <= (size_t)s64) continue;
+        if (slab_wg_smem_elems(P, Tm, 1, false) * sizeof(double) + mats > (size_t)s64) continue;
+        sb64 = std::max(sb64, slab_wg_global_elems(Tm, 1) * sizeof(double));
       }
     // FP32 terms run in the W-in-global or grid-staged mode when it allows a wider vector
     // tile (below): room for tiles of 4 vectors, at most 8 MB per CTA
     if (P.nb0 == 1)
       for (const TermDesc& Tm : P.terms)
         if (Tm.weight != 0.0)
-          sb = std::max(sb, std::min<size_t>(slab_staged_global_elems(Tm, 4) * sizeof(float), 8u << 20));
-    w.slab_slab_bytes = (sb + 255) & ~(size_t)255;
-    const size_t total = std::max(slab * w.grid, w.slab_slab_bytes * w.grid_slab);
+          sb32 = std::max(sb32, std::min<size_t>(slab_staged_global_elems(Tm, 4) * sizeof(float), 8u << 20));
+    w.slab_slab_bytes[EVR_PREC_FP64] = (sb64 + 255) & ~(size_t)255;
+    w.slab_slab_bytes[EVR_PREC_FP32] = (sb32 + 255) & ~(size_t)255;
+    const size_t total = std::max({slab * w.grid, w.slab_slab_bytes[EVR_PREC_FP64] * w.grid_slab[EVR_PREC_FP64],
+                                   w.slab_slab_bytes[EVR_PREC_FP32] * w.grid_slab[EVR_PREC_FP32]});
     w.counter = (int*)dev_alloc<int>(4, rc);  // item counters of both kernels, item-bounds flag
     if (rc) return set_error(c, rc, "workspace allocation (counter)");
     EVR_CU(cudaMemset(w.counter, 0, 4 * sizeof(int)), "memset counter");
@@ -361,10 +367,10 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
     if (rc) return set_error(c, rc, "workspace allocation (xin)");
     w.xout = (double*)dev_alloc<double>(xe, rc);
     if (rc) return set_error(c, rc, "workspace allocation (xout)");
-    EVR_CU((set_term_kernel_smem<float, false>(w.smem_bytes, w.smem_slab_bytes)), "attr");
-    EVR_CU((set_term_kernel_smem<double, false>(w.smem_bytes, w.smem_slab_bytes)), "attr");
-    EVR_CU((set_term_kernel_smem<float, true>(w.smem_bytes, w.smem_slab_bytes)), "attr");
-    EVR_CU((set_term_kernel_smem<double, true>(w.smem_bytes, w.smem_slab_bytes)), "attr");
+    EVR_CU((set_term_kernel_smem<float, false>(w.smem_bytes, s32)), "attr");
+    EVR_CU((set_term_kernel_smem<double, false>(w.smem_bytes, s64)), "attr");
+    EVR_CU((set_term_kernel_smem<float, true>(w.smem_bytes, s32)), "attr");
+    EVR_CU((set_term_kernel_smem<double, true>(w.smem_bytes, s64)), "attr");
   }
   for (const ItemSet& s : w.sets)
     if (s.nvec == nvec && s.prec == prec) return EVR_OK;
@@ -376,7 +382,9 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
   const bool slab_ok = P.nb0 == 1 && c->use_slab && !c->dp_jgrid;
   // shared memory of a slab-kernel item: the FP32 tensor-core contractions keep their
   // operand tiles at the end of the block
-  const size_t slab_smem = (size_t)w.smem_slab_bytes - (f32 && c->use_tc ? tc_reserve_bytes() : 0);
+  const int pi = f32 ? EVR_PREC_FP32 : EVR_PREC_FP64;
+  const size_t slab_smem = (size_t)w.smem_slab_bytes[pi] - (f32 && c->use_tc ? tc_reserve_bytes() : 0);
+  const size_t slab_glob = w.slab_slab_bytes[pi];
   std::vector<WorkItem> items, sitems;
   for (int t = 0; t < (int)P.terms.size(); ++t) {
     const TermDesc& Tm = P.terms[t];
@@ -387,7 +395,7 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
     // W-in-global tile (shared memory holds only the slab arrays)
     auto wg_fits = [&](int v) {
       return slab_wg_smem_elems(P, Tm, v, f32) * esz + mats <= slab_smem &&
-             slab_wg_global_elems(Tm, v) * esz <= w.slab_slab_bytes;
+             slab_wg_global_elems(Tm, v) * esz <= slab_glob;
     };
     if (f32 && slab_ok && !small && wg_fits(1)) {
       // FP32 is bound by the instructions per grid point, not by the L2 traffic of W: the
@@ -406,7 +414,7 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
       if (P.keo_type == 10) {
         auto st_fits = [&](int v) {
           return slab_wg_smem_elems(P, Tm, v, f32) * esz + mats <= slab_smem &&
-                 slab_staged_global_elems(Tm, v) * esz <= w.slab_slab_bytes;
+                 slab_staged_global_elems(Tm, v) * esz <= slab_glob;
         };
         if (st_fits(1)) {
           v4 = 1;
@@ -530,25 +538,27 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
     ps.items = set.items_slab;
     ps.n_items = set.n_slab;
     ps.counter = w.counter + 1;
-    ps.slab_per_cta = (int64_t)(w.slab_slab_bytes / sizeof(T));
-    ps.smem_elems = (int64_t)(w.smem_slab_bytes / sizeof(T));
+    const int pi = sizeof(T) == 4 ? EVR_PREC_FP32 : EVR_PREC_FP64;
+    const int sgrid = w.grid_slab[pi], ssmem = w.smem_slab_bytes[pi];
+    ps.slab_per_cta = (int64_t)(w.slab_slab_bytes[pi] / sizeof(T));
+    ps.smem_elems = (int64_t)(ssmem / sizeof(T));
     if (f32 && c->use_tc) {
       ps.use_tc = 1;
-      ps.tc_off = (int)(((size_t)w.smem_slab_bytes - tc_reserve_bytes()) & ~(size_t)15);
+      ps.tc_off = (int)(((size_t)ssmem - tc_reserve_bytes()) & ~(size_t)15);
       ps.tc_min_km = c->tc_min_km;
       ps.smem_elems = (int64_t)(ps.tc_off / sizeof(T));
     }
     cudaError_t le;
     if constexpr (sizeof(T) == 4) {
       if (ps.use_tc)
-        le = p.gfly ? launch_slab_kernel<T, true, true>(w.grid_slab, w.smem_slab_bytes, s, ps)
-                    : launch_slab_kernel<T, false, true>(w.grid_slab, w.smem_slab_bytes, s, ps);
+        le = p.gfly ? launch_slab_kernel<T, true, true>(sgrid, ssmem, s, ps)
+                    : launch_slab_kernel<T, false, true>(sgrid, ssmem, s, ps);
       else
-        le = p.gfly ? launch_slab_kernel<T, true, false>(w.grid_slab, w.smem_slab_bytes, s, ps)
-                    : launch_slab_kernel<T, false, false>(w.grid_slab, w.smem_slab_bytes, s, ps);
+        le = p.gfly ? launch_slab_kernel<T, true, false>(sgrid, ssmem, s, ps)
+                    : launch_slab_kernel<T, false, false>(sgrid, ssmem, s, ps);
     } else {
-      le = p.gfly ? launch_slab_kernel<T, true, false>(w.grid_slab, w.smem_slab_bytes, s, ps)
-                  : launch_slab_kernel<T, false, false>(w.grid_slab, w.smem_slab_bytes, s, ps);
+      le = p.gfly ? launch_slab_kernel<T, true, false>(sgrid, ssmem, s, ps)
+                  : launch_slab_kernel<T, false, false>(sgrid, ssmem, s, ps);
     }
     EVR_CU(le, "hpsi_slab_kernel launch");
   }
@@ -762,11 +772,11 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
   const HostProblem& P = c->hp;
   // the general kernel's shared memory of the regular path, so that two CTAs are resident
   // per SM and every CTA of the grid gets its per-CTA buffer in the first wave
-  int smem_items = 0, smem_slab = 0;
-  int rc0 = term_kernel_smem(c, &smem_items, &smem_slab);
+  int smem_items = 0, smem_slab[2] = {0, 0};
+  int rc0 = term_kernel_smem(c, &smem_items, smem_slab);
   if (rc0) return rc0;
   // the same attribute values as ensure_workspace sets, so neither path lowers the other's
-  EVR_CU((set_term_kernel_smem<double, false>(smem_items, smem_slab)), "attr");
+  EVR_CU((set_term_kernel_smem<double, false>(smem_items, smem_slab[EVR_PREC_FP64])), "attr");
   int per_sm = 0;
   EVR_CU((occupancy_items_kernel<double, false>(&per_sm, smem_items)), "occupancy");
   const int grid = c->num_sms * std::max(1, std::min(per_sm, 2));

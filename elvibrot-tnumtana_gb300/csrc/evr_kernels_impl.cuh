@@ -75,9 +75,16 @@ void set_plain(ItemParams<T>& p) {
   p.jgrid = nullptr;
 }
 
-// threads of a slab-kernel CTA (FP32 with 1024 threads, 64 registers and one fibre per
-// thread measured 5 % slower)
-constexpr int kSlabThreads = 512;
+// Resident slab-kernel CTAs per SM, and the threads of one: several smaller CTAs per SM,
+// each with its share of the SM's shared memory, overlap one CTA's barriers and
+// shared-memory waits with another's FMAs.  Measured on the D=6 L=8 launch: FP64 712 ms
+// with one CTA of 512 threads, 628 ms with two of 256, 606 ms with four of 128; FP32 114,
+// 112 and 154 ms (its items need the larger shared memory).  FP32 with one CTA of 1024
+// threads, 64 registers and one fibre per thread measured 5 % slower.
+template <typename T>
+constexpr int slab_ctas() { return sizeof(T) == 8 ? 4 : 2; }
+template <typename T>
+constexpr int slab_threads() { return 512 / slab_ctas<T>(); }
 
 // out(a, m, b, v) = alpha * sum_k mat[m + M*k] * in(a, k, b, v)  (+ out if acc)
 // element (a, k, b, v) of a tensor with vector stride ld lives at ((a + A*(k + K*b))*ld + v).
@@ -1024,7 +1031,7 @@ __device__ __forceinline__ void slab_keo10(const ItemParams<T>& p, const TermDes
 // TC (FP32 only): the mode contractions with K*M >= p.tc_min_km on the tensor cores; a
 // separate instantiation, so that the CUDA-core kernel carries no call into them.
 template <typename T, bool GFLY, bool TC>
-__global__ void __launch_bounds__(kSlabThreads, 1) hpsi_slab_kernel(ItemParams<T> p) {
+__global__ void __launch_bounds__(slab_threads<T>(), slab_ctas<T>()) hpsi_slab_kernel(ItemParams<T> p) {
   static_assert(!TC || sizeof(T) == 4, "tensor-core contractions are FP32");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;

@@ -15,7 +15,7 @@ CSRC = os.path.join(PKG_ROOT, "csrc")
 BUILD = os.path.join(PKG_ROOT, "_build")
 LIB = os.path.join(BUILD, "libevrgpu.so")
 SOURCES = ["evr_setup.cpp", "evr_kernels.cu", "evr_capi.cu", "evr_davidson.cu", "evr_propagate.cu", "evr_peaks.cu",
-           "evr_noalloc.cu", "evr_tc_test.cu", "evr_filter.cu", "evr_wpio.cpp", "evr_stages.cu", "evr_control.cu", "evr_batch.cu", "evr_kern_items_d0.cu", "evr_kern_items_d1.cu",
+           "evr_noalloc.cu", "evr_tc_test.cu", "evr_filter.cu", "evr_lanczos.cu", "evr_wpio.cpp", "evr_stages.cu", "evr_control.cu", "evr_batch.cu", "evr_kern_items_d0.cu", "evr_kern_items_d1.cu",
            "evr_kern_items_f0.cu", "evr_kern_items_f1.cu", "evr_kern_slab_d0.cu", "evr_kern_slab_d1.cu",
            "evr_kern_slab_f0.cu", "evr_kern_slab_f1.cu", "evr_kern_slab_f0tc.cu", "evr_kern_slab_f1tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

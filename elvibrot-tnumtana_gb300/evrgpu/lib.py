@@ -64,6 +64,11 @@ class FilterOpts(C.Structure):
                 ("conv_resi", C.c_double), ("seed", C.c_ulonglong)]
 
 
+class LanczosOpts(C.Structure):
+    _fields_ = [("nev", C.c_int), ("ncv", C.c_int), ("max_restarts", C.c_int), ("tol", C.c_double), ("sym", C.c_int),
+                ("seed", C.c_ulonglong)]
+
+
 class OcOpts(C.Structure):
     _fields_ = [("nsteps", C.c_int), ("dt", C.c_double), ("emin", C.c_double), ("emax", C.c_double),
                 ("poly_tol", C.c_double), ("checkpoint", C.c_int), ("prec", C.c_int)]
@@ -78,7 +83,7 @@ EXPORTS = ["evr_create", "evr_destroy", "evr_last_error", "evr_sizes", "evr_get_
            "evr_oc_forward", "evr_oc_backward", "evr_create_batch", "evr_batch_offsets", "evr_batch_davidson", "evr_autotune",
            "evr_psi_write", "evr_psi_read", "evr_set_vgrid", "evr_set_dipole_grid", "evr_set_ggrid",
            "evr_sil_propagate", "evr_restart_write", "evr_restart_read", "evr_autocorr_write",
-           "evr_autocorr_read", "evr_tc_selftest", "evr_set_tensor_cores", "evr_set_jacobian", "evr_filter_diag"]
+           "evr_autocorr_read", "evr_tc_selftest", "evr_set_tensor_cores", "evr_set_jacobian", "evr_filter_diag", "evr_lanczos"]
 VGRID_LAYOUT = {"terms": 0, "ref": 1}
 WP_FORMAT = {"v0": 0, "v1": 1, "unformatted": 2, "sparse": 3}
 
@@ -152,6 +157,7 @@ def load(build: bool = True):
     L.evr_sil_propagate.argtypes = [vp, _dp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp,
                                     _lp]
     L.evr_filter_diag.argtypes = [vp, C.POINTER(FilterOpts), _dp, _dp, _dp, _dp, C.POINTER(C.c_int), _dp, _lp]
+    L.evr_lanczos.argtypes = [vp, C.POINTER(LanczosOpts), _dp, _dp, _dp, _dp, _lp]
     _lib = L
     return L
 
@@ -537,6 +543,22 @@ class Problem:
     def set_operator(self, form):
         """'H' (the reference's OpPsi), 'HT' (its transpose) or 'HSYM' ((H+H^T)/2)."""
         self._check(load().evr_set_operator(self.h, {"H": 0, "HT": 1, "HSYM": 2}[form]))
+
+    def lanczos(self, nev, ncv=0, max_restarts=300, tol=0.0, v0=None, sym=-1, seed=1, want_vectors=False):
+        """Restarted Lanczos for the lowest nev levels (the reference's ARPACK path,
+        sub_propagation_Arpack_Sym); returns (eig, vectors or None, rel_resid, stats)."""
+        L = load()
+        o = LanczosOpts()
+        o.nev, o.ncv, o.max_restarts, o.tol, o.sym, o.seed = nev, ncv, max_restarts, tol, sym, seed
+        v = None if v0 is None else np.ascontiguousarray(v0, dtype=np.float64).reshape(self.N)
+        eig, rres = np.zeros(nev), np.zeros(nev)
+        vec = np.zeros((self.N, nev), order="F") if want_vectors else None
+        info = np.zeros(4, dtype=np.int64)
+        rc = L.evr_lanczos(self.h, C.byref(o), _p(v, _dp), _p(eig, _dp), _p(vec, _dp), _p(rres, _dp), _p(info, _lp))
+        stats = dict(restarts=int(info[0]), hpsi=int(info[1]), converged=int(info[2]), ncv=int(info[3]))
+        if rc not in (0, EVR_ENOCONV):
+            self._check(rc)
+        return eig, vec, rres, stats
 
     def filter_diag(self, hmin, hmax, e0, width, n_filters, max_order=2000, q0=None, nstart=1, prec="fp64",
                     conv_resi=1e-6, seed=1, want_vectors=False):

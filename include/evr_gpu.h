@@ -335,6 +335,34 @@ typedef struct evr_filter_opts {
 int evr_filter_diag(evr_ctx *ctx, const evr_filter_opts *opts, const double *q0, double *eig, double *resid,
                     double *vec, int *n_out, double *window, int64_t *info);
 
+/*
+ * Restarted Lanczos for the lowest levels (the reference's ARPACK path).
+ * Replaces sub_propagation_Arpack_Sym (Source_ElVibRot/sub_propagation/sub_module_Arpack.f90:
+ * 680-1139), which calls ARPACK's dsaupd/dseupd (implicitly restarted Lanczos with exact
+ * shifts, which = 'SM', ncv = 2*nev + 10, tol = 0) with one OpPsi per request.  Here a
+ * thick-restart Lanczos on the GPU (the same Krylov spaces as exact-shift implicit
+ * restarts): Lanczos steps with full re-orthogonalisation up to ncv vectors, Ritz pairs of
+ * the projected matrix, convergence when the Ritz bound |beta y_m| <= tol max(eps^(2/3),
+ * |E|) for all nev levels (ARPACK's test), else a restart that keeps the lowest Ritz vectors
+ * and the last Lanczos vector.  The lowest (smallest algebraic) levels are computed, which
+ * is what 'SM' selects on the positive spectra of vibrational Hamiltonians.  FP64 H.psi;
+ * the operator is H or (H + H^T)/2 as sym selects (Lanczos needs a symmetric operator).
+ * v0: optional HOST start vector (N); NULL = seeded random.  eig: out, nev eigenvalues.
+ * vec: optional HOST out (N x nev column-major).  rel_resid: optional out, |H x - E x|/|E|
+ * per level, computed with one more H.psi of the Ritz vectors (as the reference's d(j,2)).
+ * info: optional out [restarts, H.psi count, converged levels, ncv].  Returns EVR_ENOCONV
+ * (outputs filled) when max_restarts passes leave levels unconverged. */
+typedef struct evr_lanczos_opts {
+  int nev;               /* levels wanted (nb_diago)                                       */
+  int ncv;               /* basis size; 0 = 2*nev + 10 as the reference (at most N, 512)   */
+  int max_restarts;      /* maxitr (the reference: min(max_diago, max_it))                 */
+  double tol;            /* relative Ritz bound; 0 = machine epsilon (the reference's tol=0) */
+  int sym;               /* 0 = H, 1 = (H + H^T)/2, -1 = (H + H^T)/2 when some nq > nb     */
+  unsigned long long seed; /* random start vector when v0 is NULL                          */
+} evr_lanczos_opts;
+int evr_lanczos(evr_ctx *ctx, const evr_lanczos_opts *opts, const double *v0, double *eig, double *vec,
+                double *rel_resid, int64_t *info);
+
 /* FMA issue-rate micro-benchmark of the device (independent FMA chains, no memory
  * traffic): the peak of the CUDA-core pipe the contractions run on, in TFLOP/s.
  * Utility for roofline reporting; no counterpart in the reference. */
