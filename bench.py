@@ -25,7 +25,8 @@ seed (synthetic inputs with the benchmark's shapes and distributions).
            batch         256 uneven Smolyak problems (D 3..6, L 4..8), lowest 10 levels each,
                          lock-step batched Davidson, FP64 and mixed;
            prop12d       D=12 Smolyak L=6 Chebyshev propagation (dt = 10 au) timed on 200
-                         steps in complex128 and complex64-contraction form; the 2000-step
+                         steps in complex128 and complex64-contraction form (CUDA cores
+                         and tcgen05 tensor cores); the 2000-step
                          time of the workload is extrapolated from them (labelled so); the
                          FP32 - FP64 autocorrelation difference and an FP64 norm / energy
                          check of the final packets;
@@ -225,11 +226,13 @@ def run_profile(args):
     return 0
 
 
-# DRAM bytes (read + write) of one FP64 64-vector launch of the term kernels: an ncu
-# capture of the D=6 L=6 launch (`--profile sg4_6d_l6 --prec fp64`; 1.335 GB read + 0.074 GB
-# written, dominated by the per-point G table and V) scaled to the L=8 grid (37.77 M /
-# 6.49 M points)
-TRAFFIC_PER_LAUNCH = (1335056896 + 73895168) * 37.769167 / 6.487975
+# DRAM bytes (read + write) of one FP64 64-vector launch of the term kernels: a one-pass ncu
+# capture of the D=6 L=6 launch (`--profile sg4_6d_l6 --prec fp64`, metrics
+# dram__bytes_read.sum and dram__bytes_write.sum of both term kernels: slab kernel 1.338 GB
+# read + 0.571 GB written, general kernel 0.009 GB + 0.033 GB; the reads are dominated by
+# the per-point G table and V, the writes are staged tensors leaving L2) scaled to the L=8
+# grid by the grid points (37.77 M / 6.49 M)
+TRAFFIC_PER_LAUNCH = (1338332416 + 571358464 + 9097728 + 33347072) * 37.769167 / 6.487975
 DAV_LEVELS, DAV_BLOCK, DAV_RESI = 50, 64, 1e-7
 
 
@@ -319,7 +322,8 @@ def bench_batch(args):
 def bench_prop12d(args):
     """D=12 Smolyak L=6 (nb = nq = 2l+1), Gaussian displaced by 1.0 in modes 1-3, Chebyshev
     dt = 10 au in complex128 and with FP32 contractions (complex64 arithmetic in the
-    contractions, FP64 recurrence, autocorrelation and norm)."""
+    contractions, FP64 recurrence, autocorrelation and norm), the latter on the CUDA cores
+    and on the tcgen05 tensor cores."""
     from evrgpu import spec as S
     from evrgpu.lib import Problem
 
@@ -355,21 +359,24 @@ def bench_prop12d(args):
     e0 = float(np.vdot(psi0, p.hpsi(psi0.real[:, None])[:, 0]).real)  # psi0 is real
     ac, fin = {}, {}
     steps = args.prop_steps
-    for prec in ("fp64", "fp32"):
+    for key, prec, tc in (("fp64", "fp64", False), ("fp32", "fp32", False), ("fp32_tensor_cores", "fp32", True)):
+        p.set_tensor_cores(tc, 64)
         p.chebyshev(psi0, 10.0, 2, emin, emax, prec=prec)
         t0 = time.perf_counter()
         a, psiT, st = p.chebyshev(psi0, 10.0, steps, emin, emax, prec=prec, want_psi=True)
         dt = time.perf_counter() - t0
-        ac[prec] = a[:, 0]
+        ac[key] = a[:, 0]
         # FP64 checks of the final packet: norm and energy <psi|H|psi> (FP64 H.psi)
         x = psiT[:, 0]
         hx = p.hpsi(np.stack([x.real, x.imag], axis=1))
         en = float((np.vdot(x.real, hx[:, 0]) + np.vdot(x.imag, hx[:, 1])).real / np.vdot(x, x).real)
-        key = "fp64" if prec == "fp64" else "fp32"
         out[key] = {"steps": steps, "s": dt, "s_per_step": dt / steps, "order": st["max_order"],
                     "norm_final_minus_1": float(np.vdot(x, x).real - 1.0), "energy_drift_au": en - e0,
                     "s_2000_steps_extrapolated": 2000 * dt / steps}
+    p.set_tensor_cores(False)
     out["autocorr_max_abs_diff_fp32_vs_fp64"] = float(np.abs(ac["fp32"] - ac["fp64"]).max())
+    out["autocorr_max_abs_diff_fp32_tensor_cores_vs_fp64"] = float(
+        np.abs(ac["fp32_tensor_cores"] - ac["fp64"]).max())
     out["autocorr_last"] = [float(ac["fp64"][-1].real), float(ac["fp64"][-1].imag)]
     out["note"] = (f"timed on {steps} of the workload's 2000 steps; s_2000_steps_extrapolated = "
                    f"2000 x measured s per step")

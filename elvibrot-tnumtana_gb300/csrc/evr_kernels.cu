@@ -279,7 +279,7 @@ int term_kernel_smem(evr_ctx* c, int* items_bytes, int* slab_bytes) {
   // multiples of 256 bytes below the limits
   slab_bytes[EVR_PREC_FP64] = (std::min(optin - st_slab, per_sm / slab_ctas<double>() - reserved - st_slab)) & ~255;
   slab_bytes[EVR_PREC_FP32] = (std::min(optin - st_slab, per_sm / slab_ctas<float>() - reserved - st_slab)) & ~255;
-  *items_bytes = (std::min(optin - st_items, per_sm / 2 - reserved - st_items)) & ~255;
+  *items_bytes = (std::min(optin - st_items, per_sm / kItemsCtas - reserved - st_items)) & ~255;
   return EVR_OK;
 }
 
@@ -320,9 +320,9 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
   const HostProblem& P = c->hp;
   int rc = EVR_OK;
   if (!w.counter) {
-    // general kernel: 2 CTAs per SM; slab kernel: 1 CTA per SM
+    // general kernel: kItemsCtas CTAs per SM; slab kernel: slab_ctas<T>() CTAs per SM
     if ((rc = term_kernel_smem(c, &w.smem_bytes, w.smem_slab_bytes))) return rc;
-    w.grid = c->num_sms * 2;
+    w.grid = c->num_sms * kItemsCtas;
     w.grid_slab[EVR_PREC_FP64] = c->num_sms * slab_ctas<double>();
     w.grid_slab[EVR_PREC_FP32] = c->num_sms * slab_ctas<float>();
     size_t slab = 0;  // general kernel: FP64 buffers of the terms that run from global memory
@@ -779,7 +779,7 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
   EVR_CU((set_term_kernel_smem<double, false>(smem_items, smem_slab[EVR_PREC_FP64])), "attr");
   int per_sm = 0;
   EVR_CU((occupancy_items_kernel<double, false>(&per_sm, smem_items)), "occupancy");
-  const int grid = c->num_sms * std::max(1, std::min(per_sm, 2));
+  const int grid = c->num_sms * std::max(1, std::min(per_sm, kItemsCtas));
   size_t slab = 0, msz = 0;
   for (const TermDesc& Tm : P.terms) {
     slab = std::max(slab, footprint_elems<double>(P, Tm, 1));

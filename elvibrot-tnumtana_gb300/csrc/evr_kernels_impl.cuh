@@ -12,7 +12,10 @@
 namespace evr {
 namespace kern {
 
-constexpr int kThreads = 256;
+// general (items) kernel: resident CTAs per SM and threads of one (four CTAs of 128 threads
+// measured 1 % slower in FP64 at D=6 L=8)
+constexpr int kItemsCtas = 2;
+constexpr int kThreads = 512 / kItemsCtas;
 
 template <typename T>
 struct ItemParams {
@@ -75,14 +78,15 @@ void set_plain(ItemParams<T>& p) {
   p.jgrid = nullptr;
 }
 
-// Resident slab-kernel CTAs per SM, and the threads of one: several smaller CTAs per SM,
-// each with its share of the SM's shared memory, overlap one CTA's barriers and
-// shared-memory waits with another's FMAs.  Measured on the D=6 L=8 launch: FP64 712 ms
-// with one CTA of 512 threads, 628 ms with two of 256, 606 ms with four of 128; FP32 114,
-// 112 and 154 ms (its items need the larger shared memory).  FP32 with one CTA of 1024
-// threads, 64 registers and one fibre per thread measured 5 % slower.
+// Resident slab-kernel CTAs per SM, and the threads of one: two CTAs of 256 threads, each
+// with half of the SM's shared memory, overlap one CTA's barriers and shared-memory waits
+// with the other's FMAs.  Measured on the D=6 L=8 launch: FP64 712 ms with one CTA of 512
+// threads, 628 ms with two, 606 ms with four of 128 threads -- but with four most FP64 terms
+// no longer fit and run in the general kernel from global buffers (55 GB of DRAM traffic
+// per D=6 L=6 launch against 1.9 GB with two); FP32 114, 112 and 154 ms.  FP32 with one
+// CTA of 1024 threads, 64 registers and one fibre per thread measured 5 % slower.
 template <typename T>
-constexpr int slab_ctas() { return sizeof(T) == 8 ? 4 : 2; }
+constexpr int slab_ctas() { return 2; }
 template <typename T>
 constexpr int slab_threads() { return 512 / slab_ctas<T>(); }
 
@@ -637,7 +641,7 @@ __device__ __forceinline__ void items_jac_post(const ItemParams<T>& p, const Ter
 }
 
 template <typename T, bool GFLY>
-__global__ void __launch_bounds__(kThreads, 2) hpsi_items_kernel(ItemParams<T> p) {
+__global__ void __launch_bounds__(kThreads, kItemsCtas) hpsi_items_kernel(ItemParams<T> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   __shared__ TermDesc s_term;
