@@ -319,7 +319,9 @@ template <typename T>
 __device__ __forceinline__ void contract(const T* in, int64_t ldi, T* out, int64_t ldo, const FastDiv& A, int K, int M,
                                          int B, const FastDiv& Vt, const T* mat, T alpha, bool acc) {
   if constexpr (sizeof(T) == 4) {  // FP32: two columns per thread, matrix coefficients from shared memory
-    constexpr int C = 2;  // four fibres per thread for M <= 12 measured 9 % slower
+    // four fibres per thread for M <= 12 measured 9 % slower, and a thread walking a chunk of
+    // four fibres along B (one index decode per chunk) 14 % slower
+    constexpr int C = 2;
     if (M <= 4) contract_m<T, 4, C>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else if (M <= 8) contract_m<T, 8, C>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
     else if (M <= 12) contract_m<T, 12, C>(in, ldi, out, ldo, A, K, M, B, Vt, mat, alpha, acc);
