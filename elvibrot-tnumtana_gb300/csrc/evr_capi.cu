@@ -165,6 +165,12 @@ int evr_set_vgrid(evr_ctx* c, const double* v, int layout) {
   if (!c) return EVR_EINVAL;
   if (!v || (layout != EVR_VGRID_TERMS && layout != EVR_VGRID_REF))
     return set_error(c, EVR_EINVAL, "evr_set_vgrid: null values or unknown layout");
+  {
+    const int64_t n = c->hp.sum_nq * c->hp.nb0 * c->hp.nb0;
+    for (int64_t i = 0; i < n; ++i)
+      if (!std::isfinite(v[i]))
+        return set_error(c, EVR_EINVAL, "evr_set_vgrid: value " + std::to_string(i) + " is not finite");
+  }
   if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
   if (c->batch) return set_error(c, EVR_EINVAL, "evr_set_vgrid: not for batched contexts");
   EVR_CU(cudaSetDevice(c->device), "cudaSetDevice");
@@ -193,6 +199,9 @@ int evr_set_ggrid(evr_ctx* c, const double* G) {
   const HostProblem& P = c->hp;
   if (P.keo_type != 10) return set_error(c, EVR_EINVAL, "evr_set_ggrid: the KEO of the context is not type 10");
   const int D = P.D, stride = g_table_stride(D);
+  for (int64_t i = 0; i < P.sum_nq * D * D; ++i)
+    if (!std::isfinite(G[i]))
+      return set_error(c, EVR_EINVAL, "evr_set_ggrid: value " + std::to_string(i) + " is not finite");
   for (int64_t iq = 0; iq < P.sum_nq; ++iq) {  // the matrices must be symmetric
     const double* Gq = G + (size_t)iq * D * D;
     for (int i = 0; i < D; ++i)

@@ -410,6 +410,12 @@ int evr_set_dipole_grid(evr_ctx* c, const double* mu, int layout) {
   if (!mu || (layout != EVR_VGRID_TERMS && layout != EVR_VGRID_REF))
     return set_error(c, EVR_EINVAL, "evr_set_dipole_grid: null values or unknown layout");
   if (c->batch) return set_error(c, EVR_EINVAL, "evr_set_dipole_grid: not for batched contexts");
+  {
+    const int64_t n = c->hp.sum_nq * c->hp.nb0 * c->hp.nb0;
+    for (int64_t i = 0; i < n; ++i)
+      if (!std::isfinite(mu[i]))
+        return set_error(c, EVR_EINVAL, "evr_set_dipole_grid: value " + std::to_string(i) + " is not finite");
+  }
   if (c->host_only) return set_error(c, EVR_EDEVICE, "host-only context (created with device < 0)");
   int rc = cuda_check(c, cudaSetDevice(c->device), "cudaSetDevice");
   if (rc) return rc;

@@ -141,8 +141,9 @@ int evr_get_vgrid(const evr_ctx *ctx, double *v);
  * reference's OpGrid(iterm)%Grid(sum_nq, nb0, nb0), element (iq, a, b) at
  * iq + sum_nq*(a + nb0*b), with iq the point of the whole Smolyak grid (terms in the
  * reference's order, first mode fastest inside a term) and a the output state.  The two
- * layouts agree for nb0 = 1.  Synchronous (waits for the device first); a set-up call,
- * not for use inside stream capture; not for batched contexts. */
+ * layouts agree for nb0 = 1.  Non-finite values are rejected with EVR_EINVAL (the message
+ * names the first).  Synchronous (waits for the device first); a set-up call, not for use
+ * inside stream capture; not for batched contexts. */
 #define EVR_VGRID_TERMS 0
 #define EVR_VGRID_REF   1
 int evr_set_vgrid(evr_ctx *ctx, const double *v, int layout);
@@ -150,7 +151,7 @@ int evr_set_vgrid(evr_ctx *ctx, const double *v, int layout);
  * at each grid point (Source_ElVibRot/sub_Operator/sub_OpPsi_SG4.f90:2717-2728, where the
  * reference recomputes it on every H.psi), in place of G0 + sum_k g_ijk Q_k.  G: sum_nq
  * symmetric D x D matrices, point iq (the reference's whole-grid order, as EVR_VGRID_REF)
- * at G + iq*D*D, column-major.  Each matrix must be symmetric: entries with
+ * at G + iq*D*D, column-major.  Values must be finite, and each matrix symmetric: entries with
  * |G_ij - G_ji| > 1e-12 max(1, |G_ij|) are rejected with EVR_EINVAL, and the table stores
  * 0.5 (G_ij + G_ji).  The operator stays -1/2 sum_ij d_i G_ij(Q) d_j (Jacobian and rho
  * constant).  A context created with a constant G gets its per-point table here (captured

@@ -87,6 +87,14 @@ def test_set_vgrid_argument_checks():
         pg.set_dipole_grid(v)
     assert ei.value.code == E.EVR_EDEVICE
     assert L.evr_set_dipole_grid(pg.h, v.ctypes.data_as(E._dp), -1) == E.EVR_EINVAL
+    # non-finite grid values are rejected before any upload, naming the value
+    for bad in (np.nan, np.inf):
+        vb = v.copy()
+        vb[7] = bad
+        for setter in (pg.set_vgrid, pg.set_dipole_grid):
+            with pytest.raises(E.EvrError) as ei:
+                setter(vb)
+            assert ei.value.code == E.EVR_EINVAL and "value 7" in str(ei.value)
 
 
 def test_sil_needs_a_device():
@@ -121,6 +129,11 @@ def test_set_ggrid_argument_checks():
     with pytest.raises(E.EvrError) as ei:
         pt.set_ggrid(G)
     assert ei.value.code == E.EVR_EINVAL and "grid point 5" in str(ei.value)
+    G = np.tile(np.eye(3), (pt.sum_nq, 1, 1))
+    G[3, 1, 1] = np.nan  # a diagonal NaN passes the symmetry test; the finiteness test catches it
+    with pytest.raises(E.EvrError) as ei:
+        pt.set_ggrid(G)
+    assert ei.value.code == E.EVR_EINVAL and "not finite" in str(ei.value)
 
 
 def test_set_jacobian_argument_checks():
