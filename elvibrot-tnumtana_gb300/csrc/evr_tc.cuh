@@ -18,8 +18,9 @@
 //   * every warp reads its lane quarter of the accumulator (tcgen05.ld 32x32b) and writes
 //     its fibres' outputs (coalesced: consecutive lanes are consecutive fibres).
 // The dropped lo*lo term and the rounding of lo leave a relative error near 2^-23 per
-// product, FP32 level.  Waits on the mbarrier are bounded: on expiry the CTA records an
-// error code and leaves the contraction.
+// product, FP32 level.  Waits on the mbarrier are bounded: on expiry the CTA gives the
+// pending MMAs one more bounded wait, records an error code, leaves the contraction and
+// runs its later contractions on the CUDA cores; it frees its accumulator at its end.
 #pragma once
 #include <cstdint>
 
@@ -307,9 +308,15 @@ __device__ __noinline__ void contract_tc(TcState& st, const float* __restrict__ 
   // the last tile's outcome; the caller's next contraction may overwrite the operands
   const bool lost = __syncthreads_or(!ok) != 0;
   fence_after_sync();
-  if (lost && threadIdx.x == 0) {
-    sm->failed = 1;
-    atomicExch(st.err, 2);
+  if (lost) {
+    // give the MMAs whose commit was not seen one more bounded wait (the phase before the
+    // flip), so that the accumulator is normally idle when the CTA frees it at its end;
+    // later contractions of the CTA run on the CUDA cores
+    (void)mbar_wait(mbar, st.phase ^ 1u);
+    if (threadIdx.x == 0) {
+      sm->failed = 1;
+      atomicExch(st.err, 2);
+    }
   }
 }
 
