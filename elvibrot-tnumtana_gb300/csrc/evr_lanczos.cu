@@ -192,6 +192,7 @@ extern "C" int evr_lanczos(evr_ctx* c, const evr_lanczos_opts* o, const double* 
       beta_last = beta;
       if (j + 1 < m) T[j + (size_t)m * (j + 1)] = beta;  // coupling of v_j and v_(j+1)
       if (!(beta > 0.0)) {  // invariant subspace: the basis cannot grow
+        if (j + 1 == m) break;  // full basis: the Ritz pairs are exact (all levels pass the test)
         return L.fail(EVR_ENOCONV, "Lanczos breakdown (invariant subspace of size " + std::to_string(j + 1) + ")");
       }
       lanczos_scale_col<<<L.grid, 256, 0, s>>>(W.p, 1, V.p + (j + 1), ldv, 1.0 / beta, N);
