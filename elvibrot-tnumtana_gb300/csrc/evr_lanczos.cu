@@ -188,7 +188,10 @@ extern "C" int evr_lanczos(evr_ctx* c, const evr_lanczos_opts* o, const double* 
       if ((rc = L.colnorm2(W.p, 1, 1, nrm.p))) return rc;
       double b2 = 0.0;
       if ((rc = L.to_host(nrm.p, 1, &b2))) return rc;
-      const double beta = std::sqrt(std::max(b2, 0.0));
+      // with j + 1 == N the basis spans the whole space and w is rounding error: the
+      // coupling is zero and the Ritz pairs are exact (ncv = min(N, 2 nev + 10) reaches N
+      // on small problems, as in the reference)
+      const double beta = j + 1 == N ? 0.0 : std::sqrt(std::max(b2, 0.0));
       beta_last = beta;
       if (j + 1 < m) T[j + (size_t)m * (j + 1)] = beta;  // coupling of v_j and v_(j+1)
       if (!(beta > 0.0)) {  // invariant subspace: the basis cannot grow

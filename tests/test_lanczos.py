@@ -39,6 +39,22 @@ def test_lanczos_small_operator_matches_dense():
     assert np.abs(eig2 - w[:6]).max() <= 1e-10
 
 
+def test_lanczos_full_basis_is_exact():
+    """ncv = min(N, 2 nev + 10) reaches N on a small problem (N = 13 here): one sweep spans
+    the space and every level comes out exact, without a restart."""
+    from evrgpu import lib as E
+
+    spec = S.config_sg4(2, 2, seed=7, nq_A=1)
+    H, w = dense_levels(spec)
+    p = E.Problem(spec, device=0)
+    assert p.N == 13
+    eig, vec, rres, st = p.lanczos(3, want_vectors=True)
+    assert st["ncv"] == 13 and st["restarts"] == 1 and st["converged"] == 3
+    assert np.abs(eig - w[:3]).max() <= 1e-11
+    assert np.abs(vec.T @ vec - np.eye(3)).max() <= 1e-11
+    assert rres.max() <= 1e-11
+
+
 def test_lanczos_hh6d_matches_dense_and_benchmark(golden):
     from evrgpu import lib as E
 
