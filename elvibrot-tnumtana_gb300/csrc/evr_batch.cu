@@ -570,6 +570,7 @@ static int upload_batch(evr_ctx* c) {
   if ((rc = up((void**)&d.csr_ptr, P.csr_ptr.data(), P.csr_ptr.size() * sizeof(int64_t)))) return rc;
   if ((rc = up((void**)&d.csr_src, P.csr_src.data(), P.csr_src.size() * sizeof(int64_t)))) return rc;
   if ((rc = up((void**)&d.csr_w, P.csr_w.data(), P.csr_w.size() * sizeof(double)))) return rc;
+  if ((rc = upload_long_rows(c))) return rc;
   if ((rc = up((void**)&d.G0, P.G0.data(), P.G0.size() * sizeof(double)))) return rc;
   if ((rc = up((void**)&d.g, P.g.data(), P.g.size() * sizeof(double)))) return rc;
   if ((rc = up((void**)&d.e0diag, P.e0diag.data(), P.e0diag.size() * sizeof(double)))) return rc;

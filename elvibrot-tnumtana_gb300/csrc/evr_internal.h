@@ -18,6 +18,12 @@ constexpr int kMaxD = 24;      // modes (positions of a term and modes of a prob
 __host__ __device__ constexpr int g_table_stride(int D) { return (D * (D + 1) / 2 + 3) & ~3; }
 constexpr int kMaxN1 = 24;     // largest 1-D nq (and nb)
 constexpr int kMaxNb0 = 4;     // electronic states
+// default size (grid points x vectors of an item) below which a term runs in the general
+// kernel instead of the slab kernel (evr_autotune re-chooses it)
+constexpr int kSmallTermPoints = 2048;
+// weighted reduction: rows of at most this many entries are summed by one thread per
+// (row, vector), longer ones (the low basis functions, shared by many terms) by a CTA
+constexpr int kCsrShortRow = 64;
 
 // ---------------------------------------------------------------------------
 // Host-side tables (built once by evr_setup.cpp)
@@ -127,6 +133,8 @@ struct DeviceProblem {
   int64_t* csr_ptr = nullptr;
   int64_t* csr_src = nullptr;
   double* csr_w = nullptr;
+  int64_t* csr_long = nullptr;      // rows with more than kCsrShortRow entries
+  int64_t n_long = 0;
   double* G0 = nullptr;
   double* g = nullptr;
   double* mono_coef = nullptr;
@@ -142,7 +150,9 @@ struct ItemSet {
   int n_items = 0;
   WorkItem* items_slab = nullptr;  // slab kernel
   int n_slab = 0;
-  std::vector<WorkItem> h_items, h_slab;  // host copies (filtered launches of batches)
+  WorkItem* items_small = nullptr;  // general kernel as small CTAs (small terms)
+  int n_small = 0;
+  std::vector<WorkItem> h_items, h_slab, h_small;  // host copies (filtered launches of batches)
 };
 
 struct Workspace {
@@ -156,12 +166,14 @@ struct Workspace {
   double* xin = nullptr;            // interleaved copies (layout conversions)
   double* xout = nullptr;
   int grid = 0, smem_bytes = 0;             // general kernel
+  int grid_small = 0, smem_small_bytes = 0; // general kernel as small CTAs
   // slab kernel, per precision (index EVR_PREC_FP64 / EVR_PREC_FP32): grid, dynamic shared
   // memory and global tensor per CTA
   int grid_slab[2] = {0, 0}, smem_slab_bytes[2] = {0, 0};
   size_t slab_slab_bytes[2] = {0, 0};
   WorkItem* f_items = nullptr;              // filtered item lists (terms of active problems)
   WorkItem* f_slab = nullptr;
+  WorkItem* f_small = nullptr;
   size_t f_cap = 0;
 };
 
@@ -199,7 +211,9 @@ struct evr_ctx {
   bool use_stages = true;           // grid-wide stage path for single-term problems
   bool gfly = false;                // G(Q) from the linear model per point instead of a table
   int vt_cap_slab = 32, vt_cap_items = 32;  // widest vector tile of an item (evr_autotune)
-  int slab_min_points = 0;          // terms with fewer grid points x vectors run in the general kernel
+  // terms with fewer grid points x vectors run in the general kernel, as small CTAs when
+  // their buffers fit one
+  int slab_min_points = evr::kSmallTermPoints;
   int64_t ws_gen = 0;               // bumped whenever workspace buffers are freed (captured graphs)
   std::vector<unsigned char> term_active;  // batches: terms to run (empty = all)
   int n_sys = 1;                    // problems stacked in this context (evr_create_batch)
@@ -252,6 +266,7 @@ void free_stages(evr_ctx* c);
 void free_control(evr_ctx* c);
 void free_batch_info(evr_ctx* c);
 // weighted CSR reduction of the term-basis output(s) into y (evr_kernels.cu)
+int upload_long_rows(evr_ctx* c);
 int reduce_terms(evr_ctx* c, int prec, const void* ht, const void* ht2, int nvec, double scale, double* y,
                  int64_t ldy, cudaStream_t s);
 // evaluates monomials (device arrays) on every term grid into out (sum_nq * nb0^2) and

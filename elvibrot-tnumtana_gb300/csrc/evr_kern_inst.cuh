@@ -33,8 +33,8 @@ template cudaError_t set_slab_kernel_smem<EVR_KT, EVR_KGFLY, EVR_KTC>(int);
 template cudaError_t slab_kernel_static_smem<EVR_KT, EVR_KGFLY, EVR_KTC>(int*);
 #else
 template <typename T, bool GFLY>
-cudaError_t launch_items_kernel(int grid, size_t smem, cudaStream_t s, const ItemParams<T>& p) {
-  hpsi_items_kernel<T, GFLY><<<grid, kThreads, smem, s>>>(p);
+cudaError_t launch_items_kernel(int grid, size_t smem, cudaStream_t s, const ItemParams<T>& p, int threads) {
+  hpsi_items_kernel<T, GFLY><<<grid, threads, smem, s>>>(p);
   return cudaGetLastError();
 }
 template <typename T, bool GFLY>
@@ -52,7 +52,8 @@ cudaError_t items_kernel_static_smem(int* bytes) {
   *bytes = e == cudaSuccess ? (int)a.sharedSizeBytes : 0;
   return e;
 }
-template cudaError_t launch_items_kernel<EVR_KT, EVR_KGFLY>(int, size_t, cudaStream_t, const ItemParams<EVR_KT>&);
+template cudaError_t launch_items_kernel<EVR_KT, EVR_KGFLY>(int, size_t, cudaStream_t, const ItemParams<EVR_KT>&,
+                                                             int);
 template cudaError_t set_items_kernel_smem<EVR_KT, EVR_KGFLY>(int);
 template cudaError_t items_kernel_static_smem<EVR_KT, EVR_KGFLY>(int*);
 template cudaError_t occupancy_items_kernel<EVR_KT, EVR_KGFLY>(int*, int);

@@ -32,28 +32,86 @@ using namespace kern;
 namespace {
 
 // y[k*ldy + v] = scale * sum_{e in row k} w_e * (ht[src_e*ldh + v] (+ ht2[...]))   (FP64 accumulation)
+// The first short_blocks CTAs take the rows of at most kCsrShortRow entries, one thread per
+// (row, vector) summing its row in order.  The others take the long rows of the list (the
+// low basis functions, which every term's basis holds: at D=12 L=6 the first row has
+// 18,564 entries), one CTA per row: thread (g, l) sums the entries g, g + ng, ... of vector
+// v0 + l, and the ng partial sums of each vector are added in a fixed pairwise tree.  Both
+// orders are fixed, so the result is the same run to run.
 template <typename T>
-__global__ void csr_reduce_kernel(const int64_t* __restrict__ ptr, const int64_t* __restrict__ src,
-                                  const double* __restrict__ wt, const T* __restrict__ ht, const T* __restrict__ ht2,
-                                  int64_t ldh, double scale, double* __restrict__ y, int64_t ldy, int64_t N,
-                                  int nvec) {
-  const int64_t total = N * nvec;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t k = idx / nvec;
-    const int v = (int)(idx - k * nvec);
-    double s = 0.0;
-    const int64_t e1 = __ldg(ptr + k + 1);
-    if (ht2) {
-      for (int64_t e = __ldg(ptr + k); e < e1; ++e) {
-        const int64_t o = __ldg(src + e) * ldh + v;
-        s = fma(__ldg(wt + e), (double)ht[o] + (double)ht2[o], s);
+__global__ void __launch_bounds__(256) csr_reduce_kernel(const int64_t* __restrict__ ptr,
+                                                         const int64_t* __restrict__ src,
+                                                         const double* __restrict__ wt, const T* __restrict__ ht,
+                                                         const T* __restrict__ ht2, int64_t ldh, double scale,
+                                                         double* __restrict__ y, int64_t ldy, int64_t N, int nvec,
+                                                         const int64_t* __restrict__ long_rows, int64_t n_long,
+                                                         int short_blocks) {
+  if ((int)blockIdx.x < short_blocks) {
+    const int64_t total = N * nvec;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)short_blocks * blockDim.x) {
+      const int64_t k = idx / nvec;
+      const int v = (int)(idx - k * nvec);
+      const int64_t e0 = __ldg(ptr + k), e1 = __ldg(ptr + k + 1);
+      if (e1 - e0 > kCsrShortRow) continue;  // a long row: the CTAs below
+      double s = 0.0;
+      if (ht2) {
+        for (int64_t e = e0; e < e1; ++e) {
+          const int64_t o = __ldg(src + e) * ldh + v;
+          s = fma(__ldg(wt + e), (double)ht[o] + (double)ht2[o], s);
+        }
+      } else {
+        for (int64_t e = e0; e < e1; ++e) s = fma(__ldg(wt + e), (double)ht[__ldg(src + e) * ldh + v], s);
       }
-    } else {
-      for (int64_t e = __ldg(ptr + k); e < e1; ++e) s = fma(__ldg(wt + e), (double)ht[__ldg(src + e) * ldh + v], s);
+      y[k * ldy + v] = scale * s;
     }
-    y[k * ldy + v] = scale * s;
+    return;
   }
+  __shared__ double part[256];
+  const int vc = nvec < 32 ? nvec : 32;         // vector lanes
+  const int ng = (int)blockDim.x / vc;          // entry groups
+  const int g = (int)threadIdx.x / vc, l = (int)threadIdx.x - g * vc;
+  const bool on = g < ng;
+  const int nlb = (int)gridDim.x - short_blocks;
+  for (int64_t li = (int64_t)blockIdx.x - short_blocks; li < n_long; li += nlb) {
+    const int64_t k = __ldg(long_rows + li);
+    const int64_t e0 = __ldg(ptr + k), e1 = __ldg(ptr + k + 1);
+    for (int v0 = 0; v0 < nvec; v0 += vc) {
+      const int v = v0 + l;
+      double s = 0.0;
+      if (on && v < nvec) {
+        if (ht2) {
+          for (int64_t e = e0 + g; e < e1; e += ng) {
+            const int64_t o = __ldg(src + e) * ldh + v;
+            s = fma(__ldg(wt + e), (double)ht[o] + (double)ht2[o], s);
+          }
+        } else {
+          for (int64_t e = e0 + g; e < e1; e += ng) s = fma(__ldg(wt + e), (double)ht[__ldg(src + e) * ldh + v], s);
+        }
+      }
+      part[threadIdx.x] = s;
+      __syncthreads();
+      for (int h = 1; h < ng; h <<= 1) {
+        if (on && (g & (2 * h - 1)) == 0 && g + h < ng) part[threadIdx.x] += part[threadIdx.x + h * vc];
+        __syncthreads();
+      }
+      if (g == 0 && v < nvec) y[k * ldy + v] = scale * part[l];
+      __syncthreads();
+    }
+  }
+}
+
+// launch of csr_reduce_kernel: the short-row CTAs (at most 16 per SM) and one CTA per long
+// row up to 8 per SM
+template <typename T>
+static cudaError_t launch_csr_reduce(const evr_ctx* c, const T* ht, const T* ht2, int64_t ldh, double scale,
+                                     double* y, int64_t ldy, int nvec, cudaStream_t s) {
+  const int64_t N = c->hp.Np * c->hp.nb0;
+  const int sb = (int)std::max<int64_t>(1, std::min<int64_t>((N * nvec + 255) / 256, (int64_t)c->num_sms * 16));
+  const int lb = (int)std::min<int64_t>(c->dp.n_long, (int64_t)c->num_sms * 8);
+  csr_reduce_kernel<T><<<sb + lb, 256, 0, s>>>(c->dp.csr_ptr, c->dp.csr_src, c->dp.csr_w, ht, ht2, ldh, scale, y, ldy,
+                                               N, nvec, c->dp.csr_long, c->dp.n_long, sb);
+  return cudaGetLastError();
 }
 
 // grid tables: V_ab(Q) from monomials (plus the term's constant of dropped 1-point modes on
@@ -182,6 +240,7 @@ int upload_problem(evr_ctx* c) {
   if ((rc = upload(c, &d.csr_ptr, P.csr_ptr))) return rc;
   if ((rc = upload(c, &d.csr_src, P.csr_src))) return rc;
   if ((rc = upload(c, &d.csr_w, P.csr_w))) return rc;
+  if ((rc = upload_long_rows(c))) return rc;
   if ((rc = upload(c, &d.G0, P.G0))) return rc;
   if ((rc = upload(c, &d.g, P.g))) return rc;
   if ((rc = upload(c, &d.mono_coef, P.mono_coef))) return rc;
@@ -219,9 +278,27 @@ int upload_problem(evr_ctx* c) {
   return EVR_OK;
 }
 
+// the rows of the weighted reduction with more than kCsrShortRow entries, on the device
+int upload_long_rows(evr_ctx* c) {
+  const std::vector<int64_t>& ptr = c->hp.csr_ptr;
+  std::vector<int64_t> rows;
+  for (size_t k = 0; k + 1 < ptr.size(); ++k)
+    if (ptr[k + 1] - ptr[k] > kCsrShortRow) rows.push_back((int64_t)k);
+  DeviceProblem& d = c->dp;
+  if (d.csr_long) cudaFree(d.csr_long);
+  d.csr_long = nullptr;
+  d.n_long = 0;
+  EVR_CU(cudaMalloc((void**)&d.csr_long, std::max<size_t>(rows.size(), 1) * sizeof(int64_t)), "cudaMalloc");
+  if (!rows.empty())
+    EVR_CU(cudaMemcpy(d.csr_long, rows.data(), rows.size() * sizeof(int64_t), cudaMemcpyHostToDevice), "cudaMemcpy");
+  d.n_long = (int64_t)rows.size();
+  return EVR_OK;
+}
+
 void free_problem(evr_ctx* c) {
   DeviceProblem& d = c->dp;
   void* ptrs[] = {d.terms, d.termsT, d.mats, d.mats32, d.vgrid, d.vgrid32, d.map, d.csr_ptr, d.csr_src, d.csr_w,
+                  d.csr_long,
                   d.G0, d.g, d.mono_coef, d.mono_idx, d.mono_elec, d.e0diag, c->dp_ggrid, c->dp_ggrid32,
                   c->dp_mugrid, c->dp_mugrid32, c->dp_jgrid, c->dp_jgrid32};
   for (void* p : ptrs)
@@ -240,8 +317,9 @@ void free_workspace(evr_ctx* c) {
   for (ItemSet& s : w.sets) {
     if (s.items) cudaFree(s.items);
     if (s.items_slab) cudaFree(s.items_slab);
+    if (s.items_small) cudaFree(s.items_small);
   }
-  void* ptrs[] = {w.counter, w.slab, w.ht, w.ht2, w.xin, w.xout, w.f_items, w.f_slab};
+  void* ptrs[] = {w.counter, w.slab, w.ht, w.ht2, w.xin, w.xout, w.f_items, w.f_slab, w.f_small};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   w = Workspace();
@@ -257,7 +335,7 @@ static size_t tc_reserve_bytes() { return (sizeof(tc::TcSmem) + 15) & ~(size_t)1
 // precision) and the general kernel's two CTAs per SM share the SM's shared memory, each
 // CTA also holding its static block and the per-block reservation.  slab_bytes[p] for
 // p = EVR_PREC_FP64, EVR_PREC_FP32.
-int term_kernel_smem(evr_ctx* c, int* items_bytes, int* slab_bytes) {
+int term_kernel_smem(evr_ctx* c, int* items_bytes, int* slab_bytes, int* small_bytes) {
   int optin = 0, per_sm = 0, reserved = 0;
   EVR_CU(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device), "attr");
   EVR_CU(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device), "attr");
@@ -280,6 +358,7 @@ int term_kernel_smem(evr_ctx* c, int* items_bytes, int* slab_bytes) {
   slab_bytes[EVR_PREC_FP64] = (std::min(optin - st_slab, per_sm / slab_ctas<double>() - reserved - st_slab)) & ~255;
   slab_bytes[EVR_PREC_FP32] = (std::min(optin - st_slab, per_sm / slab_ctas<float>() - reserved - st_slab)) & ~255;
   *items_bytes = (std::min(optin - st_items, per_sm / kItemsCtas - reserved - st_items)) & ~255;
+  if (small_bytes) *small_bytes = (std::min(optin - st_items, per_sm / kSmallCtas - reserved - st_items)) & ~255;
   return EVR_OK;
 }
 
@@ -321,8 +400,9 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
   int rc = EVR_OK;
   if (!w.counter) {
     // general kernel: kItemsCtas CTAs per SM; slab kernel: slab_ctas<T>() CTAs per SM
-    if ((rc = term_kernel_smem(c, &w.smem_bytes, w.smem_slab_bytes))) return rc;
+    if ((rc = term_kernel_smem(c, &w.smem_bytes, w.smem_slab_bytes, &w.smem_small_bytes))) return rc;
     w.grid = c->num_sms * kItemsCtas;
+    w.grid_small = c->num_sms * kSmallCtas;
     w.grid_slab[EVR_PREC_FP64] = c->num_sms * slab_ctas<double>();
     w.grid_slab[EVR_PREC_FP32] = c->num_sms * slab_ctas<float>();
     size_t slab = 0;  // general kernel: FP64 buffers of the terms that run from global memory
@@ -385,13 +465,24 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
   const int pi = f32 ? EVR_PREC_FP32 : EVR_PREC_FP64;
   const size_t slab_smem = (size_t)w.smem_slab_bytes[pi] - (f32 && c->use_tc ? tc_reserve_bytes() : 0);
   const size_t slab_glob = w.slab_slab_bytes[pi];
-  std::vector<WorkItem> items, sitems;
+  std::vector<WorkItem> items, sitems, titems;
   for (int t = 0; t < (int)P.terms.size(); ++t) {
     const TermDesc& Tm = P.terms[t];
     if (Tm.weight == 0.0) continue;
     const size_t mats = (size_t)((Tm.msz + 3) & ~3) * esz;  // staged 1-D matrices
     if (mats > (size_t)w.smem_bytes) return set_error(c, EVR_EINVAL, "1-D matrices exceed shared memory");
     const bool small = (int64_t)Tm.NQ * std::min(nvec, c->vt_cap_slab) < c->slab_min_points;
+    if (small) {
+      // the general kernel as small CTAs when the term's buffers and matrices fit one
+      const size_t fp1 = footprint_elems<double>(P, Tm, 1) * esz;
+      if (fp1 + mats <= (size_t)w.smem_small_bytes) {
+        int vt = 1;
+        while (vt * 2 <= nvec && vt * 2 <= c->vt_cap_items && fp1 * (size_t)(vt * 2) + mats <= (size_t)w.smem_small_bytes)
+          vt *= 2;
+        for (int v0 = 0; v0 < nvec; v0 += vt) titems.push_back(WorkItem{t, v0, std::min(vt, nvec - v0), 1});
+        continue;
+      }
+    }
     // W-in-global tile (shared memory holds only the slab arrays)
     auto wg_fits = [&](int v) {
       return slab_wg_smem_elems(P, Tm, v, f32) * esz + mats <= slab_smem &&
@@ -465,22 +556,37 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
   };
   std::stable_sort(items.begin(), items.end(), by_cost);
   std::stable_sort(sitems.begin(), sitems.end(), by_cost);
+  std::stable_sort(titems.begin(), titems.end(), by_cost);
   ItemSet s;
   s.nvec = nvec;
   s.prec = prec;
   s.n_items = (int)items.size();
   s.n_slab = (int)sitems.size();
+  s.n_small = (int)titems.size();
   s.items = (WorkItem*)dev_alloc<WorkItem>(items.size(), rc);
   if (rc) return set_error(c, rc, "workspace allocation (items)");
   s.items_slab = (WorkItem*)dev_alloc<WorkItem>(sitems.size(), rc);
-  if (rc) return set_error(c, rc, "workspace allocation (items)");
+  if (rc) {
+    cudaFree(s.items);
+    return set_error(c, rc, "workspace allocation (items)");
+  }
+  s.items_small = (WorkItem*)dev_alloc<WorkItem>(titems.size(), rc);
+  if (rc) {
+    cudaFree(s.items);
+    cudaFree(s.items_slab);
+    return set_error(c, rc, "workspace allocation (items)");
+  }
   if (!items.empty())
     EVR_CU(cudaMemcpy(s.items, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice), "items");
   if (!sitems.empty())
     EVR_CU(cudaMemcpy(s.items_slab, sitems.data(), sitems.size() * sizeof(WorkItem), cudaMemcpyHostToDevice),
            "items");
+  if (!titems.empty())
+    EVR_CU(cudaMemcpy(s.items_small, titems.data(), titems.size() * sizeof(WorkItem), cudaMemcpyHostToDevice),
+           "items");
   s.h_items = items;
   s.h_slab = sitems;
+  s.h_small = titems;
   w.sets.push_back(s);
   return EVR_OK;
 }
@@ -563,13 +669,29 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
     EVR_CU(le, "hpsi_slab_kernel launch");
   }
   if (set.n_items > 0) {
-    p.items = set.items;
-    p.n_items = set.n_items;
-    p.slab_per_cta = (int64_t)(w.slab_per_cta_bytes / sizeof(T));
-    p.smem_elems = (int64_t)(w.smem_bytes / sizeof(T));
-    EVR_CU((p.gfly ? launch_items_kernel<T, true>(w.grid, w.smem_bytes, s, p)
-                   : launch_items_kernel<T, false>(w.grid, w.smem_bytes, s, p)),
+    ItemParams<T> pi = p;
+    pi.items = set.items;
+    pi.n_items = set.n_items;
+    pi.slab_per_cta = (int64_t)(w.slab_per_cta_bytes / sizeof(T));
+    pi.smem_elems = (int64_t)(w.smem_bytes / sizeof(T));
+    EVR_CU((p.gfly ? launch_items_kernel<T, true>(w.grid, w.smem_bytes, s, pi)
+                   : launch_items_kernel<T, false>(w.grid, w.smem_bytes, s, pi)),
            "hpsi_items_kernel launch");
+  }
+  if (set.n_small > 0) {
+    // small terms: the general kernel as kSmallCtas CTAs of kSmallThreads per SM, every
+    // item in shared memory (no global buffer)
+    ItemParams<T> pt = p;
+    pt.items = set.items_small;
+    pt.n_items = set.n_small;
+    pt.counter = w.counter + 3;
+    pt.slab = nullptr;
+    pt.slab_per_cta = 0;
+    pt.smem_elems = (int64_t)(w.smem_small_bytes / sizeof(T));
+    EVR_CU(cudaMemsetAsync(w.counter + 3, 0, sizeof(int), s), "memset counter");
+    EVR_CU((p.gfly ? launch_items_kernel<T, true>(w.grid_small, w.smem_small_bytes, s, pt, kSmallThreads)
+                   : launch_items_kernel<T, false>(w.grid_small, w.smem_small_bytes, s, pt, kSmallThreads)),
+           "hpsi_items_kernel launch (small CTAs)");
   }
   return EVR_OK;
 }
@@ -592,16 +714,13 @@ static int run_items(evr_ctx* c, const ItemSet& set, const double* x, int64_t ld
     if ((rc = launch_items<T>(c, set, c->dp.termsT, 1, (T*)(op == OP_HT ? w.ht : w.ht2), x, ldx, nvec, s, ex)))
       return rc;
   if (!c->capturing) EVR_CU(cudaEventRecord(c->ev[1], s), "event");
-  const int64_t N = P.Np * P.nb0;
-  int rblocks = (int)std::min<int64_t>((N * nvec + 255) / 256, (int64_t)c->num_sms * 16);
-  csr_reduce_kernel<T><<<rblocks, 256, 0, s>>>(c->dp.csr_ptr, c->dp.csr_src, c->dp.csr_w, (const T*)w.ht,
-                                                op == OP_HSYM ? (const T*)w.ht2 : nullptr, nvec,
-                                                op == OP_HSYM ? 0.5 : 1.0, y, ldy, N, nvec);
-  EVR_CU(cudaGetLastError(), "csr_reduce_kernel launch");
+  EVR_CU(launch_csr_reduce<T>(c, (const T*)w.ht, op == OP_HSYM ? (const T*)w.ht2 : nullptr, nvec,
+                               op == OP_HSYM ? 0.5 : 1.0, y, ldy, nvec, s),
+         "csr_reduce_kernel launch");
   if (!c->capturing) EVR_CU(cudaEventRecord(c->ev[2], s), "event");
-  const int per_op = (set.n_slab > 0 ? 1 : 0) + (set.n_items > 0 ? 1 : 0);
+  const int per_op = (set.n_slab > 0 ? 1 : 0) + (set.n_items > 0 ? 1 : 0) + (set.n_small > 0 ? 1 : 0);
   c->last_kernels = per_op * (op == OP_HSYM ? 2 : 1) + 1;
-  c->last_items = (int64_t)(set.n_items + set.n_slab) * (op == OP_HSYM ? 2 : 1);
+  c->last_items = (int64_t)(set.n_items + set.n_slab + set.n_small) * (op == OP_HSYM ? 2 : 1);
   return EVR_OK;
 }
 
@@ -622,32 +741,41 @@ int hpsi_interleaved(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_
   cp.n_items = set->n_items;
   cp.items_slab = set->items_slab;
   cp.n_slab = set->n_slab;
+  cp.items_small = set->items_small;
+  cp.n_small = set->n_small;
   if (!c->term_active.empty()) {
     // batches: only the terms of the active problems (host-synchronous, not for capture)
     if (c->capturing) return set_error(c, EVR_EINVAL, "filtered H.psi inside a stream capture");
     Workspace& w = c->ws;
-    const size_t need = std::max(set->h_items.size(), set->h_slab.size());
+    const size_t need = std::max({set->h_items.size(), set->h_slab.size(), set->h_small.size()});
     if (w.f_cap < need) {
       if (w.f_items) cudaFree(w.f_items);
       if (w.f_slab) cudaFree(w.f_slab);
-      w.f_items = w.f_slab = nullptr;
+      if (w.f_small) cudaFree(w.f_small);
+      w.f_items = w.f_slab = w.f_small = nullptr;
       w.f_cap = 0;
       EVR_CU(cudaMalloc((void**)&w.f_items, need * sizeof(WorkItem)), "cudaMalloc items");
       EVR_CU(cudaMalloc((void**)&w.f_slab, need * sizeof(WorkItem)), "cudaMalloc items");
+      EVR_CU(cudaMalloc((void**)&w.f_small, need * sizeof(WorkItem)), "cudaMalloc items");
       w.f_cap = need;
     }
-    std::vector<WorkItem> fi, fs;
+    std::vector<WorkItem> fi, fs, ft;
     for (const WorkItem& it : set->h_items)
       if (c->term_active[it.term]) fi.push_back(it);
     for (const WorkItem& it : set->h_slab)
       if (c->term_active[it.term]) fs.push_back(it);
+    for (const WorkItem& it : set->h_small)
+      if (c->term_active[it.term]) ft.push_back(it);
     EVR_CU(cudaStreamSynchronize(s), "sync");  // the previous launch may still read the lists
     if (!fi.empty()) EVR_CU(cudaMemcpy(w.f_items, fi.data(), fi.size() * sizeof(WorkItem), cudaMemcpyHostToDevice), "items");
     if (!fs.empty()) EVR_CU(cudaMemcpy(w.f_slab, fs.data(), fs.size() * sizeof(WorkItem), cudaMemcpyHostToDevice), "items");
+    if (!ft.empty()) EVR_CU(cudaMemcpy(w.f_small, ft.data(), ft.size() * sizeof(WorkItem), cudaMemcpyHostToDevice), "items");
     cp.items = w.f_items;
     cp.n_items = (int)fi.size();
     cp.items_slab = w.f_slab;
     cp.n_slab = (int)fs.size();
+    cp.items_small = w.f_small;
+    cp.n_small = (int)ft.size();
   }
   if (prec == EVR_PREC_FP32) return run_items<float>(c, cp, x, ldx, y, ldy, nvec, s, op, e);
   return run_items<double>(c, cp, x, ldx, y, ldy, nvec, s, op, e);
@@ -688,6 +816,7 @@ void clear_item_sets(evr_ctx* c) {
   for (ItemSet& st : c->ws.sets) {
     if (st.items) cudaFree(st.items);
     if (st.items_slab) cudaFree(st.items_slab);
+    if (st.items_small) cudaFree(st.items_small);
   }
   c->ws.sets.clear();
   ++c->ws_gen;
@@ -707,15 +836,11 @@ int check_item_bounds(evr_ctx* c) {
 
 int reduce_terms(evr_ctx* c, int prec, const void* ht, const void* ht2, int nvec, double scale, double* y,
                  int64_t ldy, cudaStream_t s) {
-  const int64_t N = c->hp.Np * c->hp.nb0;
-  const int rblocks = (int)std::min<int64_t>((N * nvec + 255) / 256, (int64_t)c->num_sms * 16);
-  if (prec == EVR_PREC_FP32)
-    csr_reduce_kernel<float><<<rblocks, 256, 0, s>>>(c->dp.csr_ptr, c->dp.csr_src, c->dp.csr_w, (const float*)ht,
-                                                      (const float*)ht2, nvec, scale, y, ldy, N, nvec);
-  else
-    csr_reduce_kernel<double><<<rblocks, 256, 0, s>>>(c->dp.csr_ptr, c->dp.csr_src, c->dp.csr_w, (const double*)ht,
-                                                       (const double*)ht2, nvec, scale, y, ldy, N, nvec);
-  return cuda_check(c, cudaGetLastError(), "csr_reduce_kernel launch");
+  const cudaError_t e = prec == EVR_PREC_FP32
+                            ? launch_csr_reduce<float>(c, (const float*)ht, (const float*)ht2, nvec, scale, y, ldy, nvec, s)
+                            : launch_csr_reduce<double>(c, (const double*)ht, (const double*)ht2, nvec, scale, y, ldy,
+                                                        nvec, s);
+  return cuda_check(c, e, "csr_reduce_kernel launch");
 }
 
 namespace {
@@ -773,7 +898,7 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
   // the general kernel's shared memory of the regular path, so that two CTAs are resident
   // per SM and every CTA of the grid gets its per-CTA buffer in the first wave
   int smem_items = 0, smem_slab[2] = {0, 0};
-  int rc0 = term_kernel_smem(c, &smem_items, smem_slab);
+  int rc0 = term_kernel_smem(c, &smem_items, smem_slab, nullptr);
   if (rc0) return rc0;
   // the same attribute values as ensure_workspace sets, so neither path lowers the other's
   EVR_CU((set_term_kernel_smem<double, false>(smem_items, smem_slab[EVR_PREC_FP64])), "attr");
@@ -829,11 +954,7 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
       for (int j = i + 1; j < P.D; ++j) p.has_offdiag |= (P.G0[i + (size_t)P.D * j] != 0.0);
   EVR_CU(cudaMemsetAsync(counter, 0, 4 * sizeof(int), s), "memset counter");  // the buffer keeps old contents
   EVR_CU((launch_items_kernel<double, false>(grid, smem_items, s, p)), "hpsi_items_kernel launch");
-  const int64_t N = P.Np * P.nb0;
-  int rblocks = (int)std::min<int64_t>((N * nvec + 255) / 256, (int64_t)c->num_sms * 16);
-  csr_reduce_kernel<double><<<rblocks, 256, 0, s>>>(c->dp.csr_ptr, c->dp.csr_src, c->dp.csr_w, ht, nullptr, nvec,
-                                                     1.0, y, ldy, N, nvec);
-  EVR_CU(cudaGetLastError(), "csr_reduce_kernel launch");
+  EVR_CU(launch_csr_reduce<double>(c, ht, nullptr, nvec, 1.0, y, ldy, nvec, s), "csr_reduce_kernel launch");
   // the kernel's buffer-check flag: a plain copy into a host int (no allocation)
   int flag = 0;
   EVR_CU(cudaMemcpyAsync(&flag, counter + 2, sizeof(int), cudaMemcpyDeviceToHost, s), "flag");
@@ -911,7 +1032,7 @@ extern "C" int evr_autotune(evr_ctx* c, int nvec, int prec, int* caps, double* b
   int bm = c->slab_min_points;
   if (!rc) {
     c->vt_cap_items = bi;
-    const int thr[] = {0, 1024, 4096, 16384};
+    const int thr[] = {0, 1024, kSmallTermPoints, 4096, 16384};
     for (int t : thr) {
       c->slab_min_points = t;
       double ms;
