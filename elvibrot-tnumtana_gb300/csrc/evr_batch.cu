@@ -573,6 +573,7 @@ static int upload_batch(evr_ctx* c) {
   if ((rc = upload_long_rows(c))) return rc;
   if ((rc = up((void**)&d.G0, P.G0.data(), P.G0.size() * sizeof(double)))) return rc;
   if ((rc = up((void**)&d.g, P.g.data(), P.g.size() * sizeof(double)))) return rc;
+  if ((rc = upload_coeffs32(c))) return rc;
   if ((rc = up((void**)&d.e0diag, P.e0diag.data(), P.e0diag.size() * sizeof(double)))) return rc;
   const int nb0 = P.nb0;
   const int64_t nv = P.sum_nq * nb0 * nb0;

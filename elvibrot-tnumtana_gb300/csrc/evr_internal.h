@@ -137,6 +137,8 @@ struct DeviceProblem {
   int64_t n_long = 0;
   double* G0 = nullptr;
   double* g = nullptr;
+  float* G0_32 = nullptr;           // FP32 copies of G0 and g (FP32 H.psi)
+  float* g32 = nullptr;
   double* mono_coef = nullptr;
   int* mono_idx = nullptr;
   int* mono_elec = nullptr;
@@ -267,6 +269,7 @@ void free_control(evr_ctx* c);
 void free_batch_info(evr_ctx* c);
 // weighted CSR reduction of the term-basis output(s) into y (evr_kernels.cu)
 int upload_long_rows(evr_ctx* c);
+int upload_coeffs32(evr_ctx* c);
 int reduce_terms(evr_ctx* c, int prec, const void* ht, const void* ht2, int nvec, double scale, double* y,
                  int64_t ldy, cudaStream_t s);
 // evaluates monomials (device arrays) on every term grid into out (sum_nq * nb0^2) and

@@ -243,6 +243,7 @@ int upload_problem(evr_ctx* c) {
   if ((rc = upload_long_rows(c))) return rc;
   if ((rc = upload(c, &d.G0, P.G0))) return rc;
   if ((rc = upload(c, &d.g, P.g))) return rc;
+  if ((rc = upload_coeffs32(c))) return rc;
   if ((rc = upload(c, &d.mono_coef, P.mono_coef))) return rc;
   if ((rc = upload(c, &d.mono_idx, P.mono_idx))) return rc;
   if ((rc = upload(c, &d.mono_elec, P.mono_elec))) return rc;
@@ -278,6 +279,21 @@ int upload_problem(evr_ctx* c) {
   return EVR_OK;
 }
 
+// FP32 copies of G0 and of the linear G model's g_ijk (read per grid point by FP32 H.psi)
+int upload_coeffs32(evr_ctx* c) {
+  DeviceProblem& d = c->dp;
+  const std::vector<double>* src[2] = {&c->hp.G0, &c->hp.g};
+  float** dst[2] = {&d.G0_32, &d.g32};
+  for (int a = 0; a < 2; ++a) {
+    std::vector<float> f(src[a]->begin(), src[a]->end());
+    if (*dst[a]) cudaFree(*dst[a]);
+    *dst[a] = nullptr;
+    EVR_CU(cudaMalloc((void**)dst[a], std::max<size_t>(f.size(), 1) * sizeof(float)), "cudaMalloc");
+    if (!f.empty()) EVR_CU(cudaMemcpy(*dst[a], f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice), "cudaMemcpy");
+  }
+  return EVR_OK;
+}
+
 // the rows of the weighted reduction with more than kCsrShortRow entries, on the device
 int upload_long_rows(evr_ctx* c) {
   const std::vector<int64_t>& ptr = c->hp.csr_ptr;
@@ -298,7 +314,7 @@ int upload_long_rows(evr_ctx* c) {
 void free_problem(evr_ctx* c) {
   DeviceProblem& d = c->dp;
   void* ptrs[] = {d.terms, d.termsT, d.mats, d.mats32, d.vgrid, d.vgrid32, d.map, d.csr_ptr, d.csr_src, d.csr_w,
-                  d.csr_long,
+                  d.csr_long, d.G0_32, d.g32,
                   d.G0, d.g, d.mono_coef, d.mono_idx, d.mono_elec, d.e0diag, c->dp_ggrid, c->dp_ggrid32,
                   c->dp_mugrid, c->dp_mugrid32, c->dp_jgrid, c->dp_jgrid32};
   for (void* p : ptrs)
@@ -629,6 +645,8 @@ static int launch_items(evr_ctx* c, const ItemSet& set, const TermDesc* terms, i
   p.jgrid = f32 ? (const T*)c->dp_jgrid32 : (const T*)c->dp_jgrid;
   p.keo_on = ex.keo;
   p.gco = c->dp.g;
+  p.G0t = f32 ? (const T*)c->dp.G0_32 : (const T*)c->dp.G0;
+  p.gcot = f32 ? (const T*)c->dp.g32 : (const T*)c->dp.g;
   p.gfly = c->gfly ? 1 : 0;
   p.err = w.counter + 2;
   if (ex.mw != 0.0 || ex.vw != 1.0 || ex.mu_dev) {
@@ -946,6 +964,7 @@ int hpsi_scratch(evr_ctx* c, const double* x, int64_t ldx, double* y, int64_t ld
   p.keo_type = P.keo_type;
   p.vtrans = 0;
   set_plain(p);
+  p.G0t = c->dp.G0;  // constant G (no G table); the no-alloc path has no G model
   p.jgrid = c->dp_jgrid;
   p.implicit_nvec = nvec;
   p.has_offdiag = 0;

@@ -36,6 +36,8 @@ struct ItemParams {
   const double* G0;        // D*D per problem, at the term's g0off (used when ggrid == nullptr)
   const double* gco;       // g_ijk per problem at the term's goff: G(Q) = G0 + g.Q evaluated per point
                            // (problems without a G table: gfly != 0)
+  const T* G0t;            // G0 and g_ijk in T, read per grid point (no FP64 conversions in FP32)
+  const T* gcot;
   int gfly;
   const int* map;
   const WorkItem* items;
@@ -75,6 +77,8 @@ template <typename T>
 void set_plain(ItemParams<T>& p) {
   p.mugrid = nullptr;
   p.gco = nullptr;
+  p.G0t = nullptr;
+  p.gcot = nullptr;
   p.gfly = 0;
   p.vw = T(1);
   p.mw = T(0);
@@ -467,31 +471,33 @@ __device__ __forceinline__ void stage_matrices(TermDesc& Tm, int D, const T* __r
 // fastest), the others left to the caller.
 template <typename T, int DM>
 __device__ __forceinline__ void point_coords(const ItemParams<T>& p, const TermDesc& Tm, int r, int npos,
-                                             double (&xq)[DM]) {
+                                             T (&xq)[DM]) {
 #pragma unroll
   for (int k = 0; k < DM; ++k)
     if (k < npos) {
       const int n = Tm.nq[k];
       const int i = r % n;
       r /= n;
-      xq[k] = (double)p.mats[Tm.m_x[k] + i];
+      xq[k] = p.mats[Tm.m_x[k] + i];
     } else {
-      xq[k] = 0.0;
+      xq[k] = T(0);
     }
 }
 
 // G_ij(Q) = G0_ij + sum_k g_ijk Q_k at a point with coordinates xq (positions i, j, k of the
-// term's mode order), for problems without a G table
+// term's mode order), for problems without a G table.  Evaluated in T from the T copies
+// of G0 and g: in FP32 H.psi the model then costs D FP32 FMAs per entry and no FP64
+// instruction (the GB300 FP64 pipe, and its conversions, issue at a small fraction of the
+// FP32 rate; FP64 arithmetic here dominated the FP32 batched H.psi)
 template <typename T, int DM>
-__device__ __forceinline__ T g_model(const ItemParams<T>& p, const TermDesc& Tm, const double (&xq)[DM], int i,
-                                     int j) {
+__device__ __forceinline__ T g_model(const ItemParams<T>& p, const TermDesc& Tm, const T (&xq)[DM], int i, int j) {
   const int D = Tm.D, Dp = Tm.Dp, oi = Tm.perm[i], oj = Tm.perm[j];
-  double s = __ldg(p.G0 + Tm.g0off + oi + Dp * oj);
-  const double* gp = p.gco + Tm.goff + oi + Dp * oj;
+  T s = __ldg(p.G0t + Tm.g0off + oi + Dp * oj);
+  const T* gp = p.gcot + Tm.goff + oi + Dp * oj;
 #pragma unroll
   for (int k = 0; k < DM; ++k)  // dropped 1-point modes sit at Q = 0
     if (k < D) s = fma(__ldg(gp + Dp * Dp * Tm.perm[k]), xq[k], s);
-  return (T)s;
+  return s;
 }
 
 // Phi_i = sum_j G_ij(Q) y_j for terms of more than 8 active positions (rare: levels above 8
@@ -510,23 +516,23 @@ __device__ __noinline__ void pointwise_G_wide(const ItemParams<T>& p, const Term
     const int pt = task / nch, ch = task - pt * nch;
     const int64_t r = r0 + pt;
     T G[kMaxD * (kMaxD + 1) / 2];
-    if (GFLY) {
-      double xq[kMaxD];
+    if (GFLY) {  // the linear model in T, as g_model
+      T xq[kMaxD];
       int rr = (int)r;
       for (int k = 0; k < D; ++k) {
         const int n = Tm.nq[k];
         const int i = rr % n;
         rr /= n;
-        xq[k] = (double)p.mats[Tm.m_x[k] + i];
+        xq[k] = p.mats[Tm.m_x[k] + i];
       }
       int s = 0;
       for (int i = 0; i < D; ++i)
         for (int j = i; j < D; ++j, ++s) {
           const int oi = Tm.perm[i], oj = Tm.perm[j];
-          double g = __ldg(p.G0 + Tm.g0off + oi + Tm.Dp * oj);
-          const double* gp = p.gco + Tm.goff + oi + Tm.Dp * oj;
+          T g = __ldg(p.G0t + Tm.g0off + oi + Tm.Dp * oj);
+          const T* gp = p.gcot + Tm.goff + oi + Tm.Dp * oj;
           for (int k = 0; k < D; ++k) g = fma(__ldg(gp + Tm.Dp * Tm.Dp * Tm.perm[k]), xq[k], g);
-          G[s] = (T)g;
+          G[s] = g;
         }
     } else if (p.ggrid) {
       const T* Gp = p.ggrid + (Tm.off_nq + r) * nG;
@@ -534,7 +540,7 @@ __device__ __noinline__ void pointwise_G_wide(const ItemParams<T>& p, const Term
     } else {
       int s = 0;
       for (int i = 0; i < D; ++i)
-        for (int j = i; j < D; ++j, ++s) G[s] = (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]);
+        for (int j = i; j < D; ++j, ++s) G[s] = __ldg(p.G0t + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]);
     }
     const T jq = jac ? jac[2 * r] : T(1);
     for (int v = ch; v < Vt; v += nch) {
@@ -576,12 +582,12 @@ __device__ __forceinline__ void items_pointwise_G(const ItemParams<T>& p, const 
   for (int task = threadIdx.x; task < NQ * nch; task += blockDim.x) {
     const int q = task / nch, ch = task - q * nch;
     const T* Gp = p.ggrid ? p.ggrid + (Tm.off_nq + q) * nG : nullptr;
-    double xq[DM];
+    T xq[DM];
     if constexpr (GFLY) point_coords<T, DM>(p, Tm, q, D, xq);
     auto gget = [&](int i, int j) -> T {
       if (i >= D || j >= D) return T(0);
       if constexpr (GFLY) return g_model<T, DM>(p, Tm, xq, i, j);
-      return Gp ? __ldg(Gp + slot(i, j)) : (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]);
+      return Gp ? __ldg(Gp + slot(i, j)) : __ldg(p.G0t + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]);
     };
     T G[kG];
     if constexpr (kCache) {
@@ -941,19 +947,19 @@ __device__ __forceinline__ void slab_pointwise_G(const ItemParams<T>& p, const T
     const int pt = task / nch, ch = task - pt * nch;
     T G[kG];
     const T* Gp = p.ggrid ? p.ggrid + (Tm.off_nq + (int64_t)q * NQs + pt) * nG : nullptr;
-    double xq[DM];
+    T xq[DM];
     if constexpr (GFLY) {
       point_coords<T, DM>(p, Tm, pt, L, xq);
 #pragma unroll
       for (int k = 0; k < DM; ++k)
-        if (k == L) xq[k] = (double)p.mats[Tm.m_x[k] + q];
+        if (k == L) xq[k] = p.mats[Tm.m_x[k] + q];
     }
     // packed slot of (i, j), i <= j < D, in the table's order
     auto slot = [D](int i, int j) { return i * D - i * (i - 1) / 2 + (j - i); };
     auto gload = [&](int i, int j) -> T {
       if (i >= D || j >= D) return T(0);
       if constexpr (GFLY) return g_model<T, DM>(p, Tm, xq, i, j);
-      return Gp ? __ldg(Gp + slot(i, j)) : (T)__ldg(p.G0 + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]);
+      return Gp ? __ldg(Gp + slot(i, j)) : __ldg(p.G0t + Tm.g0off + Tm.perm[i] + Tm.Dp * Tm.perm[j]);
     };
     if constexpr (kCache) {
       if (!GFLY && Gp && D == DM) {
