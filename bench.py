@@ -195,8 +195,9 @@ def run_reference(args):
 
 def run_profile(args):
     """A handful of H.psi launches (FP64 then FP32) for ncu captures: D=6 Smolyak level 6
-    (small case) or level 8 (the benchmark workload) on 64 vectors, or the D=3 direct
-    product (stage kernels) on 16 vectors."""
+    (small case) or level 8 (the benchmark workload) on 64 vectors, the D=3 direct
+    product (stage kernels) on 16 vectors, or the D=12 level-6 propagation workload on the
+    two vectors of one complex packet."""
     import torch
     from evrgpu import Problem, spec as S
     import evrgpu.lib as E
@@ -204,6 +205,8 @@ def run_profile(args):
     nvec = NVEC
     if args.profile == "dp3":  # direct product D=3 nb=20 nq=24: the stage kernels, 16 vectors
         spec, nvec = S.config_dp3(), 16
+    elif args.profile == "sg4_12d_l6":  # the propagation workload: one complex packet, 2 vectors
+        spec, nvec = S.config_sg4_12d_l6(), 2
     else:
         spec = S.config_sg4(6, 6, seed=1) if args.profile == "sg4_6d_l6" else S.config_sg4_6d_l8()
     p = Problem(spec, device=0)
@@ -457,7 +460,7 @@ def main():
     ap.add_argument("--no-davidson", action="store_true", help="skip the Davidson time-to-tolerance legs")
     ap.add_argument("--no-configs", action="store_true", help="skip the other workloads' compact results")
     ap.add_argument("--autotune", action="store_true", help="tune the work decomposition before timing")
-    ap.add_argument("--profile", default=None, choices=["sg4_6d_l6", "sg4_6d_l8", "dp3"],
+    ap.add_argument("--profile", default=None, choices=["sg4_6d_l6", "sg4_6d_l8", "dp3", "sg4_12d_l6"],
                     help="profiling mode: a few H.psi launches of the named workload, nothing else")
     ap.add_argument("--prec", default="both", choices=["both", "fp64", "fp32"], help="precision(s) in profiling mode")
     ap.add_argument("--tc", action="store_true", help="profiling mode: FP32 contractions on the tensor cores")
