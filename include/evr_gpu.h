@@ -234,8 +234,9 @@ int evr_tc_selftest(int device, int A, int K, int M, int B, int Vt, const float 
 /* Autotuner (no counterpart in the reference; its Tune_SG4threads_HPsi, vib.f90:1598-1705,
  * tunes OpenMP thread counts): times the term kernels on an nvec-vector block for each
  * cap of the vector tile of a work item (2..32, slab kernel then general kernel) and for
- * the size below which a term runs in the general kernel, and keeps the fastest for later
- * calls; with EVR_PREC_FP32 also whether the slab kernel's contractions run on the tensor
+ * the size (grid points x vector tile, default 2048) below which a term runs in the general
+ * kernel (as eight 64-thread CTAs per SM when its buffers fit one), and keeps the fastest
+ * for later calls; with EVR_PREC_FP32 also whether the slab kernel's contractions run on the tensor
  * cores and from which size K*M (evr_set_tensor_cores).  caps[4] (optional): slab cap,
  * general cap, size threshold, tensor-core threshold (-1: CUDA cores); best_ms: the time. */
 int evr_autotune(evr_ctx *ctx, int nvec, int prec, int *caps, double *best_ms);
