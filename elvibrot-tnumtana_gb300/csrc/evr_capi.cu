@@ -322,10 +322,11 @@ int evr_set_jacobian(evr_ctx* c, const double* jac, const double* rho) {
 int evr_set_kernel_path(evr_ctx* c, int path) {
   if (!c) return EVR_EINVAL;
   if (path < 0 || path > 2) return set_error(c, EVR_EINVAL, "evr_set_kernel_path: 0, 1 or 2");
-  const bool slab = path >= 1, stages = path == 1;
-  if (c->use_slab != slab || c->use_stages != stages) {
+  const bool slab = path >= 1, stages = path == 1, all = path == 2;
+  if (c->use_slab != slab || c->use_stages != stages || c->slab_all != all) {
     c->use_slab = slab;
     c->use_stages = stages;
+    c->slab_all = all;
     if (!c->host_only) {
       cudaSetDevice(c->device);
       cudaStreamSynchronize(c->stream);

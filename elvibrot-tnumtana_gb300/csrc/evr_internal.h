@@ -207,6 +207,7 @@ struct evr_ctx {
   int op_form = 0;                  // EVR_OP_H, EVR_OP_HT or EVR_OP_HSYM
   bool capturing = false;           // inside a stream capture: no event records
   bool use_slab = true;             // slab kernel for the terms that fit (evr_set_kernel_path)
+  bool slab_all = false;            // path 2: small terms too (no small-term routing)
   bool use_tc = false;              // FP32 slab-kernel contractions on the tensor cores (evr_set_tensor_cores;
                                     // off by default: slower than the CUDA cores at these sizes, see evr_autotune)
   int tc_min_km = 64;               // contractions with K*M below this stay on the CUDA cores

@@ -487,7 +487,7 @@ int ensure_workspace(evr_ctx* c, int nvec, int prec) {
     if (Tm.weight == 0.0) continue;
     const size_t mats = (size_t)((Tm.msz + 3) & ~3) * esz;  // staged 1-D matrices
     if (mats > (size_t)w.smem_bytes) return set_error(c, EVR_EINVAL, "1-D matrices exceed shared memory");
-    const bool small = (int64_t)Tm.NQ * std::min(nvec, c->vt_cap_slab) < c->slab_min_points;
+    const bool small = !c->slab_all && (int64_t)Tm.NQ * std::min(nvec, c->vt_cap_slab) < c->slab_min_points;
     if (small) {
       // the general kernel as small CTAs when the term's buffers and matrices fit one
       const size_t fp1 = footprint_elems<double>(P, Tm, 1) * esz;

@@ -528,8 +528,9 @@ class Problem:
         return int(caps[0]), int(caps[1]), int(caps[2]), float(ms[0])
 
     def set_kernel_path(self, path):
-        """1 or True (default): stage kernels for single-term problems, else the slab kernel
-        for the terms that fit and the general kernel for the rest; 2: the same without the
+        """1 or True (default): stage kernels for single-term problems, else small terms in the
+        general kernel, the slab kernel for the other terms that fit and the general kernel
+        for the rest; 2: the slab kernel for every term that fits (small ones included), no
         stage kernels; 0 or False: general kernel only.  Names "auto", "slab", "general" work too."""
         names = {"auto": 1, "stages": 1, "slab": 2, "general": 0}
         v = names[path] if isinstance(path, str) else (1 if path is True else 0 if path is False else int(path))

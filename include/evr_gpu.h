@@ -189,10 +189,12 @@ int evr_hpsi_device(evr_ctx *ctx, const double *psi, int64_t ld_psi, double *hps
 int evr_set_operator(evr_ctx *ctx, int form);
 
 /* Kernel path of evr_hpsi_*: 1 (default) runs a problem of a single term (a direct
- * product basis) on the grid-wide stage kernels, and otherwise every term whose slab
+ * product basis) on the grid-wide stage kernels, and otherwise the small terms (below the
+ * size threshold of evr_autotune) in the general kernel, every other term whose slab
  * pipeline fits one CTA's shared memory in the slab-streaming kernel and the rest in the
- * general kernel; 2 is path 1 without the stage kernels; 0 runs every term in the general
- * kernel.  All compute the same operator. */
+ * general kernel; 2 runs every term whose slab pipeline fits in the slab-streaming kernel,
+ * small ones included, and the rest in the general kernel, without the stage kernels; 0
+ * runs every term in the general kernel.  All compute the same operator. */
 int evr_set_kernel_path(evr_ctx *ctx, int path);
 
 /* Tensor cores for the FP32 path (no counterpart in the reference): on != 0 runs the mode
