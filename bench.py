@@ -361,8 +361,11 @@ def bench_prop12d(args):
         out["autotune"] = p.autotune(nvec=2, prec="fp64")
     e0 = float(np.vdot(psi0, p.hpsi(psi0.real[:, None])[:, 0]).real)  # psi0 is real
     ac, fin = {}, {}
-    steps = args.prop_steps
-    for key, prec, tc in (("fp64", "fp64", False), ("fp32", "fp32", False), ("fp32_tensor_cores", "fp32", True)):
+    # the plain FP64 form runs the workload's 2000 steps; the FP32 legs run prop_steps (their
+    # norm drifts by about 7e-4 over 2000 steps, close to the 1e-3 guard of the FP32 form)
+    full, steps32 = 2000, args.prop_steps
+    for key, prec, tc, steps in (("fp64", "fp64", False, full), ("fp32", "fp32", False, steps32),
+                                 ("fp32_tensor_cores", "fp32", True, steps32)):
         p.set_tensor_cores(tc, 64)
         p.chebyshev(psi0, 10.0, 2, emin, emax, prec=prec)
         t0 = time.perf_counter()
@@ -374,15 +377,17 @@ def bench_prop12d(args):
         hx = p.hpsi(np.stack([x.real, x.imag], axis=1))
         en = float((np.vdot(x.real, hx[:, 0]) + np.vdot(x.imag, hx[:, 1])).real / np.vdot(x, x).real)
         out[key] = {"steps": steps, "s": dt, "s_per_step": dt / steps, "order": st["max_order"],
-                    "norm_final_minus_1": float(np.vdot(x, x).real - 1.0), "energy_drift_au": en - e0,
-                    "s_2000_steps_extrapolated": 2000 * dt / steps}
+                    "norm_final_minus_1": float(np.vdot(x, x).real - 1.0), "energy_drift_au": en - e0}
+        if steps < full:
+            out[key]["s_2000_steps_extrapolated"] = full * dt / steps
     p.set_tensor_cores(False)
-    out["autocorr_max_abs_diff_fp32_vs_fp64"] = float(np.abs(ac["fp32"] - ac["fp64"]).max())
+    n32 = len(ac["fp32"])  # the FP32 legs against the first n32 values of the FP64 series
+    out["autocorr_max_abs_diff_fp32_vs_fp64"] = float(np.abs(ac["fp32"] - ac["fp64"][:n32]).max())
     out["autocorr_max_abs_diff_fp32_tensor_cores_vs_fp64"] = float(
-        np.abs(ac["fp32_tensor_cores"] - ac["fp64"]).max())
+        np.abs(ac["fp32_tensor_cores"] - ac["fp64"][:n32]).max())
     out["autocorr_last"] = [float(ac["fp64"][-1].real), float(ac["fp64"][-1].imag)]
-    out["note"] = (f"timed on {steps} of the workload's 2000 steps; s_2000_steps_extrapolated = "
-                   f"2000 x measured s per step")
+    out["note"] = (f"fp64 timed on all {full} steps; the FP32 legs on {steps32} of them, "
+                   f"s_2000_steps_extrapolated = {full} x measured s per step")
     return out
 
 
@@ -471,7 +476,8 @@ def main():
     ap.add_argument("--batch-tol", type=float, default=1e-7, help="residual tolerance of the batch Davidson (au)")
     ap.add_argument("--batch-check", action="store_true",
                     help="also solve the batch in FP64 at 1/100 of the tolerance and compare both against it")
-    ap.add_argument("--prop-steps", type=int, default=200, help="time steps timed in the propagation workload")
+    ap.add_argument("--prop-steps", type=int, default=200,
+                    help="time steps timed in the FP32 legs of the propagation workload (FP64: all 2000)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
